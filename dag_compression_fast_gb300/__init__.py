@@ -1,0 +1,434 @@
+"""dag_compression_fast_gb300: GB300-native sparse voxel DAG compression.
+
+Python mirror of the reference's DAGCompression namespace
+(src/DAGCompression.h:42-49 of Phyronnaz/DAG_Compression_Fast) over the dagc
+C ABI (include/dagc.h):
+
+    CreateDAG(Fragments, Depth)  -> Context.create_dag(fragments, depth)
+    MergeDAGs(CpuDags)           -> Context.merge_dags(dags)
+    CreateFinalDAG(CpuDag)       -> Context.create_final_dag(dag)
+    FreeAll()                    -> Context.free_all()
+
+Where the reference aborts (CUDA error, failed check) this module raises
+DagcError carrying the library status. All compression runs in the native
+library; if it has not been built this module refuses to import.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "_lib")
+LIBDAGC_PATH = os.path.join(LIB_DIR, "libdagc.so")
+LIBGEN_PATH = os.path.join(LIB_DIR, "libdagc_gen.so")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_OUT_OF_MEMORY = 2
+ERR_BAD_INPUT = 3
+ERR_HASH_COLLISION = 4
+ERR_DEVICE_TIMEOUT = 5
+ERR_CUDA = 6
+ERR_TOO_LARGE = 7
+
+# Every symbol of include/dagc.h, in declaration order.
+DAGC_SYMBOLS = [
+    "dagc_context_create", "dagc_context_destroy", "dagc_last_error", "dagc_status_string",
+    "dagc_version", "dagc_create", "dagc_dag_num_levels", "dagc_dag_level_size",
+    "dagc_dag_num_leaves", "dagc_dag_level_device", "dagc_dag_leaves_device",
+    "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_free",
+    "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
+    "dagc_compress_host",
+    "dagc_compress", "dagc_last_counts", "dagc_sort_keys", "dagc_sort_pairs",
+]
+GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
+               "dagc_gen_triangle_soup", "dagc_gen_batched"]
+
+
+class DagcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"dagc status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+def _load(path: str) -> ctypes.CDLL:
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build the native library first "
+            "(python -m dag_compression_fast_gb300.build)")
+    return ctypes.CDLL(path)
+
+
+_lib = None
+_gen = None
+
+
+def lib() -> ctypes.CDLL:
+    """The dagc CUDA library (loaded on first use)."""
+    global _lib
+    if _lib is None:
+        L = _load(LIBDAGC_PATH)
+        vp, u64, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+        pvp = ctypes.POINTER(ctypes.c_void_p)
+        pu64 = ctypes.POINTER(u64)
+        L.dagc_context_create.argtypes = [i32, pvp]
+        L.dagc_context_destroy.argtypes = [vp]
+        L.dagc_context_destroy.restype = None
+        L.dagc_last_error.argtypes = [vp]
+        L.dagc_last_error.restype = ctypes.c_char_p
+        L.dagc_status_string.argtypes = [i32]
+        L.dagc_status_string.restype = ctypes.c_char_p
+        L.dagc_create.argtypes = [vp, vp, u64, i32, vp, pvp]
+        L.dagc_dag_num_levels.argtypes = [vp, ctypes.POINTER(i32)]
+        L.dagc_dag_level_size.argtypes = [vp, i32, pu64]
+        L.dagc_dag_num_leaves.argtypes = [vp, pu64]
+        L.dagc_dag_level_device.argtypes = [vp, i32, pvp, pvp, pvp]
+        L.dagc_dag_leaves_device.argtypes = [vp, pvp]
+        L.dagc_dag_download_level.argtypes = [vp, i32, vp, vp, vp]
+        L.dagc_dag_download_leaves.argtypes = [vp, vp]
+        L.dagc_dag_upload.argtypes = [vp, i32, vp, vp, vp, vp, vp, u64, vp, pvp]
+        L.dagc_dag_free.argtypes = [vp]
+        L.dagc_dag_free.restype = None
+        L.dagc_merge.argtypes = [vp, vp, u64, vp, pvp]
+        L.dagc_final.argtypes = [vp, vp, vp, pvp, pu64]
+        L.dagc_free_words.argtypes = [vp, vp, vp]
+        L.dagc_words_download.argtypes = [vp, vp, u64, vp]
+        L.dagc_free_all.argtypes = [vp]
+        L.dagc_compress_host.argtypes = [vp, vp, u64, i32, vp, vp, u64, pu64]
+        L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
+        L.dagc_last_counts.argtypes = [vp, pu64, i32]
+        L.dagc_sort_keys.argtypes = [vp, vp, vp, u64, i32, i32, vp]
+        L.dagc_sort_pairs.argtypes = [vp, vp, vp, vp, vp, u64, i32, i32, vp]
+        _lib = L
+    return _lib
+
+
+def gen_lib() -> ctypes.CDLL:
+    """The host-only synthetic fragment generators."""
+    global _gen
+    if _gen is None:
+        G = _load(LIBGEN_PATH)
+        vp, u64, i32, dbl = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_double
+        G.dagc_gen_free.argtypes = [vp]
+        G.dagc_gen_free.restype = None
+        G.dagc_gen_sphere_shell.argtypes = [i32, u64, dbl, vp, vp]
+        G.dagc_gen_terrain.argtypes = [i32, u64, dbl, vp, vp]
+        G.dagc_gen_triangle_soup.argtypes = [i32, u64, u64, i32, vp, vp]
+        G.dagc_gen_batched.argtypes = [i32, i32, i32, u64, dbl, dbl, i32, vp, vp, vp, vp, vp]
+        _gen = G
+    return _gen
+
+
+def _np_ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a.size else None
+
+
+def _stream_handle(stream):
+    """cudaStream_t as an integer: None -> the current torch stream."""
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+@dataclass
+class HostDag:
+    """Host copy of an FCpuDag (src/DAGCompression.h:12-40): per level (root
+    first) child masks, children (n, 8) and ascending hashes, plus leaves."""
+
+    masks: list = field(default_factory=list)
+    children: list = field(default_factory=list)
+    hashes: list = field(default_factory=list)
+    leaves: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint64))
+
+    @property
+    def num_levels(self) -> int:
+        return len(self.masks)
+
+    def level_sizes(self):
+        return [int(h.size) for h in self.hashes]
+
+
+class Dag:
+    """A device-resident DAG (the FCpuDag equivalent kept in HBM)."""
+
+    def __init__(self, ctx: "Context", handle: int):
+        self.ctx = ctx
+        self.handle = handle
+
+    def _live(self):
+        if not self.handle:
+            raise DagcError(ERR_INVALID_ARGUMENT, "DAG was consumed or freed")
+        return self.handle
+
+    @property
+    def num_levels(self) -> int:
+        n = ctypes.c_int(0)
+        self.ctx._check(lib().dagc_dag_num_levels(self._live(), ctypes.byref(n)))
+        return n.value
+
+    def level_sizes(self):
+        out = []
+        for l in range(self.num_levels):
+            n = ctypes.c_uint64(0)
+            self.ctx._check(lib().dagc_dag_level_size(self._live(), l, ctypes.byref(n)))
+            out.append(n.value)
+        return out
+
+    @property
+    def num_leaves(self) -> int:
+        n = ctypes.c_uint64(0)
+        self.ctx._check(lib().dagc_dag_num_leaves(self._live(), ctypes.byref(n)))
+        return n.value
+
+    def to_host(self) -> HostDag:
+        """FGpuLevel::ToCPU for every level plus the leaves."""
+        d = HostDag()
+        for l, n in enumerate(self.level_sizes()):
+            m = np.zeros(n, np.uint8)
+            c = np.zeros((n, 8), np.uint32)
+            h = np.zeros(n, np.uint64)
+            self.ctx._check(lib().dagc_dag_download_level(self._live(), l, _np_ptr(m), _np_ptr(c), _np_ptr(h)))
+            d.masks.append(m)
+            d.children.append(c)
+            d.hashes.append(h)
+        d.leaves = np.zeros(self.num_leaves, np.uint64)
+        self.ctx._check(lib().dagc_dag_download_leaves(self._live(), _np_ptr(d.leaves)))
+        return d
+
+    def free(self):
+        if self.handle:
+            lib().dagc_dag_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Words:
+    """The final uint32 DAG (device memory owned by the caller)."""
+
+    def __init__(self, ctx: "Context", ptr: int, n: int):
+        self.ctx = ctx
+        self.ptr = ptr
+        self.n = n
+
+    def to_numpy(self) -> np.ndarray:
+        out = np.zeros(self.n, np.uint32)
+        if self.n:
+            self.ctx._check(lib().dagc_words_download(self.ctx.handle, self.ptr, self.n, _np_ptr(out)))
+        return out
+
+    def free(self):
+        if self.ptr:
+            lib().dagc_free_words(self.ctx.handle, self.ptr, None)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _device_u64(fragments, device: int):
+    """(pointer, count, keepalive) for a uint64 fragment array on the device."""
+    import torch
+    if isinstance(fragments, torch.Tensor):
+        t = fragments
+        if t.dtype not in (torch.int64, torch.uint64):
+            raise DagcError(ERR_INVALID_ARGUMENT, "fragments must be 64-bit")
+        if not t.is_cuda:
+            t = t.to(f"cuda:{device}")
+        t = t.contiguous()
+        return t.data_ptr(), t.numel(), t
+    a = np.ascontiguousarray(fragments, dtype=np.uint64)
+    t = torch.from_numpy(a.view(np.int64)).to(f"cuda:{device}")
+    return t.data_ptr(), t.numel(), t
+
+
+class Context:
+    """One dagc context (device scratch arena + DAG memory pool)."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        h = ctypes.c_void_p()
+        st = lib().dagc_context_create(device, ctypes.byref(h))
+        if st:
+            raise DagcError(st, "dagc_context_create failed")
+        self.handle = h.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().dagc_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st:
+            msg = lib().dagc_last_error(self.handle).decode(errors="replace")
+            raise DagcError(st, msg)
+
+    # ------------------------------------------------------------ API ----
+    def create_dag(self, fragments, depth: int, stream=None) -> Dag:
+        """DAGCompression::CreateDAG: fragments (device tensor or host array of
+        uint64 Morton codes) -> device-resident DAG with depth-2 levels."""
+        ptr, n, keep = _device_u64(fragments, self.device)
+        out = ctypes.c_void_p()
+        st = lib().dagc_create(self.handle, ptr, n, depth, _stream_handle(stream), ctypes.byref(out))
+        del keep
+        self._check(st)
+        return Dag(self, out.value)
+
+    def merge_dags(self, dags, stream=None) -> Dag:
+        """DAGCompression::MergeDAGs: 8^m sub-DAGs in Morton order -> one DAG
+        with m more levels. Consumes the inputs."""
+        arr = (ctypes.c_void_p * len(dags))(*[d._live() for d in dags])
+        out = ctypes.c_void_p()
+        st = lib().dagc_merge(self.handle, arr, len(dags), _stream_handle(stream), ctypes.byref(out))
+        self._check(st)
+        for i, d in enumerate(dags):
+            d.handle = arr[i]  # consumed inputs come back as NULL
+        return Dag(self, out.value)
+
+    def create_final_dag(self, dag: Dag, stream=None) -> Words:
+        """DAGCompression::CreateFinalDAG: consumes the DAG, returns the uint32 words."""
+        ptr = ctypes.c_void_p()
+        n = ctypes.c_uint64(0)
+        st = lib().dagc_final(self.handle, dag._live(), _stream_handle(stream), ctypes.byref(ptr), ctypes.byref(n))
+        self._check(st)
+        dag.handle = None
+        return Words(self, ptr.value or 0, n.value)
+
+    def compress(self, fragments, depth: int, stream=None) -> Words:
+        """CreateDAG + CreateFinalDAG in one call."""
+        ptr, n, keep = _device_u64(fragments, self.device)
+        wp = ctypes.c_void_p()
+        nw = ctypes.c_uint64(0)
+        st = lib().dagc_compress(self.handle, ptr, n, depth, _stream_handle(stream), ctypes.byref(wp), ctypes.byref(nw))
+        del keep
+        self._check(st)
+        return Words(self, wp.value or 0, nw.value)
+
+    def compress_host(self, fragments: np.ndarray, depth: int, stream=None) -> np.ndarray:
+        """Host fragments -> host words through dagc_compress_host."""
+        a = np.ascontiguousarray(fragments, dtype=np.uint64)
+        nw = ctypes.c_uint64(0)
+        sh = _stream_handle(stream)
+        self._check(lib().dagc_compress_host(self.handle, _np_ptr(a), a.size, depth, sh, None, 0, ctypes.byref(nw)))
+        out = np.zeros(nw.value, np.uint32)
+        self._check(lib().dagc_compress_host(self.handle, _np_ptr(a), a.size, depth, sh, _np_ptr(out), out.size,
+                                             ctypes.byref(nw)))
+        return out
+
+    def upload_dag(self, host: HostDag, stream=None) -> Dag:
+        """FGpuLevel::FromCPU for every level: a host DAG -> device DAG."""
+        nl = host.num_levels
+        sizes = np.array(host.level_sizes(), np.uint64)
+        ms = [np.ascontiguousarray(m, np.uint8) for m in host.masks]
+        cs = [np.ascontiguousarray(c, np.uint32) for c in host.children]
+        hs = [np.ascontiguousarray(h, np.uint64) for h in host.hashes]
+        mp = (ctypes.c_void_p * max(nl, 1))(*[m.ctypes.data for m in ms])
+        cp = (ctypes.c_void_p * max(nl, 1))(*[c.ctypes.data for c in cs])
+        hp = (ctypes.c_void_p * max(nl, 1))(*[h.ctypes.data for h in hs])
+        leaves = np.ascontiguousarray(host.leaves, np.uint64)
+        out = ctypes.c_void_p()
+        st = lib().dagc_dag_upload(self.handle, nl, _np_ptr(sizes), mp, cp, hp, _np_ptr(leaves), leaves.size,
+                                   _stream_handle(stream), ctypes.byref(out))
+        self._check(st)
+        return Dag(self, out.value)
+
+    def free_all(self):
+        """DAGCompression::FreeAll."""
+        self._check(lib().dagc_free_all(self.handle))
+
+    def last_counts(self):
+        buf = (ctypes.c_uint64 * 64)()
+        k = lib().dagc_last_counts(self.handle, buf, 64)
+        return [int(buf[i]) for i in range(k)]
+
+    def sort_keys(self, keys, lo_bit: int = 0, hi_bit: int = 64, stream=None):
+        import torch
+        ptr, n, t = _device_u64(keys, self.device)
+        out = torch.empty_like(t)
+        self._check(lib().dagc_sort_keys(self.handle, ptr, out.data_ptr(), n, lo_bit, hi_bit, _stream_handle(stream)))
+        return out
+
+    def sort_pairs(self, keys, values=None, lo_bit: int = 0, hi_bit: int = 64, stream=None):
+        import torch
+        ptr, n, t = _device_u64(keys, self.device)
+        kout = torch.empty_like(t)
+        vout = torch.empty(n, dtype=torch.int32, device=t.device)
+        vin = None
+        if values is not None:
+            values = values.to(t.device).contiguous()
+            vin = values.data_ptr()
+        self._check(lib().dagc_sort_pairs(self.handle, ptr, kout.data_ptr(), vin, vout.data_ptr(), n, lo_bit, hi_bit,
+                                          _stream_handle(stream)))
+        return kout, vout
+
+
+# ---------------------------------------------------------------- inputs ----
+def _gen_call(fn, *args) -> np.ndarray:
+    out = ctypes.POINTER(ctypes.c_uint64)()
+    n = ctypes.c_uint64(0)
+    st = fn(*args, ctypes.byref(out), ctypes.byref(n))
+    if st:
+        raise DagcError(ERR_INVALID_ARGUMENT, f"generator failed ({st})")
+    try:
+        return np.ctypeslib.as_array(out, (n.value,)).copy() if n.value else np.zeros(0, np.uint64)
+    finally:
+        gen_lib().dagc_gen_free(out)
+
+
+def gen_sphere_shell(depth: int = 7, seed: int = 0xDA6C0DE, target_fragments: float = 0.0) -> np.ndarray:
+    return _gen_call(gen_lib().dagc_gen_sphere_shell, depth, seed, float(target_fragments))
+
+
+def gen_terrain(depth: int = 11, seed: int = 0xDA6C0DE + 1, column_fraction: float = 1.0) -> np.ndarray:
+    return _gen_call(gen_lib().dagc_gen_terrain, depth, seed, float(column_fraction))
+
+
+def gen_triangle_soup(depth: int = 13, seed: int = 0xDA6C0DE + 2, num_triangles: int = 2_000_000,
+                      threads: int = 0) -> np.ndarray:
+    threads = threads or (os.cpu_count() or 1)
+    return _gen_call(gen_lib().dagc_gen_triangle_soup, depth, seed, num_triangles, threads)
+
+
+def gen_batched(chunk_depth: int = 10, grid_xz: int = 16, chunk_row: int = 7, seed: int = 0xDA6C0DE + 3,
+                min_fragments: float = 1e4, max_fragments: float = 8e6, threads: int = 0):
+    """(codes, counts, chunk_morton): chunk-local codes concatenated in chunk Morton order."""
+    threads = threads or (os.cpu_count() or 1)
+    G = gen_lib()
+    P = ctypes.POINTER(ctypes.c_uint64)
+    codes, counts, morton = P(), P(), P()
+    total, k = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    st = G.dagc_gen_batched(chunk_depth, grid_xz, chunk_row, seed, float(min_fragments), float(max_fragments),
+                            threads, ctypes.byref(codes), ctypes.byref(total), ctypes.byref(counts),
+                            ctypes.byref(morton), ctypes.byref(k))
+    if st:
+        raise DagcError(ERR_INVALID_ARGUMENT, f"batched generator failed ({st})")
+    try:
+        c = np.ctypeslib.as_array(codes, (total.value,)).copy() if total.value else np.zeros(0, np.uint64)
+        n = np.ctypeslib.as_array(counts, (k.value,)).copy()
+        m = np.ctypeslib.as_array(morton, (k.value,)).copy()
+        return c, n, m
+    finally:
+        G.dagc_gen_free(codes)
+        G.dagc_gen_free(counts)
+        G.dagc_gen_free(morton)

@@ -1,0 +1,539 @@
+// DAG construction kernels for sm_103a: fused fragment-unique + leaf build,
+// level extract + node hash, hash-run unique with a full-compare collision
+// check, and the final word layout. Each is a persistent kernel over
+// 2048-item tiles taken in order from an atomic counter, with a single-value
+// decoupled look-back (bounded waits) for its compaction offsets, so counts
+// never leave the device.
+//
+// Reference steps replaced (src/DAGCompression.cu):
+//   SelectUnique :396-422 + leaf ReduceByKey :424-463 at :1035-1068 -> leaf_build
+//   ExtractLevel :916-974 + ComputeHashes :827-833 / HashChildren :765-774 -> extract_level
+//   SortLevel's flags/scan/scatters :886-913 -> unique_runs
+//   ComputeChildPositions :834-844 + WriteTo :845-861 + leaf copy :1597 -> final_*
+
+#include "dagc_device.cuh"
+#include "dagc_kernels.h"
+
+#include <algorithm>
+
+namespace dagc {
+namespace {
+
+constexpr int kT = kScanThreads;  // 256
+constexpr int kI = kScanItems;    // 8 items per thread (blocked)
+constexpr int kTile = kScanTile;  // 2048
+// Padded shared index for blocked access of 64-bit items: one pad word per 8.
+__device__ __forceinline__ int pad8(int i) { return i + (i >> 3); }
+constexpr int kPadded = kTile + kTile / 8;
+
+__device__ __forceinline__ uint64_t load_count(const uint64_t* d_n, uint64_t n) { return d_n ? *d_n : n; }
+
+// Takes the next tile id for the CTA (thread 0 fetches, all threads read).
+__device__ __forceinline__ uint32_t next_tile(uint32_t* counter, uint32_t* s_slot) {
+    if (threadIdx.x == 0) *s_slot = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t t = *s_slot;
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// Fused unique + leaf build.
+// ---------------------------------------------------------------------------
+struct LeafSmem {
+    uint64_t keys[kPadded];
+    uint64_t run_or[kTile];
+    uint64_t run_par[kTile];
+    uint32_t scan[34];
+    uint32_t slot;
+    uint64_t tail_or;
+    uint64_t p_base;
+};
+
+__global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LeafSmem& S = *reinterpret_cast<LeafSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t n = load_count(a.d_n, a.n_bound);
+    const uint32_t ntiles = scan_tiles(n);
+    while (true) {
+        const uint32_t tile = next_tile(a.tile_counter, &S.slot);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile;
+        const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
+        for (int i = tid; i < kTile; i += kT) {
+            if (i < (int)tile_n) S.keys[pad8(i)] = a.sorted[base + i];
+            S.run_or[i] = 0;
+        }
+        __syncthreads();
+
+        const int i0 = tid * kI;
+        uint64_t prev;
+        bool have_prev;
+        if (i0 == 0) {
+            have_prev = base > 0;
+            prev = have_prev ? (a.sorted[base - 1] >> 6) : 0;
+        } else {
+            have_prev = true;
+            prev = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0;
+        }
+        uint32_t heads = 0;
+#pragma unroll
+        for (int j = 0; j < kI; ++j) {
+            const int i = i0 + j;
+            if (i < (int)tile_n) {
+                const uint64_t par = S.keys[pad8(i)] >> 6;
+                if (!have_prev || par != prev) ++heads;
+                prev = par;
+                have_prev = true;
+            }
+        }
+        uint32_t total_heads;
+        const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
+
+        // Accumulate run ORs; runs are tile-local indices, -1 = the previous
+        // tile's open run (handled by that tile's read-ahead).
+        {
+            int run = (int)excl - 1;
+            uint64_t acc = 0;
+            bool hp = false;
+            uint64_t pv = 0;
+            if (i0 == 0) { hp = base > 0; pv = hp ? (a.sorted[base - 1] >> 6) : 0; }
+            else { hp = true; pv = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0; }
+#pragma unroll
+            for (int j = 0; j < kI; ++j) {
+                const int i = i0 + j;
+                if (i < (int)tile_n) {
+                    const uint64_t key = S.keys[pad8(i)];
+                    const uint64_t par = key >> 6;
+                    if (!hp || par != pv) {
+                        if (run >= 0 && acc) atomicOr((unsigned long long*)&S.run_or[run], (unsigned long long)acc);
+                        ++run;
+                        acc = 0;
+                        S.run_par[run] = par;
+                    }
+                    acc |= 1ull << (key & 63);
+                    pv = par;
+                    hp = true;
+                }
+            }
+            if (run >= 0 && acc) atomicOr((unsigned long long*)&S.run_or[run], (unsigned long long)acc);
+        }
+        if (tid == 0) S.tail_or = 0;
+        __syncthreads();
+
+        if (warp == 0) {
+            const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
+            if (lane == 0) S.p_base = pb;
+        } else if (warp == 1 && total_heads > 0 && base + tile_n < n) {
+            // Read ahead: the tile's last run may continue into later tiles.
+            const uint64_t last_par = S.run_par[total_heads - 1];
+            uint64_t acc = 0;
+            for (uint64_t pos = base + tile_n;; pos += 32) {
+                const uint64_t i = pos + lane;
+                const bool in = i < n;
+                const uint64_t key = in ? a.sorted[i] : 0;
+                const bool match = in && (key >> 6) == last_par;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, match);
+                const uint32_t run_len = __ffs(~m) ? (uint32_t)(__ffs(~m) - 1) : 32u;
+                if (lane < run_len) acc |= 1ull << (key & 63);
+                if (run_len < 32) break;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+            if (lane == 0) S.tail_or = acc;
+        }
+        __syncthreads();
+        const uint64_t p_base = S.p_base;
+        bool overflow = false;
+        for (uint32_t r = tid; r < total_heads; r += kT) {
+            uint64_t m = S.run_or[r];
+            if (r == total_heads - 1) m |= S.tail_or;
+            if (p_base + r < a.out_capacity) {
+                a.parents[p_base + r] = S.run_par[r];
+                a.leaves[p_base + r] = m;
+            } else {
+                overflow = true;
+            }
+        }
+        if (overflow) atomicOr(a.err, kErrCapacity);
+        if (tid == 0 && base + tile_n == n) {
+            const uint64_t cnt = p_base + total_heads;
+            *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Extract one level + node hash. Child codes are unique and sorted, so a
+// parent owns at most 8 consecutive children; the head child builds the node.
+// ---------------------------------------------------------------------------
+struct ExtractSmem {
+    uint64_t codes[kPadded];
+    uint32_t map[kTile];
+    uint32_t scan[34];
+    uint32_t slot;
+    uint64_t p_base;
+};
+
+__global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ExtractSmem& S = *reinterpret_cast<ExtractSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t n = load_count(a.d_n, a.n_bound);
+    const uint32_t ntiles = scan_tiles(n);
+    while (true) {
+        const uint32_t tile = next_tile(a.tile_counter, &S.slot);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile;
+        const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
+        for (int i = tid; i < (int)tile_n; i += kT) {
+            S.codes[pad8(i)] = a.child_codes[base + i];
+            S.map[i] = a.child_map[base + i];
+        }
+        __syncthreads();
+        const int i0 = tid * kI;
+        uint32_t head_bits = 0, heads = 0;
+        {
+            bool hp;
+            uint64_t pv;
+            if (i0 == 0) { hp = base > 0; pv = hp ? (a.child_codes[base - 1] >> 3) : 0; }
+            else { hp = true; pv = i0 - 1 < (int)tile_n ? (S.codes[pad8(i0 - 1)] >> 3) : 0; }
+#pragma unroll
+            for (int j = 0; j < kI; ++j) {
+                const int i = i0 + j;
+                if (i < (int)tile_n) {
+                    const uint64_t par = S.codes[pad8(i)] >> 3;
+                    if (!hp || par != pv) { head_bits |= 1u << j; ++heads; }
+                    pv = par;
+                    hp = true;
+                }
+            }
+        }
+        uint32_t total_heads;
+        const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
+        if (warp == 0) {
+            const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
+            if (lane == 0) S.p_base = pb;
+        }
+        __syncthreads();
+        uint64_t p = S.p_base + excl;
+        bool overflow = false;
+        for (int j = 0; j < kI; ++j) {
+            if (!(head_bits & (1u << j))) continue;
+            if (p >= a.out_capacity) { overflow = true; break; }
+            const int i = i0 + j;
+            const uint64_t code0 = S.codes[pad8(i)];
+            const uint64_t par = code0 >> 3;
+            uint32_t ch[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) ch[c] = kEmptyChild;
+            uint32_t mask = 0;
+            for (int k = 0; k < 8; ++k) {
+                const uint64_t gi = base + i + k;
+                if (gi >= n) break;
+                uint64_t code;
+                uint32_t m;
+                if (i + k < (int)tile_n) { code = S.codes[pad8(i + k)]; m = S.map[i + k]; }
+                else { code = a.child_codes[gi]; m = a.child_map[gi]; }
+                if ((code >> 3) != par) break;
+                const uint32_t slot = (uint32_t)(code & 7);
+                ch[slot] = m;
+                mask |= 1u << slot;
+            }
+            uint64_t h[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) h[c] = ch[c] == kEmptyChild ? 0 : __ldg(a.child_hashes + ch[c]);
+            a.node_codes[p] = par;
+            a.node_masks[p] = (uint8_t)mask;
+            uint4* dst = reinterpret_cast<uint4*>(a.node_children + p * 8);
+            dst[0] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
+            dst[1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
+            a.node_hashes[p] = hash_children(h);
+            ++p;
+        }
+        if (overflow) atomicOr(a.err, kErrCapacity);
+        if (tid == 0 && base + tile_n == n) {
+            const uint64_t cnt = S.p_base + total_heads;
+            *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Unique over runs of equal keys (after the hash sort), with the collision
+// check: every run member must carry the same mask and children as its
+// predecessor in the run.
+// ---------------------------------------------------------------------------
+struct UniqueSmem {
+    uint64_t keys[kPadded];
+    uint32_t perm[kTile];
+    uint32_t scan[34];
+    uint32_t slot;
+    uint64_t p_base;
+};
+
+__global__ void __launch_bounds__(kT) unique_runs(UniqueArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    UniqueSmem& S = *reinterpret_cast<UniqueSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t n = load_count(a.d_n, a.n_bound);
+    const uint32_t ntiles = scan_tiles(n);
+    while (true) {
+        const uint32_t tile = next_tile(a.tile_counter, &S.slot);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile;
+        const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
+        for (int i = tid; i < (int)tile_n; i += kT) {
+            S.keys[pad8(i)] = a.keys[base + i];
+            S.perm[i] = a.perm[base + i];
+        }
+        __syncthreads();
+        const int i0 = tid * kI;
+        uint32_t head_bits = 0, heads = 0;
+        bool collision = false;
+        {
+            bool hp;
+            uint64_t pv;
+            uint32_t pperm = 0;
+            if (i0 == 0) {
+                hp = base > 0;
+                pv = hp ? a.keys[base - 1] : 0;
+                pperm = hp ? a.perm[base - 1] : 0;
+            } else {
+                hp = true;
+                pv = i0 - 1 < (int)tile_n ? S.keys[pad8(i0 - 1)] : 0;
+                pperm = i0 - 1 < (int)tile_n ? S.perm[i0 - 1] : 0;
+            }
+            for (int j = 0; j < kI; ++j) {
+                const int i = i0 + j;
+                if (i >= (int)tile_n) break;
+                const uint64_t k = S.keys[pad8(i)];
+                const uint32_t pm = S.perm[i];
+                if (!hp || k != pv) {
+                    head_bits |= 1u << j;
+                    ++heads;
+                } else if (a.children) {
+                    const uint4* x = reinterpret_cast<const uint4*>(a.children + (uint64_t)pm * 8);
+                    const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)pperm * 8);
+                    const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
+                    const bool same = a.masks[pm] == a.masks[pperm] && x0.x == y0.x && x0.y == y0.y &&
+                                      x0.z == y0.z && x0.w == y0.w && x1.x == y1.x && x1.y == y1.y &&
+                                      x1.z == y1.z && x1.w == y1.w;
+                    collision |= !same;
+                }
+                pv = k;
+                pperm = pm;
+                hp = true;
+            }
+        }
+        if (__any_sync(0xFFFFFFFFu, collision) && lane == 0) atomicOr(a.err, kErrCollision);
+        uint32_t total_heads;
+        const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
+        if (warp == 0) {
+            const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
+            if (lane == 0) S.p_base = pb;
+        }
+        __syncthreads();
+        // uid of the run an item belongs to; items before the tile's first
+        // head continue the previous tile's last run (uid p_base - 1).
+        int64_t uid = (int64_t)S.p_base + excl - 1;
+        bool overflow = false;
+        for (int j = 0; j < kI; ++j) {
+            const int i = i0 + j;
+            if (i >= (int)tile_n) break;
+            const uint32_t pm = S.perm[i];
+            if (head_bits & (1u << j)) {
+                ++uid;
+                if ((uint64_t)uid < a.out_capacity) {
+                    a.out_keys[uid] = S.keys[pad8(i)];
+                    if (a.out_masks) a.out_masks[uid] = a.masks[pm];
+                    if (a.out_children) {
+                        const uint4* src = reinterpret_cast<const uint4*>(a.children + (uint64_t)pm * 8);
+                        uint4* dst = reinterpret_cast<uint4*>(a.out_children + (uint64_t)uid * 8);
+                        dst[0] = src[0];
+                        dst[1] = src[1];
+                    }
+                } else {
+                    overflow = true;
+                }
+            }
+            a.map[pm] = (uint64_t)uid < a.out_capacity ? (uint32_t)uid : (uint32_t)(a.out_capacity - 1);
+        }
+        if (overflow) atomicOr(a.err, kErrCapacity);
+        if (tid == 0 && base + tile_n == n) {
+            const uint64_t cnt = S.p_base + total_heads;
+            *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Final layout.
+// ---------------------------------------------------------------------------
+struct FinalScanSmem {
+    uint32_t scan[34];
+    uint32_t slot;
+    uint64_t p_base;
+};
+
+// word_pos[i] = sum over nodes j < i of (popc(mask_j) + 1); word_pos[n] = total.
+__global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
+    __shared__ FinalScanSmem S;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint64_t n = a.num_nodes;
+    const uint32_t ntiles = scan_tiles(n);
+    while (true) {
+        const uint32_t tile = next_tile(a.tile_counter, &S.slot);
+        if (tile >= ntiles) break;
+        const uint64_t i0 = (uint64_t)tile * kTile + (uint64_t)tid * kI;
+        uint32_t w[kI];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kI; ++j) {
+            w[j] = i0 + j < n ? (uint32_t)__popc(a.masks[i0 + j]) + 1u : 0u;
+            sum += w[j];
+        }
+        uint32_t total;
+        const uint32_t excl = block_exclusive_sum<uint32_t>(sum, S.scan, &total);
+        if (warp == 0) {
+            const uint64_t pb = sv_lookback(a.status, tile, total, a.err);
+            if (lane == 0) S.p_base = pb;
+        }
+        __syncthreads();
+        uint64_t pos = S.p_base + excl;
+#pragma unroll
+        for (int j = 0; j < kI; ++j) {
+            if (i0 + j < n) a.word_pos[i0 + j] = (uint32_t)pos;
+            pos += w[j];
+        }
+        if (tid == 0 && (uint64_t)(tile + 1) * kTile >= n) {
+            a.word_pos[n] = (uint32_t)(S.p_base + total);
+            *a.d_total = S.p_base + total;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kT) final_write(FinalArgs a) {
+    __shared__ uint64_t s_off[24];
+    if (threadIdx.x <= (unsigned)a.num_levels) s_off[threadIdx.x] = a.level_offsets[threadIdx.x];
+    __syncthreads();
+    const uint64_t n = a.num_nodes;
+    const uint64_t leaf_start = a.word_pos[n];
+    const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n + a.num_leaves; i += gstride) {
+        if (i >= n) {
+            const uint64_t j = i - n;
+            const uint64_t leaf = a.leaves[j];
+            a.words[leaf_start + 2 * j] = (uint32_t)leaf;
+            a.words[leaf_start + 2 * j + 1] = (uint32_t)(leaf >> 32);
+            continue;
+        }
+        int l = 0;
+        while (l + 1 < a.num_levels && i >= s_off[l + 1]) ++l;
+        const bool last = l + 1 == a.num_levels;
+        const uint32_t mask = a.masks[i];
+        const uint64_t pos = a.word_pos[i];
+        a.words[pos] = mask;
+        const uint4* src = reinterpret_cast<const uint4*>(a.children + i * 8);
+        const uint4 c0 = src[0], c1 = src[1];
+        const uint32_t ch[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+        uint32_t k = 1;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const bool has = (mask >> c) & 1u;
+            // WriteTo's structural check (src/DAGCompression.cu:860) plus a
+            // range check, so a malformed DAG can never index out of bounds.
+            const uint64_t limit = last ? a.num_leaves : s_off[l + 2] - s_off[l + 1];
+            const bool ok = has == (ch[c] != kEmptyChild) && (!has || ch[c] < limit);
+            bad |= !ok;
+            if (!has || !ok) continue;
+            const uint64_t ptr = last ? leaf_start + 2ull * ch[c] : a.word_pos[s_off[l + 1] + ch[c]];
+            a.words[pos + k++] = (uint32_t)ptr;
+        }
+    }
+    if (bad) atomicOr(a.err, kErrBadInput);
+}
+
+// ---------------------------------------------------------------------------
+// Small helpers.
+// ---------------------------------------------------------------------------
+__global__ void remap_children(const uint32_t* __restrict__ in, const uint32_t* __restrict__ map,
+                               uint32_t* __restrict__ out, uint64_t n_words) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = in[i];
+        out[i] = c == kEmptyChild ? kEmptyChild : map[c];
+    }
+}
+
+__global__ void iota_offset(uint32_t* out, uint64_t n, uint32_t offset) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = offset + (uint32_t)i;
+}
+
+int g_blocks_small = 152 * 8;
+
+}  // namespace
+
+void kernels_configure() {
+    cudaFuncSetAttribute(leaf_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LeafSmem));
+    cudaFuncSetAttribute(extract_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    cudaFuncSetAttribute(unique_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(UniqueSmem));
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_blocks_small = sms * 8;
+}
+
+int occupancy_kernel(int which) {
+    int occ = 0;
+    switch (which) {
+        case kKernelLeafBuild:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_build, kT, sizeof(LeafSmem));
+            break;
+        case kKernelExtract:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, extract_level, kT, sizeof(ExtractSmem));
+            break;
+        case kKernelUnique:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, unique_runs, kT, sizeof(UniqueSmem));
+            break;
+        default:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, final_positions, kT, 0);
+            break;
+    }
+    return occ;
+}
+
+void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s) {
+    leaf_build<<<a.grid, kT, sizeof(LeafSmem), s>>>(a);
+}
+void launch_extract(const ExtractArgs& a, cudaStream_t s) {
+    extract_level<<<a.grid, kT, sizeof(ExtractSmem), s>>>(a);
+}
+void launch_unique(const UniqueArgs& a, cudaStream_t s) {
+    unique_runs<<<a.grid, kT, sizeof(UniqueSmem), s>>>(a);
+}
+void launch_final_positions(const FinalArgs& a, cudaStream_t s) {
+    final_positions<<<a.grid_scan, kT, 0, s>>>(a);
+}
+void launch_final_write(const FinalArgs& a, cudaStream_t s) {
+    final_write<<<a.grid_write, kT, 0, s>>>(a);
+}
+void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* out, uint64_t n_nodes,
+                           cudaStream_t s) {
+    if (n_nodes == 0) return;
+    const uint64_t words = n_nodes * 8;
+    const int grid = (int)std::min<uint64_t>((words + 255) / 256, (uint64_t)g_blocks_small);
+    remap_children<<<grid, 256, 0, s>>>(in, map, out, words);
+}
+void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s) {
+    if (n == 0) return;
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)g_blocks_small);
+    iota_offset<<<grid, 256, 0, s>>>(out, n, offset);
+}
+
+}  // namespace dagc

@@ -1,0 +1,1185 @@
+// dagc host orchestration and C ABI (include/dagc.h).
+//
+// Host code is C++ and reaches the GPU only through the kernel launchers of
+// dagc_kernels.h. The pipelines keep every count on the device: a call
+// enqueues its whole kernel sequence, then reads the counts back once.
+//
+// Reference mapping (src/DAGCompression.cu of Phyronnaz/DAG_Compression_Fast):
+//   create_dag        <- DAGCompression::CreateDAG          :1003-1107
+//   merge_dags        <- DAGCompression::MergeDAGs          :1446-1548 (+ :1109-1320)
+//   final_dag         <- DAGCompression::CreateFinalDAG     :1550-1610
+//   DevicePool        <- FPool :32-269 / FMemory (src/Memory.cpp:42-98)
+
+#include "../../include/dagc.h"
+#include "dagc_hash.h"
+#include "dagc_kernels.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace dagc {
+namespace {
+
+constexpr int kMaxDepth = 21;
+constexpr uint64_t kMaxFragments = (1ull << 30) - 1;
+constexpr int kMaxSorts = 48;
+constexpr int kMaxTileCounters = 1024;
+
+// Device-count slots of one call.
+enum : int {
+    kCntFragments = 0,
+    kCntBricks = 1,
+    kCntLeaves = 2,
+    kCntNodes = 3,                 // + level
+    kCntUnique = 3 + kMaxDepth,    // + level
+    kCntSlots = 3 + 2 * kMaxDepth + 1,
+};
+
+struct CallHeader {
+    uint32_t err;
+    uint32_t pad;
+    uint64_t counts[64];
+    uint32_t tile_counters[kMaxTileCounters];
+    uint32_t hist[kMaxSorts][kMaxPasses * 256];
+};
+static_assert(kCntSlots <= 64, "count slots");
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Best-fit cache of device blocks (the reference's FPool): freed blocks are
+// kept and reused; on cudaMalloc failure the cache is released and the
+// allocation retried once (the OOM fallback of src/Memory.cpp:56-70).
+class DevicePool {
+public:
+    ~DevicePool() { trim(); }
+    cudaError_t alloc(void** p, size_t bytes) {
+        bytes = align_up(std::max<size_t>(bytes, 1), 512);
+        auto it = free_.lower_bound(bytes);
+        if (it != free_.end() && it->first <= 2 * bytes + (4u << 20)) {
+            *p = it->second;
+            live_[*p] = it->first;
+            cached_ -= it->first;
+            in_use_ += it->first;
+            free_.erase(it);
+            peak_ = std::max(peak_, in_use_);
+            return cudaSuccess;
+        }
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            trim();
+            e = cudaMalloc(p, bytes);
+        }
+        if (e != cudaSuccess) { cudaGetLastError(); *p = nullptr; return e; }
+        live_[*p] = bytes;
+        in_use_ += bytes;
+        peak_ = std::max(peak_, in_use_);
+        return cudaSuccess;
+    }
+    void release(void* p) {
+        if (!p) return;
+        auto it = live_.find(p);
+        if (it == live_.end()) return;
+        free_.emplace(it->second, p);
+        cached_ += it->second;
+        in_use_ -= it->second;
+        live_.erase(it);
+    }
+    void trim() {
+        for (auto& kv : free_) cudaFree(kv.second);
+        free_.clear();
+        cached_ = 0;
+    }
+    size_t in_use() const { return in_use_; }
+    size_t peak() const { return peak_; }
+
+private:
+    std::multimap<size_t, void*> free_;
+    std::unordered_map<void*, size_t> live_;
+    size_t in_use_ = 0, cached_ = 0, peak_ = 0;
+};
+
+// One growable scratch block; every call lays its buffers out from offset 0.
+struct Arena {
+    void* base = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (base) cudaFree(base);
+        base = nullptr;
+        cap = 0;
+        const size_t want = align_up(bytes + bytes / 4, 1u << 21);
+        cudaError_t e = cudaMalloc(&base, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaMalloc(&base, align_up(bytes, 1u << 21));
+            if (e != cudaSuccess) { cudaGetLastError(); base = nullptr; return e; }
+            cap = align_up(bytes, 1u << 21);
+            return cudaSuccess;
+        }
+        cap = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (base) cudaFree(base);
+        base = nullptr;
+        cap = 0;
+    }
+};
+
+struct Layout {
+    size_t off = 0;
+    template <typename T>
+    size_t take(uint64_t count) {
+        off = align_up(off, 256);
+        const size_t o = off;
+        off += (size_t)count * sizeof(T);
+        return o;
+    }
+};
+
+}  // namespace
+}  // namespace dagc
+
+using namespace dagc;
+
+struct dagc_context_t {
+    int device = 0;
+    int sms = 152;
+    int grid_hist = 0, grid_pass_kv = 0, grid_pass_k = 0;
+    int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
+    DevicePool pool;
+    Arena arena;
+    std::string last_error;
+    std::vector<uint64_t> last_counts;
+    uint64_t* h_stage = nullptr;  // pinned: counts + error word read back
+    std::mutex mu;
+};
+
+struct dagc_dag_t {
+    dagc_context ctx = nullptr;
+    int num_levels = 0;
+    std::vector<uint64_t> level_offset;  // num_levels + 1 (nodes, concatenated, root level first)
+    uint64_t num_leaves = 0;
+    void* block = nullptr;
+    uint64_t* hashes = nullptr;
+    uint32_t* children = nullptr;
+    uint8_t* masks = nullptr;
+    uint64_t* leaves = nullptr;
+    uint64_t* d_level_offset = nullptr;
+    uint64_t num_nodes() const { return level_offset.empty() ? 0 : level_offset.back(); }
+};
+
+namespace {
+
+int set_error(dagc_context ctx, int status, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return status;
+}
+
+int cuda_status(cudaError_t e) {
+    return e == cudaErrorMemoryAllocation ? DAGC_ERR_OUT_OF_MEMORY : DAGC_ERR_CUDA;
+}
+
+#define DAGC_CUDA(ctx, expr)                                                                      \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            cudaGetLastError();                                                                   \
+            return set_error(ctx, cuda_status(e_), std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+        }                                                                                         \
+    } while (0)
+
+#define DAGC_LAUNCHED(ctx) DAGC_CUDA(ctx, cudaGetLastError())
+
+int grid_for(int per_sm, int sms, uint64_t tiles) {
+    const uint64_t g = (uint64_t)std::max(per_sm, 1) * (uint64_t)sms;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, std::max<uint64_t>(tiles, 1)));
+}
+
+int device_error_status(uint32_t err, std::string& msg) {
+    if (err & kErrTimeout) { msg = "a bounded device wait ran out"; return DAGC_ERR_DEVICE_TIMEOUT; }
+    if (err & kErrBadInput) { msg = "fragment code out of range for the depth, or malformed DAG"; return DAGC_ERR_BAD_INPUT; }
+    if (err & kErrCollision) { msg = "64-bit node hash collision between different nodes"; return DAGC_ERR_HASH_COLLISION; }
+    if (err & kErrCapacity) { msg = "internal capacity bound exceeded"; return DAGC_ERR_CUDA; }
+    if (err & kErrNotRooted) { msg = "level 0 does not hold exactly one node"; return DAGC_ERR_BAD_INPUT; }
+    if (err & kErrMergeRoot) { msg = "sub-DAG root missing from merged level"; return DAGC_ERR_BAD_INPUT; }
+    return DAGC_OK;
+}
+
+// Per-call scratch slots inside the zeroed header.
+// Each single-value look-back launch gets its own zeroed status region sized
+// for its tile bound; the regions are carved in launch order.
+struct CallSlots {
+    CallHeader* h;
+    int next_counter = 0, next_hist = 0;
+    uint64_t* sv_next = nullptr;
+    uint64_t* sv_end = nullptr;
+    uint32_t* counter() { return &h->tile_counters[next_counter++]; }
+    uint32_t* counters(int k) { uint32_t* p = &h->tile_counters[next_counter]; next_counter += k; return p; }
+    uint32_t* hist() { return h->hist[next_hist++]; }
+    uint64_t* sv(uint64_t n_bound) {
+        uint64_t* p = sv_next;
+        sv_next += scan_tiles(n_bound) + 1;
+        return sv_next <= sv_end ? p : nullptr;
+    }
+    uint64_t* count(int slot) { return &h->counts[slot]; }
+};
+inline uint64_t sv_words(uint64_t n_bound) { return scan_tiles(n_bound) + 1; }
+
+struct SortBuffers {
+    uint32_t* status[2];
+};
+
+int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint64_t* keys_in,
+             uint64_t* keys_out, uint64_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
+             uint32_t* vals_alt, bool with_values, uint64_t n_bound, const uint64_t* d_n, int lo, int hi,
+             int validate_bits, cudaStream_t s) {
+    if (cs.next_hist >= kMaxSorts || cs.next_counter + kMaxPasses > kMaxTileCounters)
+        return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many sorts in one call");
+    SortArgs a{};
+    a.keys_in = keys_in;
+    a.keys_out = keys_out;
+    a.keys_alt = keys_alt;
+    a.vals_in = vals_in;
+    a.vals_out = vals_out;
+    a.vals_alt = vals_alt;
+    a.with_values = with_values;
+    a.n = n_bound;
+    a.d_n = d_n;
+    a.lo_bit = lo;
+    a.hi_bit = hi;
+    a.validate_bits = validate_bits;
+    a.hist = cs.hist();
+    a.status[0] = sb.status[0];
+    a.status[1] = sb.status[1];
+    a.tile_counters = cs.counters(kMaxPasses);
+    a.err = &cs.h->err;
+    const uint64_t tiles = sort_tiles(n_bound);
+    a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
+    a.grid_pass = grid_for((with_values ? ctx->grid_pass_kv : ctx->grid_pass_k) / std::max(ctx->sms, 1),
+                           ctx->sms, tiles);
+    launch_sort(a, s);
+    DAGC_LAUNCHED(ctx);
+    return DAGC_OK;
+}
+
+int alloc_dag(dagc_context ctx, int num_levels, const std::vector<uint64_t>& level_sizes,
+              uint64_t num_leaves, dagc_dag* out) {
+    std::unique_ptr<dagc_dag_t> d(new dagc_dag_t);
+    d->ctx = ctx;
+    d->num_levels = num_levels;
+    d->level_offset.assign(num_levels + 1, 0);
+    for (int l = 0; l < num_levels; ++l) d->level_offset[l + 1] = d->level_offset[l] + level_sizes[l];
+    d->num_leaves = num_leaves;
+    const uint64_t nn = d->num_nodes();
+    Layout L;
+    const size_t o_h = L.take<uint64_t>(nn);
+    const size_t o_c = L.take<uint32_t>(nn * 8);
+    const size_t o_l = L.take<uint64_t>(num_leaves);
+    const size_t o_o = L.take<uint64_t>(num_levels + 1);
+    const size_t o_m = L.take<uint8_t>(nn);
+    void* block = nullptr;
+    DAGC_CUDA(ctx, ctx->pool.alloc(&block, L.off));
+    char* b = static_cast<char*>(block);
+    d->block = block;
+    d->hashes = reinterpret_cast<uint64_t*>(b + o_h);
+    d->children = reinterpret_cast<uint32_t*>(b + o_c);
+    d->leaves = reinterpret_cast<uint64_t*>(b + o_l);
+    d->d_level_offset = reinterpret_cast<uint64_t*>(b + o_o);
+    d->masks = reinterpret_cast<uint8_t*>(b + o_m);
+    *out = d.release();
+    return DAGC_OK;
+}
+
+void free_dag(dagc_dag d) {
+    if (!d) return;
+    if (d->ctx) d->ctx->pool.release(d->block);
+    delete d;
+}
+
+uint64_t level_cap(int level, uint64_t n) {
+    // A level-l node is identified by the top 3*l code bits: at most 8^l of them.
+    if (3 * level >= 62) return n;
+    return std::min<uint64_t>(n, 1ull << (3 * level));
+}
+
+// -------------------------------------------------------------- CreateDAG --
+// Output of the device pipeline before materialisation: per-level unique
+// arrays in the scratch pools (upper-bound strides) and the counts.
+struct CreatePools {
+    std::vector<uint64_t*> hashes;
+    std::vector<uint32_t*> children;
+    std::vector<uint8_t*> masks;
+    uint64_t* leaves = nullptr;
+    std::vector<uint64_t> unique;  // u_l
+    uint64_t num_leaves = 0;
+};
+
+int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
+                    CreatePools& out) {
+    const int nl = depth - 2;
+    const int bits = 3 * depth;
+    std::vector<uint64_t> cap(nl);
+    uint64_t capmax = 1;
+    for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
+    const uint64_t p0cap = level_cap(depth - 2, n);
+    uint64_t sv_total = sv_words(n) + sv_words(p0cap);
+    for (int l = nl - 1; l >= 0; --l) sv_total += sv_words(l == nl - 1 ? p0cap : cap[l + 1]) + sv_words(cap[l]);
+
+    Layout L;
+    const size_t o_hdr = L.take<CallHeader>(1);
+    const size_t o_sv = L.take<uint64_t>(sv_total);
+    const size_t zero_bytes = L.off;
+    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+    const size_t o_A = L.take<uint64_t>(n);
+    const size_t o_B = L.take<uint64_t>(n);
+    const size_t o_P = L.take<uint64_t>(p0cap);
+    const size_t o_LM = L.take<uint64_t>(p0cap);
+    const size_t o_SK = L.take<uint64_t>(p0cap);
+    const size_t o_SKa = L.take<uint64_t>(p0cap);
+    const size_t o_V = L.take<uint32_t>(p0cap);
+    const size_t o_Va = L.take<uint32_t>(p0cap);
+    const size_t o_M0 = L.take<uint32_t>(p0cap);
+    const size_t o_M1 = L.take<uint32_t>(p0cap);
+    const size_t o_NC0 = L.take<uint64_t>(capmax);
+    const size_t o_NC1 = L.take<uint64_t>(capmax);
+    const size_t o_NM = L.take<uint8_t>(capmax);
+    const size_t o_NCH = L.take<uint32_t>(capmax * 8);
+    const size_t o_NH = L.take<uint64_t>(capmax);
+    const size_t o_PL = L.take<uint64_t>(p0cap);
+    std::vector<size_t> o_ph(nl), o_pc(nl), o_pm(nl);
+    for (int l = 0; l < nl; ++l) {
+        o_ph[l] = L.take<uint64_t>(cap[l]);
+        o_pc[l] = L.take<uint32_t>(cap[l] * 8);
+        o_pm[l] = L.take<uint8_t>(cap[l]);
+    }
+    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    char* b = static_cast<char*>(ctx->arena.base);
+    auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
+    auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
+    auto P8 = [&](size_t o) { return reinterpret_cast<uint8_t*>(b + o); };
+
+    CallSlots cs;
+    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
+    cs.sv_next = P64(o_sv);
+    cs.sv_end = P64(o_sv) + sv_total;
+    SortBuffers sb{{P32(o_ss0), P32(o_ss1)}};
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+    uint32_t* err = &cs.h->err;
+
+    // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
+    //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
+    int st = run_sort(ctx, cs, sb, d_frag, P64(o_A), P64(o_B), nullptr, nullptr, nullptr, false, n, nullptr,
+                      6, std::max(6, bits), bits < 64 ? bits : 0, s);
+    if (st) return st;
+
+    // 2. Fused unique + leaf build.
+    {
+        LeafBuildArgs a{};
+        a.sorted = P64(o_A);
+        a.d_n = nullptr;
+        a.n_bound = n;
+        a.parents = P64(o_P);
+        a.leaves = P64(o_LM);
+        a.out_capacity = p0cap;
+        a.d_out_n = cs.count(kCntBricks);
+        a.status = cs.sv(n);
+        a.tile_counter = cs.counter();
+        a.err = err;
+        a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, scan_tiles(n));
+        launch_leaf_build(a, s);
+        DAGC_LAUNCHED(ctx);
+    }
+    // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
+    st = run_sort(ctx, cs, sb, P64(o_LM), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, p0cap,
+                  cs.count(kCntBricks), 0, 64, 0, s);
+    if (st) return st;
+    {
+        UniqueArgs a{};
+        a.keys = P64(o_SK);
+        a.perm = P32(o_V);
+        a.d_n = cs.count(kCntBricks);
+        a.n_bound = p0cap;
+        a.map = P32(o_M0);
+        a.out_keys = P64(o_PL);
+        a.out_capacity = p0cap;
+        a.d_out_n = cs.count(kCntLeaves);
+        a.status = cs.sv(p0cap);
+        a.tile_counter = cs.counter();
+        a.err = err;
+        a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(p0cap));
+        launch_unique(a, s);
+        DAGC_LAUNCHED(ctx);
+    }
+    // 4. Level loop, bottom-up.
+    const uint64_t* child_codes = P64(o_P);
+    const uint32_t* child_map = P32(o_M0);
+    const uint64_t* child_hashes = P64(o_PL);
+    const uint64_t* d_child_n = cs.count(kCntBricks);
+    uint64_t child_bound = p0cap;
+    uint64_t* node_codes[2] = {P64(o_NC0), P64(o_NC1)};
+    uint32_t* maps[2] = {P32(o_M1), P32(o_M0)};
+    for (int l = nl - 1, it = 0; l >= 0; --l, ++it) {
+        ExtractArgs e{};
+        e.child_codes = child_codes;
+        e.child_map = child_map;
+        e.d_n = d_child_n;
+        e.n_bound = child_bound;
+        e.child_hashes = child_hashes;
+        e.node_codes = node_codes[it & 1];
+        e.node_masks = P8(o_NM);
+        e.node_children = P32(o_NCH);
+        e.node_hashes = P64(o_NH);
+        e.out_capacity = cap[l];
+        e.d_out_n = cs.count(kCntNodes + l);
+        e.status = cs.sv(child_bound);
+        e.tile_counter = cs.counter();
+        e.err = err;
+        e.grid = grid_for(ctx->grid_extract / ctx->sms, ctx->sms, scan_tiles(child_bound));
+        launch_extract(e, s);
+        DAGC_LAUNCHED(ctx);
+
+        st = run_sort(ctx, cs, sb, P64(o_NH), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
+                      cap[l], cs.count(kCntNodes + l), 0, 64, 0, s);
+        if (st) return st;
+
+        UniqueArgs u{};
+        u.keys = P64(o_SK);
+        u.perm = P32(o_V);
+        u.d_n = cs.count(kCntNodes + l);
+        u.n_bound = cap[l];
+        u.masks = P8(o_NM);
+        u.children = P32(o_NCH);
+        u.map = maps[it & 1];
+        u.out_keys = P64(o_ph[l]);
+        u.out_masks = P8(o_pm[l]);
+        u.out_children = P32(o_pc[l]);
+        u.out_capacity = cap[l];
+        u.d_out_n = cs.count(kCntUnique + l);
+        u.status = cs.sv(cap[l]);
+        u.tile_counter = cs.counter();
+        u.err = err;
+        u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(cap[l]));
+        launch_unique(u, s);
+        DAGC_LAUNCHED(ctx);
+
+        child_codes = node_codes[it & 1];
+        child_map = maps[it & 1];
+        child_hashes = P64(o_ph[l]);
+        d_child_n = cs.count(kCntNodes + l);
+        child_bound = cap[l];
+    }
+
+    if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
+    // 5. One read-back of every count and the error word.
+    static_assert(sizeof(CallHeader) >= 8 * 65, "header");
+    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, cs.h, 8 + 8 * 64, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    const uint32_t e32 = (uint32_t)(ctx->h_stage[0] & 0xFFFFFFFFu);
+    const uint64_t* counts = ctx->h_stage + 1;
+    ctx->last_counts.assign(3 + nl, 0);
+    ctx->last_counts[0] = n;
+    ctx->last_counts[1] = counts[kCntBricks];
+    ctx->last_counts[2] = counts[kCntLeaves];
+    for (int l = 0; l < nl; ++l) ctx->last_counts[3 + l] = counts[kCntNodes + l];
+    std::string msg;
+    st = device_error_status(e32, msg);
+    if (st) return set_error(ctx, st, msg);
+    if (nl > 0 && counts[kCntUnique + 0] != 1) return set_error(ctx, DAGC_ERR_BAD_INPUT, "root level must hold one node");
+    if (nl == 0 && counts[kCntLeaves] != 1) return set_error(ctx, DAGC_ERR_BAD_INPUT, "depth-2 volume must hold one leaf");
+
+    out.hashes.resize(nl);
+    out.children.resize(nl);
+    out.masks.resize(nl);
+    out.unique.resize(nl);
+    for (int l = 0; l < nl; ++l) {
+        out.hashes[l] = P64(o_ph[l]);
+        out.children[l] = P32(o_pc[l]);
+        out.masks[l] = P8(o_pm[l]);
+        out.unique[l] = counts[kCntUnique + l];
+    }
+    out.leaves = P64(o_PL);
+    out.num_leaves = counts[kCntLeaves];
+    return DAGC_OK;
+}
+
+int materialise(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, dagc_dag* out) {
+    dagc_dag d = nullptr;
+    int st = alloc_dag(ctx, nl, p.unique, p.num_leaves, &d);
+    if (st) return st;
+    for (int l = 0; l < nl; ++l) {
+        const uint64_t o = d->level_offset[l], u = p.unique[l];
+        if (!u) continue;
+        cudaMemcpyAsync(d->hashes + o, p.hashes[l], u * 8, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(d->children + o * 8, p.children[l], u * 32, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(d->masks + o, p.masks[l], u, cudaMemcpyDeviceToDevice, s);
+    }
+    if (p.num_leaves) cudaMemcpyAsync(d->leaves, p.leaves, p.num_leaves * 8, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (nl + 1) * 8, cudaMemcpyHostToDevice, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        free_dag(d);
+        cudaGetLastError();
+        return set_error(ctx, cuda_status(e), std::string("materialise: ") + cudaGetErrorString(e));
+    }
+    *out = d;
+    return DAGC_OK;
+}
+
+int empty_dag(dagc_context ctx, int nl, dagc_dag* out) {
+    return alloc_dag(ctx, nl, std::vector<uint64_t>(nl, 0), 0, out);
+}
+
+// --------------------------------------------------------- CreateFinalDAG --
+int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, uint64_t* n_words) {
+    *d_words = nullptr;
+    *n_words = 0;
+    if (d->num_leaves == 0) return DAGC_OK;
+    const uint64_t nn = d->num_nodes();
+    Layout L;
+    const size_t o_hdr = L.take<CallHeader>(1);
+    const uint64_t svt = scan_tiles(nn) + 1;
+    const size_t o_sv = L.take<uint64_t>(svt);
+    const size_t zero_bytes = L.off;
+    const size_t o_pos = L.take<uint32_t>(nn + 1);
+    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    char* b = static_cast<char*>(ctx->arena.base);
+    CallHeader* h = reinterpret_cast<CallHeader*>(b + o_hdr);
+    uint32_t* pos = reinterpret_cast<uint32_t*>(b + o_pos);
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+    FinalArgs a{};
+    a.masks = d->masks;
+    a.children = d->children;
+    a.num_nodes = nn;
+    a.leaves = d->leaves;
+    a.num_leaves = d->num_leaves;
+    a.level_offsets = d->d_level_offset;
+    a.num_levels = d->num_levels;
+    a.word_pos = pos;
+    a.d_total = &h->counts[0];
+    a.status = reinterpret_cast<uint64_t*>(b + o_sv);
+    a.tile_counter = &h->tile_counters[0];
+    a.err = &h->err;
+    a.grid_scan = grid_for(ctx->grid_scan / ctx->sms, ctx->sms, scan_tiles(nn));
+    a.grid_write = grid_for(8, ctx->sms, (nn + d->num_leaves + 255) / 256);
+    uint64_t node_words = 0;
+    if (nn) {
+        launch_final_positions(a, s);
+        DAGC_LAUNCHED(ctx);
+        DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, &h->counts[0], 8, cudaMemcpyDeviceToHost, s));
+        DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+        node_words = ctx->h_stage[0];
+    } else {
+        DAGC_CUDA(ctx, cudaMemsetAsync(pos, 0, 4, s));
+    }
+    const uint64_t total = node_words + 2 * d->num_leaves;
+    if (total >= (1ull << 32)) return set_error(ctx, DAGC_ERR_TOO_LARGE, "final DAG exceeds 2^32 words");
+    void* w = nullptr;
+    DAGC_CUDA(ctx, ctx->pool.alloc(&w, total * 4));
+    a.words = static_cast<uint32_t*>(w);
+    launch_final_write(a, s);
+    cudaError_t le = cudaGetLastError();
+    if (le == cudaSuccess) le = cudaMemcpyAsync(ctx->h_stage, h, 8, cudaMemcpyDeviceToHost, s);
+    if (le == cudaSuccess) le = cudaStreamSynchronize(s);
+    if (le != cudaSuccess) {
+        ctx->pool.release(w);
+        return set_error(ctx, cuda_status(le), std::string("final: ") + cudaGetErrorString(le));
+    }
+    std::string msg;
+    const int st = device_error_status((uint32_t)ctx->h_stage[0], msg);
+    if (st) { ctx->pool.release(w); return set_error(ctx, st, msg); }
+    *d_words = a.words;
+    *n_words = total;
+    return DAGC_OK;
+}
+
+// -------------------------------------------------------------- MergeDAGs --
+struct HostNode {
+    uint64_t hash;
+    uint8_t mask;
+    uint32_t ch[8];
+};
+
+int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_dag* out) {
+    const int nl = in[0]->num_levels;
+    int m = 0;
+    for (uint64_t x = k; x > 1; x /= 8) ++m;
+    uint64_t total_leaves = 0;
+    std::vector<uint64_t> level_total(nl, 0);
+    for (uint64_t i = 0; i < k; ++i) {
+        total_leaves += in[i]->num_leaves;
+        for (int l = 0; l < nl; ++l) level_total[l] += in[i]->level_offset[l + 1] - in[i]->level_offset[l];
+    }
+    const int out_levels = nl + m;
+    if (total_leaves == 0) return empty_dag(ctx, out_levels, out);
+    uint64_t capmax = total_leaves;
+    for (int l = 0; l < nl; ++l) capmax = std::max(capmax, level_total[l]);
+    if (capmax > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "merged level too large");
+
+    Layout L;
+    const size_t o_hdr = L.take<CallHeader>(1);
+    uint64_t sv_total = sv_words(total_leaves);
+    for (int l = 0; l < nl; ++l) sv_total += sv_words(level_total[l]);
+    const size_t o_sv = L.take<uint64_t>(sv_total);
+    const size_t zero_bytes = L.off;
+    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(capmax) * 256);
+    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(capmax) * 256);
+    const size_t o_KC = L.take<uint64_t>(capmax);
+    const size_t o_MC = L.take<uint8_t>(capmax);
+    const size_t o_CC = L.take<uint32_t>(capmax * 8);
+    const size_t o_SK = L.take<uint64_t>(capmax);
+    const size_t o_SKa = L.take<uint64_t>(capmax);
+    const size_t o_V = L.take<uint32_t>(capmax);
+    const size_t o_Va = L.take<uint32_t>(capmax);
+    const size_t o_M0 = L.take<uint32_t>(capmax);
+    const size_t o_M1 = L.take<uint32_t>(capmax);
+    const size_t o_PL = L.take<uint64_t>(total_leaves);
+    std::vector<size_t> o_ph(nl), o_pc(nl), o_pm(nl);
+    for (int l = 0; l < nl; ++l) {
+        o_ph[l] = L.take<uint64_t>(level_total[l]);
+        o_pc[l] = L.take<uint32_t>(level_total[l] * 8);
+        o_pm[l] = L.take<uint8_t>(level_total[l]);
+    }
+    const size_t o_root_hash = L.take<uint64_t>(k);
+    const size_t o_root_uid = L.take<uint32_t>(k);
+    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    char* b = static_cast<char*>(ctx->arena.base);
+    auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
+    auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
+    auto P8 = [&](size_t o) { return reinterpret_cast<uint8_t*>(b + o); };
+    CallSlots cs;
+    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
+    cs.sv_next = P64(o_sv);
+    cs.sv_end = P64(o_sv) + sv_total;
+    SortBuffers sb{{P32(o_ss0), P32(o_ss1)}};
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+    uint32_t* err = &cs.h->err;
+
+    // Leaves: sorted union of all inputs' leaves.
+    std::vector<uint64_t> prev_off(k + 1, 0);
+    for (uint64_t i = 0; i < k; ++i) {
+        prev_off[i + 1] = prev_off[i] + in[i]->num_leaves;
+        if (in[i]->num_leaves)
+            DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_KC) + prev_off[i], in[i]->leaves, in[i]->num_leaves * 8,
+                                           cudaMemcpyDeviceToDevice, s));
+    }
+    int st = run_sort(ctx, cs, sb, P64(o_KC), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
+                      total_leaves, nullptr, 0, 64, 0, s);
+    if (st) return st;
+    {
+        UniqueArgs a{};
+        a.keys = P64(o_SK);
+        a.perm = P32(o_V);
+        a.n_bound = total_leaves;
+        a.map = P32(o_M0);
+        a.out_keys = P64(o_PL);
+        a.out_capacity = total_leaves;
+        a.d_out_n = cs.count(kCntLeaves);
+        a.status = cs.sv(total_leaves);
+        a.tile_counter = cs.counter();
+        a.err = err;
+        a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(total_leaves));
+        launch_unique(a, s);
+        DAGC_LAUNCHED(ctx);
+    }
+    uint32_t* maps[2] = {P32(o_M0), P32(o_M1)};
+    int cur = 0;
+    for (int l = nl - 1; l >= 0; --l) {
+        std::vector<uint64_t> off(k + 1, 0);
+        for (uint64_t i = 0; i < k; ++i) {
+            const dagc_dag d = in[i];
+            const uint64_t a0 = d->level_offset[l], u = d->level_offset[l + 1] - a0;
+            off[i + 1] = off[i] + u;
+            if (!u) continue;
+            DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_KC) + off[i], d->hashes + a0, u * 8, cudaMemcpyDeviceToDevice, s));
+            DAGC_CUDA(ctx, cudaMemcpyAsync(P8(o_MC) + off[i], d->masks + a0, u, cudaMemcpyDeviceToDevice, s));
+            launch_remap_children(d->children + a0 * 8, maps[cur] + prev_off[i], P32(o_CC) + off[i] * 8, u, s);
+            DAGC_LAUNCHED(ctx);
+        }
+        const uint64_t nlev = off[k];
+        st = run_sort(ctx, cs, sb, P64(o_KC), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, nlev,
+                      nullptr, 0, 64, 0, s);
+        if (st) return st;
+        UniqueArgs u{};
+        u.keys = P64(o_SK);
+        u.perm = P32(o_V);
+        u.n_bound = nlev;
+        u.masks = P8(o_MC);
+        u.children = P32(o_CC);
+        u.map = maps[cur ^ 1];
+        u.out_keys = P64(o_ph[l]);
+        u.out_masks = P8(o_pm[l]);
+        u.out_children = P32(o_pc[l]);
+        u.out_capacity = level_total[l];
+        u.d_out_n = cs.count(kCntUnique + l);
+        u.status = cs.sv(level_total[l]);
+        u.tile_counter = cs.counter();
+        u.err = err;
+        u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(nlev));
+        launch_unique(u, s);
+        DAGC_LAUNCHED(ctx);
+        cur ^= 1;
+        prev_off = off;
+    }
+    // Root ids of every input in the merged top level (or the leaves when
+    // the inputs have no inner level), and their hashes.
+    std::vector<uint64_t> root_hash(k, 0);
+    std::vector<uint32_t> root_uid(k, kEmptyChild);
+    auto input_empty = [&](uint64_t i) { return nl > 0 ? in[i]->level_offset[1] == 0 : in[i]->num_leaves == 0; };
+    for (uint64_t i = 0; i < k; ++i) {
+        if (input_empty(i)) continue;
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P32(o_root_uid) + i, maps[cur] + prev_off[i], 4, cudaMemcpyDeviceToDevice, s));
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_root_hash) + i, nl > 0 ? in[i]->hashes : in[i]->leaves, 8,
+                                       cudaMemcpyDeviceToDevice, s));
+    }
+    std::vector<uint64_t> stage_hash(k, 0);
+    std::vector<uint32_t> stage_uid(k, 0);
+    DAGC_CUDA(ctx, cudaMemcpyAsync(stage_hash.data(), P64(o_root_hash), k * 8, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaMemcpyAsync(stage_uid.data(), P32(o_root_uid), k * 4, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, cs.h, 8 + 8 * 64, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    {
+        std::string msg;
+        st = device_error_status((uint32_t)(ctx->h_stage[0] & 0xFFFFFFFFu), msg);
+        if (st) return set_error(ctx, st, msg);
+    }
+    if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
+    const uint64_t* counts = ctx->h_stage + 1;
+    for (uint64_t i = 0; i < k; ++i) {
+        if (input_empty(i)) continue;
+        root_uid[i] = stage_uid[i];
+        root_hash[i] = stage_hash[i];
+    }
+
+    // Top levels: groups of 8 consecutive roots, built on the host like the
+    // reference (src/DAGCompression.cu:1504-1533), deduplicated by hash.
+    std::vector<std::vector<HostNode>> top;  // top[0] = just above the inputs
+    uint64_t groups = k;
+    while (groups > 1) {
+        const uint64_t ng = groups / 8;
+        std::vector<HostNode> cand;
+        std::vector<int64_t> cand_of(ng, -1);
+        for (uint64_t g = 0; g < ng; ++g) {
+            HostNode nd{};
+            uint64_t hs[8];
+            for (int c = 0; c < 8; ++c) {
+                hs[c] = root_hash[8 * g + c];
+                nd.ch[c] = root_uid[8 * g + c];
+                if (hs[c]) nd.mask |= (uint8_t)(1u << c);
+            }
+            nd.hash = hash_children(hs);
+            if (nd.mask) { cand_of[g] = (int64_t)cand.size(); cand.push_back(nd); }
+        }
+        std::vector<uint32_t> order(cand.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (uint32_t)i;
+        std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return cand[a].hash < cand[c].hash; });
+        std::vector<HostNode> lvl;
+        std::vector<uint32_t> uid_of(cand.size());
+        for (size_t i = 0; i < order.size(); ++i) {
+            const HostNode& nd = cand[order[i]];
+            if (lvl.empty() || lvl.back().hash != nd.hash) lvl.push_back(nd);
+            else if (lvl.back().mask != nd.mask || std::memcmp(lvl.back().ch, nd.ch, 32) != 0)
+                return set_error(ctx, DAGC_ERR_HASH_COLLISION, "64-bit node hash collision between different nodes");
+            uid_of[order[i]] = (uint32_t)(lvl.size() - 1);
+        }
+        std::vector<uint64_t> nh(ng, 0);
+        std::vector<uint32_t> nu(ng, kEmptyChild);
+        for (uint64_t g = 0; g < ng; ++g)
+            if (cand_of[g] >= 0) { nh[g] = cand[cand_of[g]].hash; nu[g] = uid_of[cand_of[g]]; }
+        root_hash = nh;
+        root_uid = nu;
+        top.push_back(std::move(lvl));
+        groups = ng;
+    }
+
+    // Materialise: top levels (root first), then the merged input levels.
+    std::vector<uint64_t> sizes(out_levels);
+    for (int t = 0; t < m; ++t) sizes[t] = top[m - 1 - t].size();
+    for (int l = 0; l < nl; ++l) sizes[m + l] = counts[kCntUnique + l];
+    dagc_dag d = nullptr;
+    st = alloc_dag(ctx, out_levels, sizes, counts[kCntLeaves], &d);
+    if (st) return st;
+    std::vector<uint64_t> th, tm8;
+    std::vector<uint32_t> tc;
+    for (int t = 0; t < m; ++t) {
+        for (const HostNode& nd : top[m - 1 - t]) {
+            th.push_back(nd.hash);
+            tm8.push_back(nd.mask);
+            tc.insert(tc.end(), nd.ch, nd.ch + 8);
+        }
+    }
+    std::vector<uint8_t> tm(tm8.begin(), tm8.end());
+    const uint64_t ntop = th.size();
+    cudaError_t ce = cudaSuccess;
+    if (ntop) {
+        ce = cudaMemcpyAsync(d->hashes, th.data(), ntop * 8, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->children, tc.data(), ntop * 32, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->masks, tm.data(), ntop, cudaMemcpyHostToDevice, s);
+    }
+    for (int l = 0; l < nl && !ce; ++l) {
+        const uint64_t o = d->level_offset[m + l], u = sizes[m + l];
+        if (!u) continue;
+        ce = cudaMemcpyAsync(d->hashes + o, P64(o_ph[l]), u * 8, cudaMemcpyDeviceToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->children + o * 8, P32(o_pc[l]), u * 32, cudaMemcpyDeviceToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->masks + o, P8(o_pm[l]), u, cudaMemcpyDeviceToDevice, s);
+    }
+    if (!ce && d->num_leaves) ce = cudaMemcpyAsync(d->leaves, P64(o_PL), d->num_leaves * 8, cudaMemcpyDeviceToDevice, s);
+    if (!ce) ce = cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (out_levels + 1) * 8, cudaMemcpyHostToDevice, s);
+    if (!ce) ce = cudaStreamSynchronize(s);
+    if (ce) {
+        free_dag(d);
+        cudaGetLastError();
+        return set_error(ctx, cuda_status(ce), std::string("merge: ") + cudaGetErrorString(ce));
+    }
+    *out = d;
+    return DAGC_OK;
+}
+
+bool valid_ctx(dagc_context ctx) { return ctx != nullptr; }
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+int dagc_version(void) { return 1; }
+
+const char* dagc_status_string(int status) {
+    switch (status) {
+        case DAGC_OK: return "ok";
+        case DAGC_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case DAGC_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case DAGC_ERR_BAD_INPUT: return "bad input";
+        case DAGC_ERR_HASH_COLLISION: return "hash collision";
+        case DAGC_ERR_DEVICE_TIMEOUT: return "device timeout";
+        case DAGC_ERR_CUDA: return "cuda error";
+        case DAGC_ERR_TOO_LARGE: return "too large";
+        default: return "unknown status";
+    }
+}
+
+int dagc_context_create(int device, dagc_context* out) {
+    if (!out) return DAGC_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+    std::unique_ptr<dagc_context_t> c(new dagc_context_t);
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    sort_configure();
+    kernels_configure();
+    e = cudaMallocHost(&c->h_stage, 4096);
+    if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+    int occ = 0;
+    // Persistent grid sizes: resident CTAs per SM x SMs.
+    occ = occupancy_sort_pass(true);  c->grid_pass_kv = std::max(1, occ) * c->sms;
+    occ = occupancy_sort_pass(false); c->grid_pass_k = std::max(1, occ) * c->sms;
+    c->grid_hist = 8 * c->sms;
+    c->grid_leaf = std::max(1, occupancy_kernel(0)) * c->sms;
+    c->grid_extract = std::max(1, occupancy_kernel(1)) * c->sms;
+    c->grid_unique = std::max(1, occupancy_kernel(2)) * c->sms;
+    c->grid_scan = std::max(1, occupancy_kernel(3)) * c->sms;
+    c->grid_write = 8 * c->sms;
+    *out = c.release();
+    return DAGC_OK;
+}
+
+void dagc_context_destroy(dagc_context ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    ctx->arena.release();
+    ctx->pool.trim();
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    delete ctx;
+}
+
+const char* dagc_last_error(dagc_context ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth, void* stream,
+                dagc_dag* out) {
+    if (!valid_ctx(ctx) || !out) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    if (depth < 2 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [2, 21]");
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+    if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int nl = depth - 2;
+    if (n == 0) {  // src/DAGCompression.cu:1010-1013
+        ctx->last_counts.assign(3 + nl, 0);
+        return empty_dag(ctx, nl, out);
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CreatePools p;
+    int st = create_pipeline(ctx, d_fragments, n, depth, s, p);
+    if (st) return st;
+    return materialise(ctx, p, nl, s, out);
+}
+
+int dagc_dag_num_levels(dagc_dag d, int* num_levels) {
+    if (!d || !num_levels) return DAGC_ERR_INVALID_ARGUMENT;
+    *num_levels = d->num_levels;
+    return DAGC_OK;
+}
+
+int dagc_dag_level_size(dagc_dag d, int level, uint64_t* n) {
+    if (!d || !n || level < 0 || level >= d->num_levels) return DAGC_ERR_INVALID_ARGUMENT;
+    *n = d->level_offset[level + 1] - d->level_offset[level];
+    return DAGC_OK;
+}
+
+int dagc_dag_num_leaves(dagc_dag d, uint64_t* n) {
+    if (!d || !n) return DAGC_ERR_INVALID_ARGUMENT;
+    *n = d->num_leaves;
+    return DAGC_OK;
+}
+
+int dagc_dag_level_device(dagc_dag d, int level, const uint8_t** m, const uint32_t** c, const uint64_t** h) {
+    if (!d || level < 0 || level >= d->num_levels) return DAGC_ERR_INVALID_ARGUMENT;
+    const uint64_t o = d->level_offset[level];
+    if (m) *m = d->masks + o;
+    if (c) *c = d->children + o * 8;
+    if (h) *h = d->hashes + o;
+    return DAGC_OK;
+}
+
+int dagc_dag_leaves_device(dagc_dag d, const uint64_t** leaves) {
+    if (!d || !leaves) return DAGC_ERR_INVALID_ARGUMENT;
+    *leaves = d->leaves;
+    return DAGC_OK;
+}
+
+int dagc_dag_download_level(dagc_dag d, int level, uint8_t* m, uint32_t* c, uint64_t* h) {
+    if (!d || level < 0 || level >= d->num_levels) return DAGC_ERR_INVALID_ARGUMENT;
+    dagc_context ctx = d->ctx;
+    const uint64_t o = d->level_offset[level], u = d->level_offset[level + 1] - o;
+    if (!u) return DAGC_OK;
+    if (m) DAGC_CUDA(ctx, cudaMemcpy(m, d->masks + o, u, cudaMemcpyDeviceToHost));
+    if (c) DAGC_CUDA(ctx, cudaMemcpy(c, d->children + o * 8, u * 32, cudaMemcpyDeviceToHost));
+    if (h) DAGC_CUDA(ctx, cudaMemcpy(h, d->hashes + o, u * 8, cudaMemcpyDeviceToHost));
+    return DAGC_OK;
+}
+
+int dagc_dag_download_leaves(dagc_dag d, uint64_t* leaves) {
+    if (!d || (!leaves && d->num_leaves)) return DAGC_ERR_INVALID_ARGUMENT;
+    if (d->num_leaves) DAGC_CUDA(d->ctx, cudaMemcpy(leaves, d->leaves, d->num_leaves * 8, cudaMemcpyDeviceToHost));
+    return DAGC_OK;
+}
+
+int dagc_dag_upload(dagc_context ctx, int num_levels, const uint64_t* sizes, const uint8_t* const* m,
+                    const uint32_t* const* c, const uint64_t* const* h, const uint64_t* leaves,
+                    uint64_t num_leaves, void* stream, dagc_dag* out) {
+    if (!valid_ctx(ctx) || !out || num_levels < 0 || num_levels > kMaxDepth - 2 || (num_levels && !sizes))
+        return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<uint64_t> sz(sizes, sizes + num_levels);
+    // Structural validation on the host, so that no kernel ever indexes out of
+    // bounds: children in range of the next level (or the leaves), the mask
+    // bit set exactly for the present children, hashes ascending and unique.
+    for (int l = 0; l < num_levels; ++l) {
+        if (sz[l] && (!m[l] || !c[l] || !h[l])) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null level array");
+        const uint64_t next = l + 1 < num_levels ? sz[l + 1] : num_leaves;
+        for (uint64_t i = 0; i < sz[l]; ++i) {
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t ch = c[l][i * 8 + k];
+                const bool has = (m[l][i] >> k) & 1;
+                if (has != (ch != kEmptyChild) || (has && ch >= next))
+                    return set_error(ctx, DAGC_ERR_BAD_INPUT, "malformed DAG level " + std::to_string(l));
+            }
+            if (i && h[l][i] <= h[l][i - 1]) return set_error(ctx, DAGC_ERR_BAD_INPUT, "level hashes not ascending");
+        }
+    }
+    for (uint64_t i = 1; i < num_leaves; ++i)
+        if (leaves[i] <= leaves[i - 1]) return set_error(ctx, DAGC_ERR_BAD_INPUT, "leaves not ascending");
+    dagc_dag d = nullptr;
+    int st = alloc_dag(ctx, num_levels, sz, num_leaves, &d);
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t ce = cudaSuccess;
+    for (int l = 0; l < num_levels && !ce; ++l) {
+        const uint64_t o = d->level_offset[l], u = sz[l];
+        if (!u) continue;
+        ce = cudaMemcpyAsync(d->masks + o, m[l], u, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->children + o * 8, c[l], u * 32, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->hashes + o, h[l], u * 8, cudaMemcpyHostToDevice, s);
+    }
+    if (!ce && num_leaves) ce = cudaMemcpyAsync(d->leaves, leaves, num_leaves * 8, cudaMemcpyHostToDevice, s);
+    if (!ce) ce = cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (num_levels + 1) * 8, cudaMemcpyHostToDevice, s);
+    if (!ce) ce = cudaStreamSynchronize(s);
+    if (ce) {
+        free_dag(d);
+        cudaGetLastError();
+        return set_error(ctx, cuda_status(ce), std::string("upload: ") + cudaGetErrorString(ce));
+    }
+    *out = d;
+    return DAGC_OK;
+}
+
+void dagc_dag_free(dagc_dag d) {
+    if (!d) return;
+    if (d->ctx) {
+        std::lock_guard<std::mutex> lock(d->ctx->mu);
+        free_dag(d);
+    } else {
+        delete d;
+    }
+}
+
+int dagc_merge(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_dag* out) {
+    if (!valid_ctx(ctx) || !out || !dags || k == 0) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    uint64_t x = k;
+    while (x > 1) {  // src/DAGCompression.cu:1451, :1467
+        if (x % 8) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "MergeDAGs needs 8^m inputs");
+        x /= 8;
+    }
+    for (uint64_t i = 0; i < k; ++i) {
+        if (!dags[i] || dags[i]->ctx != ctx) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad DAG handle");
+        if (dags[i]->num_levels != dags[0]->num_levels)
+            return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "sub-DAGs of different depths");
+    }
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (k == 1) { *out = dags[0]; dags[0] = nullptr; return DAGC_OK; }
+    const int st = merge_dags(ctx, dags, k, static_cast<cudaStream_t>(stream), out);
+    if (st) return st;
+    for (uint64_t i = 0; i < k; ++i) { free_dag(dags[i]); dags[i] = nullptr; }
+    return DAGC_OK;
+}
+
+int dagc_final(dagc_context ctx, dagc_dag dag, void* stream, uint32_t** d_words, uint64_t* n_words) {
+    if (!valid_ctx(ctx) || !dag || !d_words || !n_words || dag->ctx != ctx) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int st = final_dag(ctx, dag, static_cast<cudaStream_t>(stream), d_words, n_words);
+    if (st) return st;
+    free_dag(dag);
+    return DAGC_OK;
+}
+
+int dagc_free_words(dagc_context ctx, uint32_t* d_words, void* stream) {
+    (void)stream;
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->pool.release(d_words);
+    return DAGC_OK;
+}
+
+int dagc_words_download(dagc_context ctx, const uint32_t* d_words, uint64_t n, uint32_t* h_words) {
+    if (!valid_ctx(ctx) || (n && (!d_words || !h_words))) return DAGC_ERR_INVALID_ARGUMENT;
+    if (n) DAGC_CUDA(ctx, cudaMemcpy(h_words, d_words, n * 4, cudaMemcpyDeviceToHost));
+    return DAGC_OK;
+}
+
+int dagc_free_all(dagc_context ctx) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    DAGC_CUDA(ctx, cudaDeviceSynchronize());
+    ctx->arena.release();
+    ctx->pool.trim();
+    return DAGC_OK;
+}
+
+int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth, void* stream,
+                  uint32_t** d_words, uint64_t* n_words) {
+    if (!d_words || !n_words) return DAGC_ERR_INVALID_ARGUMENT;
+    dagc_dag d = nullptr;
+    int st = dagc_create(ctx, d_fragments, n, depth, stream, &d);
+    if (st) return st;
+    st = dagc_final(ctx, d, stream, d_words, n_words);
+    if (st) dagc_dag_free(d);
+    return st;
+}
+
+int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n, int depth, void* stream,
+                       uint32_t* h_words, uint64_t capacity, uint64_t* n_words) {
+    if (!valid_ctx(ctx) || !n_words || (n && !h_fragments)) return DAGC_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* d_in = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+        if (n) {
+            DAGC_CUDA(ctx, ctx->pool.alloc(&d_in, n * 8));
+            const cudaError_t e = cudaMemcpyAsync(d_in, h_fragments, n * 8, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) { ctx->pool.release(d_in); DAGC_CUDA(ctx, e); }
+        }
+    }
+    uint32_t* w = nullptr;
+    uint64_t nw = 0;
+    int st = dagc_compress(ctx, static_cast<const uint64_t*>(d_in), n, depth, stream, &w, &nw);
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        ctx->pool.release(d_in);
+    }
+    if (st) return st;
+    *n_words = nw;
+    if (h_words && capacity >= nw && nw) {
+        const cudaError_t e = cudaMemcpyAsync(h_words, w, nw * 4, cudaMemcpyDeviceToHost, s);
+        const cudaError_t e2 = e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+        dagc_free_words(ctx, w, stream);
+        if (e2 != cudaSuccess) { cudaGetLastError(); return set_error(ctx, cuda_status(e2), cudaGetErrorString(e2)); }
+        return DAGC_OK;
+    }
+    dagc_free_words(ctx, w, stream);
+    return h_words && capacity < nw ? set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "word buffer too small") : DAGC_OK;
+}
+
+int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap) {
+    if (!valid_ctx(ctx) || (!out && cap > 0)) return 0;
+    const int k = std::min<int>(cap, (int)ctx->last_counts.size());
+    for (int i = 0; i < k; ++i) out[i] = ctx->last_counts[i];
+    return k;
+}
+
+int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint64_t n, int lo, int hi, void* stream) {
+    return dagc_sort_pairs(ctx, d_in, d_out, nullptr, nullptr, n, lo, hi, stream);
+}
+
+int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out, const uint32_t* d_vals_in,
+                    uint32_t* d_vals_out, uint64_t n, int lo, int hi, void* stream) {
+    if (!valid_ctx(ctx) || lo < 0 || hi > 64 || lo > hi) return DAGC_ERR_INVALID_ARGUMENT;
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 keys");
+    if (n == 0) return DAGC_OK;
+    if (!d_keys_in || !d_keys_out || d_keys_in == d_keys_out) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad key buffers");
+    const bool with_values = d_vals_out != nullptr;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Layout L;
+    const size_t o_hdr = L.take<CallHeader>(1);
+    const size_t zero_bytes = L.off;
+    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+    const size_t o_ka = L.take<uint64_t>(n);
+    const size_t o_va = L.take<uint32_t>(with_values ? n : 0);
+    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    char* b = static_cast<char*>(ctx->arena.base);
+    CallSlots cs;
+    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
+    SortBuffers sb{{reinterpret_cast<uint32_t*>(b + o_ss0), reinterpret_cast<uint32_t*>(b + o_ss1)}};
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+    int st = run_sort(ctx, cs, sb, d_keys_in, d_keys_out, reinterpret_cast<uint64_t*>(b + o_ka), d_vals_in, d_vals_out,
+                      with_values ? reinterpret_cast<uint32_t*>(b + o_va) : nullptr, with_values, n, nullptr, lo, hi, 0, s);
+    if (st) return st;
+    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, cs.h, 8, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    std::string msg;
+    st = device_error_status((uint32_t)ctx->h_stage[0], msg);
+    return st ? set_error(ctx, st, msg) : DAGC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// Host-side declarations of the dagc kernel launchers (implemented in the .cu
+// files). Plain C++: the orchestrator (dagc.cpp) includes this header only.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dagc_hash.h"  // DAGC_HD
+
+namespace dagc {
+
+// ------------------------------------------------------------ error bits ----
+// Kernels never trap: they OR one of these into the call's error word and
+// carry on with a defined (if meaningless) value so that every wait still ends.
+enum : uint32_t {
+    kErrBadInput = 1u,      // fragment code >= 2^(3*depth)
+    kErrCollision = 2u,     // equal 64-bit hash, different node
+    kErrTimeout = 4u,       // a bounded wait ran out
+    kErrCapacity = 8u,      // an upper bound on a buffer was exceeded
+    kErrNotRooted = 16u,    // level 0 does not hold exactly one node
+    kErrMergeRoot = 32u,    // a sub-DAG root hash missing from the merged level
+};
+
+constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;
+
+
+// ---------------------------------------------------------------- sort ----
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
+constexpr int kRadixBits = 8;
+constexpr int kMaxPasses = 8;
+
+DAGC_HD uint32_t sort_tiles(uint64_t n) { return (uint32_t)((n + kSortTile - 1) / kSortTile); }
+
+// Device count pointer convention: when d_n is non-null the kernels read the
+// element count from device memory (written by an earlier kernel) and n is an
+// upper bound used only to size the grid; otherwise n is the count.
+struct SortArgs {
+    const uint64_t* keys_in;
+    uint64_t* keys_out;
+    uint64_t* keys_alt;       // ping-pong buffer (n elements)
+    const uint32_t* vals_in;  // null with with_values -> values are 0..n-1
+    uint32_t* vals_out;
+    uint32_t* vals_alt;
+    bool with_values;
+    uint64_t n;               // count or upper bound (see d_n)
+    const uint64_t* d_n;
+    int lo_bit, hi_bit;
+    int validate_bits;        // > 0: flag keys with bits >= validate_bits set
+    uint32_t* hist;           // kMaxPasses * 256 words, zeroed
+    uint32_t* status[2];      // 2 x sort_tiles(n) * 256 words; status[0] zeroed on entry
+    uint32_t* tile_counters;  // kMaxPasses words, zeroed
+    uint32_t* err;
+    int grid_hist, grid_pass; // persistent grid sizes
+};
+
+// Number of digit passes for a bit range.
+DAGC_HD int sort_passes(int lo_bit, int hi_bit) {
+    return hi_bit > lo_bit ? (hi_bit - lo_bit + kRadixBits - 1) / kRadixBits : 0;
+}
+// Where the result lands: keys_out always (the pass sequence is arranged so).
+void launch_sort(const SortArgs& a, cudaStream_t s);
+size_t sort_pass_smem(bool with_values);
+void sort_configure();  // sets shared-memory attributes once per device
+
+// ---------------------------------------------------------- DAG kernels ----
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+DAGC_HD uint32_t scan_tiles(uint64_t n) { return (uint32_t)((n + kScanTile - 1) / kScanTile); }
+
+// Fused unique + 4x4x4 leaf build over fragments sorted by (code >> 6):
+// parents[p] = code >> 6 and leaves[p] = OR of 1 << (code & 63) per distinct
+// parent; *d_out_n = number of parents.
+struct LeafBuildArgs {
+    const uint64_t* sorted; const uint64_t* d_n; uint64_t n_bound;
+    uint64_t* parents; uint64_t* leaves; uint64_t out_capacity; uint64_t* d_out_n;
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
+};
+void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s);
+
+// Unique over (key, perm) sorted by key: uid = rank of the key among distinct
+// keys; map[perm[i]] = uid; for the first of each run, out_keys[uid] = key and
+// payloads are gathered from perm. With node payloads (masks/children) the
+// run members are compared in full (collision check).
+//
+// Every kernel that produces a count is given the capacity of its outputs: it
+// never writes past it, clamps the count (and ids) it publishes to it and
+// flags kErrCapacity, so that later kernels stay inside their buffers even on
+// rejected input.
+struct UniqueArgs {
+    const uint64_t* keys; const uint32_t* perm; const uint64_t* d_n; uint64_t n_bound;
+    const uint8_t* masks; const uint32_t* children;  // null for leaves
+    uint32_t* map;
+    uint64_t* out_keys; uint8_t* out_masks; uint32_t* out_children;
+    uint64_t out_capacity;
+    uint64_t* d_out_n;
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
+};
+void launch_unique(const UniqueArgs& a, cudaStream_t s);
+
+// ExtractLevel + ComputeHashes: from the sorted unique codes of the child
+// level and their child ids, build one parent node per distinct code >> 3.
+struct ExtractArgs {
+    const uint64_t* child_codes; const uint32_t* child_map; const uint64_t* d_n; uint64_t n_bound;
+    const uint64_t* child_hashes;  // unique child hashes (or leaf masks), indexed by child id
+    uint64_t* node_codes; uint8_t* node_masks; uint32_t* node_children; uint64_t* node_hashes;
+    uint64_t out_capacity;
+    uint64_t* d_out_n;
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
+};
+void launch_extract(const ExtractArgs& a, cudaStream_t s);
+
+// Final layout: word position of every node (exclusive scan of popc+1 over all
+// levels concatenated), then headers, child pointers and leaves.
+struct FinalArgs {
+    const uint8_t* masks; const uint32_t* children; uint64_t num_nodes;
+    const uint64_t* leaves; uint64_t num_leaves;
+    const uint64_t* level_offsets; int num_levels;  // device, num_levels + 1 entries
+    uint32_t* word_pos;  // num_nodes + 1
+    uint64_t* d_total;   // exact 64-bit sum of node words
+    uint32_t* words;
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid_scan, grid_write;
+};
+void launch_final_positions(const FinalArgs& a, cudaStream_t s);
+void launch_final_write(const FinalArgs& a, cudaStream_t s);
+
+// Gathers / copies used by the merge and the compaction of level outputs.
+void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* out, uint64_t n_nodes,
+                           cudaStream_t s);
+void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s);
+
+void kernels_configure();
+
+// Resident CTAs per SM of the persistent kernels (for grid sizing).
+int occupancy_sort_pass(bool with_values);
+enum KernelId { kKernelLeafBuild = 0, kKernelExtract = 1, kKernelUnique = 2, kKernelFinalScan = 3 };
+int occupancy_kernel(int which);
+
+}  // namespace dagc

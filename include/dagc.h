@@ -1,0 +1,142 @@
+/* dagc — GB300-native sparse voxel DAG compression: C ABI.
+ *
+ * Shuffled uint64 Morton fragment codes go in; a deduplicated sparse voxel DAG
+ * comes out, first in the reference's intermediate hash-sorted form (FCpuDag,
+ * src/DAGCompression.h:6-40 of Phyronnaz/DAG_Compression_Fast), then in its
+ * final uint32 node/leaf word layout (src/DAGCompression.cu:1550-1610).
+ *
+ * Every entry point takes plain pointers and sizes; device pointers are
+ * prefixed d_, host pointers h_. `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream). Every function returns a dagc status
+ * code; dagc_last_error() gives the message of the last failure on a context.
+ * The library never aborts or traps.
+ *
+ * Limits: depth in [2, 21] (3 * depth <= 64 code bits), fewer than 2^30
+ * fragments per call, fewer than 2^32 words in a final DAG.
+ */
+#ifndef DAGC_H
+#define DAGC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DAGC_OK 0
+#define DAGC_ERR_INVALID_ARGUMENT 1
+#define DAGC_ERR_OUT_OF_MEMORY 2
+#define DAGC_ERR_BAD_INPUT 3        /* a fragment code >= 2^(3*depth) */
+#define DAGC_ERR_HASH_COLLISION 4   /* two different nodes with one 64-bit hash */
+#define DAGC_ERR_DEVICE_TIMEOUT 5   /* a bounded device-side wait ran out */
+#define DAGC_ERR_CUDA 6
+#define DAGC_ERR_TOO_LARGE 7        /* beyond the limits above */
+
+typedef struct dagc_context_t* dagc_context;
+typedef struct dagc_dag_t* dagc_dag;
+
+/* ------------------------------------------------------------ context ---- */
+/* One context per host thread (or lock around it). It owns the device scratch
+ * arena and the stream-ordered pool the DAG arrays come from. */
+int dagc_context_create(int device, dagc_context* out);
+void dagc_context_destroy(dagc_context ctx);
+const char* dagc_last_error(dagc_context ctx);
+const char* dagc_status_string(int status);
+int dagc_version(void);
+
+/* ------------------------------------------------------------ CreateDAG ---- */
+/* Replaces DAGCompression::CreateDAG (src/DAGCompression.h:45,
+ * src/DAGCompression.cu:1003-1107). d_fragments: n device Morton codes, each
+ * < 2^(3*depth), duplicates allowed, any order; left unchanged (the reference
+ * reuses that buffer as scratch, this library does not). Synchronous on return
+ * like the reference. *out receives a device-resident DAG: depth-2 levels,
+ * level 0 = root, each level ascending by node hash, plus ascending leaves. */
+int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth,
+                void* stream, dagc_dag* out);
+
+/* -------------------------------------------------------- DAG accessors ---- */
+int dagc_dag_num_levels(dagc_dag dag, int* num_levels);
+int dagc_dag_level_size(dagc_dag dag, int level, uint64_t* num_nodes);
+int dagc_dag_num_leaves(dagc_dag dag, uint64_t* num_leaves);
+/* Device arrays of one level: masks uint8[n], children uint32[n][8]
+ * (0xFFFFFFFF = empty slot; indices into level+1, or into the leaves for the
+ * last level), hashes uint64[n]. Valid until the DAG is freed or consumed. */
+int dagc_dag_level_device(dagc_dag dag, int level, const uint8_t** d_masks,
+                          const uint32_t** d_children, const uint64_t** d_hashes);
+int dagc_dag_leaves_device(dagc_dag dag, const uint64_t** d_leaves);
+/* Host copies (FCpuLevel::ToCPU, src/DAGCompression.cu:788-803). Any of the
+ * output pointers may be NULL. */
+int dagc_dag_download_level(dagc_dag dag, int level, uint8_t* h_masks, uint32_t* h_children,
+                            uint64_t* h_hashes);
+int dagc_dag_download_leaves(dagc_dag dag, uint64_t* h_leaves);
+/* Builds a device DAG from host arrays (FGpuLevel::FromCPU,
+ * src/DAGCompression.cu:804-816), e.g. an FCpuDag produced elsewhere. */
+int dagc_dag_upload(dagc_context ctx, int num_levels, const uint64_t* level_sizes,
+                    const uint8_t* const* h_masks, const uint32_t* const* h_children,
+                    const uint64_t* const* h_hashes, const uint64_t* h_leaves,
+                    uint64_t num_leaves, void* stream, dagc_dag* out);
+void dagc_dag_free(dagc_dag dag);
+
+/* ------------------------------------------------------------ MergeDAGs ---- */
+/* Replaces DAGCompression::MergeDAGs (src/DAGCompression.h:46,
+ * src/DAGCompression.cu:1446-1548). k = 8^m sub-DAGs of equal depth in Morton
+ * order of their subvolumes (empty ones allowed); the result has m more
+ * levels. Consumes (frees) the inputs, like the reference's rvalue argument.
+ * Runs entirely on the device. */
+int dagc_merge(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_dag* out);
+
+/* ------------------------------------------------------- CreateFinalDAG ---- */
+/* Replaces DAGCompression::CreateFinalDAG (src/DAGCompression.h:47,
+ * src/DAGCompression.cu:1550-1610). Consumes the DAG. *d_words receives a
+ * device array of *n_words uint32 (root at word 0), owned by the caller and
+ * released with dagc_free_words. An empty DAG gives 0 words and NULL. */
+int dagc_final(dagc_context ctx, dagc_dag dag, void* stream, uint32_t** d_words,
+               uint64_t* n_words);
+int dagc_free_words(dagc_context ctx, uint32_t* d_words, void* stream);
+/* Copies n words of a final DAG to host memory (synchronous). */
+int dagc_words_download(dagc_context ctx, const uint32_t* d_words, uint64_t n, uint32_t* h_words);
+
+/* -------------------------------------------------------------- FreeAll ---- */
+/* Replaces DAGCompression::FreeAll (src/DAGCompression.h:48): releases the
+ * cached scratch arena and trims the pool. */
+int dagc_free_all(dagc_context ctx);
+
+/* --------------------------------------------------- end-to-end (host) ---- */
+/* CreateDAG + CreateFinalDAG from host fragments to host words: copies the
+ * fragments in, compresses, copies the words out. If h_words is NULL or
+ * capacity is too small only *n_words is set (and DAGC_ERR_INVALID_ARGUMENT is
+ * returned when h_words is non-NULL). */
+int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n, int depth,
+                       void* stream, uint32_t* h_words, uint64_t capacity, uint64_t* n_words);
+
+/* Fused device path: CreateDAG + CreateFinalDAG without materialising the
+ * intermediate DAG. Same result as dagc_create followed by dagc_final. */
+int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth,
+                  void* stream, uint32_t** d_words, uint64_t* n_words);
+
+/* --------------------------------------------------------- statistics ---- */
+/* Counts of the last dagc_create / dagc_compress on this context:
+ * out[0] = fragments, out[1] = distinct 4x4x4 bricks (leaf parents),
+ * out[2] = unique leaves, out[3 + l] = nodes of level l before dedup for
+ * l in [0, depth-2). Returns the number of values written (<= cap). */
+int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
+
+/* ------------------------------------------------------------- sorting ---- */
+/* The fragment sort as a standalone primitive: stable LSD radix sort of n
+ * uint64 keys on bits [lo_bit, hi_bit), d_in -> d_out (may not alias). The
+ * reference wraps cub::DeviceRadixSort::SortKeys (src/DAGCompression.cu:336-357). */
+int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint64_t n,
+                   int lo_bit, int hi_bit, void* stream);
+/* Pairs variant with uint32 values (src/DAGCompression.cu:359-394). d_vals_in
+ * may be NULL: the values are then the input positions 0..n-1 (MakeSequence,
+ * src/DAGCompression.cu:743-750). */
+int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out,
+                    const uint32_t* d_vals_in, uint32_t* d_vals_out, uint64_t n, int lo_bit,
+                    int hi_bit, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DAGC_H */

@@ -1,0 +1,193 @@
+"""GPU parity tests: the CUDA path (through the dagc C ABI) against the CPU
+oracle, bit-exact, on seeded inputs, edge cases and full-size workloads."""
+import numpy as np
+import pytest
+
+import dag_compression_fast_gb300 as D
+from oracle import oracle as O
+from oracle.decode import decode_final
+from tests.inputs import chunks_of, random_codes
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_dag_equal(gpu: D.HostDag, ref: O.Dag):
+    assert gpu.num_levels == ref.num_levels
+    assert gpu.level_sizes() == ref.level_sizes()
+    assert np.array_equal(gpu.leaves, ref.leaves)
+    for l in range(ref.num_levels):
+        assert np.array_equal(gpu.hashes[l], ref.hashes[l]), f"hashes of level {l}"
+        assert np.array_equal(gpu.masks[l], ref.masks[l]), f"masks of level {l}"
+        assert np.array_equal(gpu.children[l], ref.children[l]), f"children of level {l}"
+
+
+def clustered_codes(depth, n, seed):
+    return random_codes(depth, n, seed, cluster=True)
+
+
+# ------------------------------------------------------------------ sort ----
+@pytest.mark.parametrize("n", [1, 2, 100, 4095, 4096, 4097, 65_537, 1_000_003])
+@pytest.mark.parametrize("lo,hi", [(0, 64), (6, 33), (0, 3), (61, 64)])
+def test_sort_keys_matches_stable_numpy(ctx, n, lo, hi):
+    rng = np.random.default_rng(n * 131 + lo)
+    k = rng.integers(0, 2**64 - 1, n, dtype=np.uint64)
+    if n > 10:
+        k[: n // 3] = k[0]  # long runs of one key
+    out = ctx.sort_keys(k, lo, hi).cpu().numpy().view(np.uint64)
+    mask = np.uint64((1 << (hi - lo)) - 1) if hi - lo < 64 else np.uint64(2**64 - 1)
+    expect = k[np.argsort((k >> np.uint64(lo)) & mask, kind="stable")]
+    assert np.array_equal(out, expect)
+
+
+@pytest.mark.parametrize("n", [1, 5000, 300_001])
+def test_sort_pairs_iota_is_stable_permutation(ctx, n):
+    rng = np.random.default_rng(n)
+    k = rng.integers(0, 1000, n, dtype=np.uint64)  # many ties
+    keys, vals = ctx.sort_pairs(k)
+    keys = keys.cpu().numpy().view(np.uint64)
+    vals = vals.cpu().numpy().view(np.uint32)
+    order = np.argsort(k, kind="stable")
+    assert np.array_equal(keys, k[order])
+    assert np.array_equal(vals, order.astype(np.uint32))
+
+
+# ------------------------------------------------------------ CreateDAG ----
+CASES = {
+    "sphere_d7": lambda: (D.gen_sphere_shell(7, 0xDA6C0DE), 7),
+    "terrain_d8": lambda: (D.gen_terrain(8, 3), 8),
+    "random_dense_d5": lambda: (random_codes(5, 50_000, 1), 5),
+    "clustered_d10": lambda: (clustered_codes(10, 200_000, 2), 10),
+    "tiny_d3": lambda: (np.array([69, 0, 69, 5], np.uint64), 3),
+    "depth2": lambda: (np.array([0, 63, 7, 7], np.uint64), 2),
+    "single": lambda: (np.array([12345], np.uint64), 9),
+    "all_duplicates": lambda: (np.full(100_000, 777, np.uint64), 6),
+    "sparse_d21": lambda: (np.random.default_rng(4).integers(0, 2**63, 20_000, dtype=np.uint64), 21),
+    "soup_d10": lambda: (D.gen_triangle_soup(10, 5, 3000, threads=4), 10),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_create_dag_bit_exact(ctx, case):
+    codes, depth = CASES[case]()
+    ref = O.create_dag(codes, depth)
+    dag = ctx.create_dag(codes, depth)
+    assert_dag_equal(dag.to_host(), ref)
+    words = ctx.create_final_dag(dag)
+    w = words.to_numpy()
+    assert np.array_equal(w, O.final_dag(ref))
+    assert np.array_equal(decode_final(w, depth), np.unique(codes))
+
+
+def test_counts_reported(ctx):
+    codes, depth = CASES["sphere_d7"]()
+    ctx.create_dag(codes, depth).free()
+    c = ctx.last_counts()
+    ref = O.create_dag(codes, depth)
+    assert c[0] == codes.size
+    assert c[2] == ref.leaves.size
+
+
+def test_empty_input(ctx):
+    dag = ctx.create_dag(np.zeros(0, np.uint64), 7)
+    assert dag.level_sizes() == [0] * 5 and dag.num_leaves == 0
+    assert ctx.create_final_dag(dag).n == 0
+
+
+def test_out_of_range_code_is_bad_input(ctx):
+    codes = random_codes(7, 10_000, 3)
+    codes[1234] = np.uint64(1 << 21)
+    with pytest.raises(D.DagcError) as e:
+        ctx.create_dag(codes, 7)
+    assert e.value.status == D.ERR_BAD_INPUT
+    # The context stays usable after a rejected input.
+    ok = random_codes(7, 1000, 4)
+    assert_dag_equal(ctx.create_dag(ok, 7).to_host(), O.create_dag(ok, 7))
+
+
+def test_bad_depth_rejected(ctx):
+    with pytest.raises(D.DagcError) as e:
+        ctx.create_dag(np.array([1], np.uint64), 22)
+    assert e.value.status == D.ERR_INVALID_ARGUMENT
+
+
+def test_arena_reuse_large_then_small(ctx):
+    big = clustered_codes(11, 1_500_000, 8)
+    small = random_codes(6, 500, 9)
+    for codes, depth in ((big, 11), (small, 6), (big, 11)):
+        assert_dag_equal(ctx.create_dag(codes, depth).to_host(), O.create_dag(codes, depth, threads=8))
+
+
+def test_compress_host_and_fused(ctx):
+    codes, depth = CASES["terrain_d8"]()
+    ref_words = O.final_dag(O.create_dag(codes, depth))
+    assert np.array_equal(ctx.compress_host(codes, depth), ref_words)
+    assert np.array_equal(ctx.compress(codes, depth).to_numpy(), ref_words)
+
+
+def test_input_left_unchanged(ctx):
+    import torch
+    codes = random_codes(8, 100_000, 12)
+    t = torch.from_numpy(codes.view(np.int64)).cuda()
+    ctx.create_dag(t, 8).free()
+    assert np.array_equal(t.cpu().numpy().view(np.uint64), codes)
+
+
+# -------------------------------------------------------------- MergeDAGs ----
+@pytest.mark.parametrize("depth,levels_up,seed", [(7, 1, 1), (9, 2, 2), (8, 1, 3)])
+def test_merge_bit_exact(ctx, depth, levels_up, seed):
+    codes = clustered_codes(depth, 100_000, seed)
+    codes = codes[(codes >> np.uint64(3 * (depth - 1))) != np.uint64(5)]  # one empty octant
+    chunks, sub = chunks_of(codes, depth, levels_up)
+    ref_parts = [O.create_dag(c, sub) for c in chunks]
+    ref = O.merge_dags(ref_parts)
+    gpu = ctx.merge_dags([ctx.create_dag(c, sub) for c in chunks])
+    assert_dag_equal(gpu.to_host(), ref)
+    # ... and equals compressing the whole volume at once.
+    assert O.dags_equal(ref, O.create_dag(codes, depth))
+    assert np.array_equal(ctx.create_final_dag(gpu).to_numpy(), O.final_dag(ref))
+
+
+def test_merge_all_empty(ctx):
+    gpu = ctx.merge_dags([ctx.create_dag(np.zeros(0, np.uint64), 5) for _ in range(8)])
+    assert gpu.level_sizes() == [0] * 4 and gpu.num_leaves == 0
+
+
+def test_merge_collision_detected_on_device(ctx):
+    # Two uploaded DAGs whose level-0 nodes share a hash but differ in content:
+    # the merge's full compare must report a collision instead of picking one.
+    def one(mask, child, h):
+        return D.HostDag(masks=[np.array([mask], np.uint8)],
+                         children=[np.array([[child if (mask >> c) & 1 else 0xFFFFFFFF for c in range(8)]],
+                                            np.uint32)],
+                         hashes=[np.array([h], np.uint64)],
+                         leaves=np.array([1], np.uint64))
+    empty = D.HostDag(masks=[np.zeros(0, np.uint8)], children=[np.zeros((0, 8), np.uint32)],
+                      hashes=[np.zeros(0, np.uint64)], leaves=np.zeros(0, np.uint64))
+    parts = [ctx.upload_dag(one(1, 0, 42)), ctx.upload_dag(one(2, 0, 42))]
+    parts += [ctx.upload_dag(empty) for _ in range(6)]
+    with pytest.raises(D.DagcError) as e:
+        ctx.merge_dags(parts)
+    assert e.value.status == D.ERR_HASH_COLLISION
+
+
+def test_upload_rejects_malformed(ctx):
+    bad = D.HostDag(masks=[np.array([1], np.uint8)],
+                    children=[np.array([[5] + [0xFFFFFFFF] * 7], np.uint32)],  # child 5 of 1 leaf
+                    hashes=[np.array([7], np.uint64)], leaves=np.array([1], np.uint64))
+    with pytest.raises(D.DagcError) as e:
+        ctx.upload_dag(bad)
+    assert e.value.status == D.ERR_BAD_INPUT
+
+
+# -------------------------------------------------------- full-size cases ----
+def test_terrain_2048_full_size_bit_exact(ctx):
+    """Procedural terrain, 2048^3 (depth 11), ~31M fragments: exact against the
+    multi-threaded oracle, and decoded back to the input voxel set."""
+    codes = D.gen_terrain(11, 0xDA6C0DE + 1)
+    assert codes.size > 30_000_000
+    ref = O.create_dag(codes, 11, threads=16)
+    dag = ctx.create_dag(codes, 11)
+    assert_dag_equal(dag.to_host(), ref)
+    w = ctx.create_final_dag(dag).to_numpy()
+    assert np.array_equal(w, O.final_dag(ref))
+    assert np.array_equal(decode_final(w, 11), np.unique(codes))
