@@ -43,8 +43,12 @@ DAGC_SYMBOLS = [
     "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_free",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
-    "dagc_compress", "dagc_last_counts", "dagc_sort_keys", "dagc_sort_pairs",
+    "dagc_compress", "dagc_last_counts", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
 ]
+
+STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
+          "final", "merge"]
 GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
                "dagc_gen_triangle_soup", "dagc_gen_batched"]
 
@@ -102,6 +106,10 @@ def lib() -> ctypes.CDLL:
         L.dagc_compress_host.argtypes = [vp, vp, u64, i32, vp, vp, u64, pu64]
         L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
+        L.dagc_profile_enable.argtypes = [vp, i32]
+        L.dagc_profile_reset.argtypes = [vp]
+        L.dagc_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), pu64, pu64]
+        L.dagc_kernel_launches.argtypes = [vp, pu64]
         L.dagc_sort_keys.argtypes = [vp, vp, vp, u64, i32, i32, vp]
         L.dagc_sort_pairs.argtypes = [vp, vp, vp, vp, vp, u64, i32, i32, vp]
         _lib = L
@@ -356,6 +364,27 @@ class Context:
     def free_all(self):
         """DAGCompression::FreeAll."""
         self._check(lib().dagc_free_all(self.handle))
+
+    def profile(self, enable: bool = True):
+        """Turns per-stage CUDA-event timing on or off (see include/dagc.h)."""
+        self._check(lib().dagc_profile_enable(self.handle, int(enable)))
+
+    def profile_reset(self):
+        self._check(lib().dagc_profile_reset(self.handle))
+
+    def profile_read(self):
+        """{stage: (device_ms, launches, algorithmic_bytes)} accumulated so far."""
+        out = {}
+        for i, name in enumerate(STAGES):
+            ms, la, by = ctypes.c_double(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+            self._check(lib().dagc_profile_read(self.handle, i, ctypes.byref(ms), ctypes.byref(la), ctypes.byref(by)))
+            out[name] = (ms.value, la.value, by.value)
+        return out
+
+    def kernel_launches(self) -> int:
+        n = ctypes.c_uint64(0)
+        self._check(lib().dagc_kernel_launches(self.handle, ctypes.byref(n)))
+        return n.value
 
     def last_counts(self):
         buf = (ctypes.c_uint64 * 64)()

@@ -150,8 +150,26 @@ struct Layout {
 
 using namespace dagc;
 
+struct StageStats {
+    double ms = 0;
+    uint64_t launches = 0;
+    uint64_t bytes = 0;
+};
+
+struct PendingTiming {
+    int stage;
+    cudaEvent_t a, b;
+    uint64_t launches;
+    uint64_t bytes;
+};
+
 struct dagc_context_t {
     int device = 0;
+    bool profiling = false;
+    StageStats stages[DAGC_NUM_STAGES];
+    std::vector<cudaEvent_t> free_events;
+    std::vector<PendingTiming> pending;
+    uint64_t launches = 0;
     int sms = 152;
     int grid_hist = 0, grid_pass_kv = 0, grid_pass_k = 0;
     int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
@@ -199,6 +217,66 @@ int cuda_status(cudaError_t e) {
 
 #define DAGC_LAUNCHED(ctx) DAGC_CUDA(ctx, cudaGetLastError())
 
+cudaEvent_t take_event(dagc_context ctx) {
+    if (!ctx->free_events.empty()) {
+        cudaEvent_t e = ctx->free_events.back();
+        ctx->free_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return e;
+}
+
+// Brackets the launches of one stage with events on the call's stream when
+// profiling is on; bytes may be filled in later (see settle_bytes).
+struct StageTimer {
+    dagc_context ctx;
+    int stage;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    uint64_t launches0 = 0;
+    // stage < 0 disables the timer.
+    StageTimer(dagc_context c, int st, cudaStream_t stream) : ctx(c), stage(st), s(stream) {
+        launches0 = ctx->launches;
+        if (st >= 0 && ctx->profiling && (a = take_event(ctx))) cudaEventRecord(a, s);
+    }
+    void stop(uint64_t bytes = 0) {
+        if (!a) return;
+        cudaEvent_t b = take_event(ctx);
+        if (!b) { ctx->free_events.push_back(a); a = nullptr; return; }
+        cudaEventRecord(b, s);
+        ctx->pending.push_back({stage, a, b, ctx->launches - launches0, bytes});
+        a = nullptr;
+    }
+};
+
+// Fills in the algorithmic bytes of pending timings of `stage` recorded
+// without them (their sizes were only known on the device at launch time).
+void set_pending_bytes(dagc_context ctx, int stage, uint64_t bytes) {
+    for (PendingTiming& p : ctx->pending)
+        if (p.stage == stage && p.bytes == 0) p.bytes = bytes;
+}
+
+// Called after a stream synchronisation: folds the finished event pairs into
+// the per-stage totals.
+void settle_profile(dagc_context ctx) {
+    for (const PendingTiming& p : ctx->pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            StageStats& st = ctx->stages[p.stage];
+            st.ms += ms;
+            st.launches += p.launches;
+            st.bytes += p.bytes;
+        } else {
+            cudaGetLastError();
+        }
+        ctx->free_events.push_back(p.a);
+        ctx->free_events.push_back(p.b);
+    }
+    ctx->pending.clear();
+}
+
 int grid_for(int per_sm, int sms, uint64_t tiles) {
     const uint64_t g = (uint64_t)std::max(per_sm, 1) * (uint64_t)sms;
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, std::max<uint64_t>(tiles, 1)));
@@ -238,10 +316,12 @@ struct SortBuffers {
     uint32_t* status[2];
 };
 
+// pass_stage >= 0: time the histogram under hist_stage and every digit pass
+// separately under pass_stage (host-known n only, for the byte counts).
 int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint64_t* keys_in,
              uint64_t* keys_out, uint64_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
              uint32_t* vals_alt, bool with_values, uint64_t n_bound, const uint64_t* d_n, int lo, int hi,
-             int validate_bits, cudaStream_t s) {
+             int validate_bits, cudaStream_t s, int hist_stage = -1, int pass_stage = -1) {
     if (cs.next_hist >= kMaxSorts || cs.next_counter + kMaxPasses > kMaxTileCounters)
         return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many sorts in one call");
     SortArgs a{};
@@ -266,7 +346,21 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
     a.grid_pass = grid_for((with_values ? ctx->grid_pass_kv : ctx->grid_pass_k) / std::max(ctx->sms, 1),
                            ctx->sms, tiles);
-    launch_sort(a, s);
+    const int passes = sort_passes(lo, hi);
+    const uint64_t kv = with_values ? 12 : 8;
+    {
+        StageTimer t(ctx, hist_stage, s);
+        launch_sort_histogram(a, s);
+        ctx->launches += passes == 0 ? 2 : 1;
+        t.stop(d_n ? 0 : n_bound * 8);
+    }
+    DAGC_LAUNCHED(ctx);
+    for (int i = 0; i < passes; ++i) {
+        StageTimer t(ctx, pass_stage, s);
+        launch_sort_pass(a, i, s);
+        ++ctx->launches;
+        t.stop(d_n ? 0 : 2 * kv * n_bound);
+    }
     DAGC_LAUNCHED(ctx);
     return DAGC_OK;
 }
@@ -379,11 +473,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
     //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
     int st = run_sort(ctx, cs, sb, d_frag, P64(o_A), P64(o_B), nullptr, nullptr, nullptr, false, n, nullptr,
-                      6, std::max(6, bits), bits < 64 ? bits : 0, s);
+                      6, std::max(6, bits), bits < 64 ? bits : 0, s, DAGC_STAGE_FRAGMENT_HIST,
+                      DAGC_STAGE_FRAGMENT_PASS);
     if (st) return st;
 
     // 2. Fused unique + leaf build.
     {
+        StageTimer t(ctx, DAGC_STAGE_LEAF_BUILD, s);
         LeafBuildArgs a{};
         a.sorted = P64(o_A);
         a.d_n = nullptr;
@@ -397,9 +493,12 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         a.err = err;
         a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, scan_tiles(n));
         launch_leaf_build(a, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
+        t.stop();
     }
     // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
+    StageTimer t_dedup(ctx, DAGC_STAGE_LEAF_DEDUP, s);
     st = run_sort(ctx, cs, sb, P64(o_LM), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, p0cap,
                   cs.count(kCntBricks), 0, 64, 0, s);
     if (st) return st;
@@ -418,9 +517,12 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         a.err = err;
         a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(p0cap));
         launch_unique(a, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
     }
+    t_dedup.stop();
     // 4. Level loop, bottom-up.
+    StageTimer t_levels(ctx, DAGC_STAGE_LEVELS, s);
     const uint64_t* child_codes = P64(o_P);
     const uint32_t* child_map = P32(o_M0);
     const uint64_t* child_hashes = P64(o_PL);
@@ -446,6 +548,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         e.err = err;
         e.grid = grid_for(ctx->grid_extract / ctx->sms, ctx->sms, scan_tiles(child_bound));
         launch_extract(e, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
 
         st = run_sort(ctx, cs, sb, P64(o_NH), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
@@ -470,6 +573,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         u.err = err;
         u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(cap[l]));
         launch_unique(u, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
 
         child_codes = node_codes[it & 1];
@@ -479,6 +583,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         child_bound = cap[l];
     }
 
+    t_levels.stop();
     if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
     // 5. One read-back of every count and the error word.
     static_assert(sizeof(CallHeader) >= 8 * 65, "header");
@@ -491,6 +596,19 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     ctx->last_counts[1] = counts[kCntBricks];
     ctx->last_counts[2] = counts[kCntLeaves];
     for (int l = 0; l < nl; ++l) ctx->last_counts[3 + l] = counts[kCntNodes + l];
+    if (ctx->profiling) {
+        // Algorithmic bytes: the minimum each stage must read and write.
+        const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
+        set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
+        set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
+        uint64_t lb = 0;
+        for (int l = 0; l < nl; ++l) {
+            const uint64_t child = l + 1 < nl ? counts[kCntNodes + l + 1] : p0;
+            lb += 20 * child + 293 * counts[kCntNodes + l] + 41 * counts[kCntUnique + l];
+        }
+        set_pending_bytes(ctx, DAGC_STAGE_LEVELS, lb);
+        settle_profile(ctx);
+    }
     std::string msg;
     st = device_error_status(e32, msg);
     if (st) return set_error(ctx, st, msg);
@@ -516,6 +634,9 @@ int materialise(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, 
     dagc_dag d = nullptr;
     int st = alloc_dag(ctx, nl, p.unique, p.num_leaves, &d);
     if (st) return st;
+    uint64_t total_u = 0;
+    for (int l = 0; l < nl; ++l) total_u += p.unique[l];
+    StageTimer t(ctx, DAGC_STAGE_MATERIALISE, s);
     for (int l = 0; l < nl; ++l) {
         const uint64_t o = d->level_offset[l], u = p.unique[l];
         if (!u) continue;
@@ -525,7 +646,9 @@ int materialise(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, 
     }
     if (p.num_leaves) cudaMemcpyAsync(d->leaves, p.leaves, p.num_leaves * 8, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (nl + 1) * 8, cudaMemcpyHostToDevice, s);
+    t.stop(2 * (41 * total_u + 8 * p.num_leaves));
     const cudaError_t e = cudaStreamSynchronize(s);
+    settle_profile(ctx);
     if (e != cudaSuccess) {
         free_dag(d);
         cudaGetLastError();
@@ -572,8 +695,10 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     a.grid_scan = grid_for(ctx->grid_scan / ctx->sms, ctx->sms, scan_tiles(nn));
     a.grid_write = grid_for(8, ctx->sms, (nn + d->num_leaves + 255) / 256);
     uint64_t node_words = 0;
+    StageTimer t(ctx, DAGC_STAGE_FINAL, s);
     if (nn) {
         launch_final_positions(a, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
         DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, &h->counts[0], 8, cudaMemcpyDeviceToHost, s));
         DAGC_CUDA(ctx, cudaStreamSynchronize(s));
@@ -587,6 +712,8 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     DAGC_CUDA(ctx, ctx->pool.alloc(&w, total * 4));
     a.words = static_cast<uint32_t*>(w);
     launch_final_write(a, s);
+    ++ctx->launches;
+    t.stop(nn * 2 + (41 * nn + 8 * d->num_leaves) + 4 * total);
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) le = cudaMemcpyAsync(ctx->h_stage, h, 8, cudaMemcpyDeviceToHost, s);
     if (le == cudaSuccess) le = cudaStreamSynchronize(s);
@@ -594,6 +721,7 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
         ctx->pool.release(w);
         return set_error(ctx, cuda_status(le), std::string("final: ") + cudaGetErrorString(le));
     }
+    settle_profile(ctx);
     std::string msg;
     const int st = device_error_status((uint32_t)ctx->h_stage[0], msg);
     if (st) { ctx->pool.release(w); return set_error(ctx, st, msg); }
@@ -664,6 +792,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
     DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
     uint32_t* err = &cs.h->err;
 
+    StageTimer t_merge(ctx, DAGC_STAGE_MERGE, s);
     // Leaves: sorted union of all inputs' leaves.
     std::vector<uint64_t> prev_off(k + 1, 0);
     for (uint64_t i = 0; i < k; ++i) {
@@ -689,6 +818,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         a.err = err;
         a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(total_leaves));
         launch_unique(a, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
     }
     uint32_t* maps[2] = {P32(o_M0), P32(o_M1)};
@@ -703,6 +833,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
             DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_KC) + off[i], d->hashes + a0, u * 8, cudaMemcpyDeviceToDevice, s));
             DAGC_CUDA(ctx, cudaMemcpyAsync(P8(o_MC) + off[i], d->masks + a0, u, cudaMemcpyDeviceToDevice, s));
             launch_remap_children(d->children + a0 * 8, maps[cur] + prev_off[i], P32(o_CC) + off[i] * 8, u, s);
+            ++ctx->launches;
             DAGC_LAUNCHED(ctx);
         }
         const uint64_t nlev = off[k];
@@ -726,6 +857,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         u.err = err;
         u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(nlev));
         launch_unique(u, s);
+        ++ctx->launches;
         DAGC_LAUNCHED(ctx);
         cur ^= 1;
         prev_off = off;
@@ -741,6 +873,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_root_hash) + i, nl > 0 ? in[i]->hashes : in[i]->leaves, 8,
                                        cudaMemcpyDeviceToDevice, s));
     }
+    t_merge.stop();
     std::vector<uint64_t> stage_hash(k, 0);
     std::vector<uint32_t> stage_uid(k, 0);
     DAGC_CUDA(ctx, cudaMemcpyAsync(stage_hash.data(), P64(o_root_hash), k * 8, cudaMemcpyDeviceToHost, s));
@@ -753,6 +886,7 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         if (st) return set_error(ctx, st, msg);
     }
     if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
+    settle_profile(ctx);
     const uint64_t* counts = ctx->h_stage + 1;
     for (uint64_t i = 0; i < k; ++i) {
         if (input_empty(i)) continue;
@@ -897,6 +1031,8 @@ void dagc_context_destroy(dagc_context ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
+    settle_profile(ctx);
+    for (cudaEvent_t e : ctx->free_events) cudaEventDestroy(e);
     ctx->arena.release();
     ctx->pool.trim();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -1136,6 +1272,36 @@ int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n
     }
     dagc_free_words(ctx, w, stream);
     return h_words && capacity < nw ? set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "word buffer too small") : DAGC_OK;
+}
+
+int dagc_profile_enable(dagc_context ctx, int enable) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->profiling = enable != 0;
+    return DAGC_OK;
+}
+
+int dagc_profile_reset(dagc_context ctx) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    for (auto& st : ctx->stages) st = StageStats{};
+    return DAGC_OK;
+}
+
+int dagc_profile_read(dagc_context ctx, int stage, double* ms, uint64_t* launches, uint64_t* bytes) {
+    if (!valid_ctx(ctx) || stage < 0 || stage >= DAGC_NUM_STAGES) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const StageStats& st = ctx->stages[stage];
+    if (ms) *ms = st.ms;
+    if (launches) *launches = st.launches;
+    if (bytes) *bytes = st.bytes;
+    return DAGC_OK;
+}
+
+int dagc_kernel_launches(dagc_context ctx, uint64_t* launches) {
+    if (!valid_ctx(ctx) || !launches) return DAGC_ERR_INVALID_ARGUMENT;
+    *launches = ctx->launches;
+    return DAGC_OK;
 }
 
 int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap) {

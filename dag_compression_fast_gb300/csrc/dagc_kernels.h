@@ -61,6 +61,10 @@ DAGC_HD int sort_passes(int lo_bit, int hi_bit) {
 }
 // Where the result lands: keys_out always (the pass sequence is arranged so).
 void launch_sort(const SortArgs& a, cudaStream_t s);
+// The same, one launch at a time: histogram (+ copy when there is no digit),
+// then digit pass i for i in [0, sort_passes).
+void launch_sort_histogram(const SortArgs& a, cudaStream_t s);
+void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s);
 size_t sort_pass_smem(bool with_values);
 void sort_configure();  // sets shared-memory attributes once per device
 

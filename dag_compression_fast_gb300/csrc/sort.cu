@@ -241,40 +241,49 @@ int occupancy_sort_pass(bool with_values) {
     return occ;
 }
 
-void launch_sort(const SortArgs& a, cudaStream_t s) {
+// Launch parameters of digit pass i: the passes ping-pong so that the last
+// one always writes keys_out (pass i writes keys_out when passes-1-i is even).
+static PassParams pass_params(const SortArgs& a, int i) {
     const int passes = sort_passes(a.lo_bit, a.hi_bit);
+    const bool to_out = ((passes - 1 - i) & 1) == 0;
+    PassParams p;
+    p.keys_in = i == 0 ? a.keys_in : (to_out ? a.keys_alt : a.keys_out);
+    p.keys_out = to_out ? a.keys_out : a.keys_alt;
+    p.vals_in = i == 0 ? a.vals_in : (to_out ? a.vals_alt : a.vals_out);
+    p.vals_out = to_out ? a.vals_out : a.vals_alt;
+    p.d_n = a.d_n;
+    p.n_host = a.n;
+    p.hist = a.hist + i * 256;
+    p.status = a.status[i & 1];
+    p.status_clear = i + 1 < passes ? a.status[(i + 1) & 1] : nullptr;
+    p.tile_counter = a.tile_counters + i;
+    p.err = a.err;
+    p.shift = a.lo_bit + i * kRadixBits;
+    p.bits = a.hi_bit - p.shift < kRadixBits ? a.hi_bit - p.shift : kRadixBits;
+    return p;
+}
+
+void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
     // The histogram pass also validates the key range, so it runs even when
     // there is no digit to sort.
     radix_histogram<<<a.grid_hist, kSortThreads, 0, s>>>(a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
                                                          a.validate_bits, a.hist, a.status[0], a.err);
-    if (passes == 0) {
+    if (sort_passes(a.lo_bit, a.hi_bit) == 0)
         copy_keys<<<a.grid_hist, 256, 0, s>>>(a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
                                               a.d_n, a.n);
-        return;
-    }
-    for (int i = 0; i < passes; ++i) {
-        // Pass i writes keys_out when (passes - 1 - i) is even, else keys_alt,
-        // so that the last pass always lands in keys_out.
-        const bool to_out = ((passes - 1 - i) & 1) == 0;
-        PassParams p;
-        p.keys_in = i == 0 ? a.keys_in : (to_out ? a.keys_alt : a.keys_out);
-        p.keys_out = to_out ? a.keys_out : a.keys_alt;
-        p.vals_in = i == 0 ? a.vals_in : (to_out ? a.vals_alt : a.vals_out);
-        p.vals_out = to_out ? a.vals_out : a.vals_alt;
-        p.d_n = a.d_n;
-        p.n_host = a.n;
-        p.hist = a.hist + i * 256;
-        p.status = a.status[i & 1];
-        p.status_clear = i + 1 < passes ? a.status[(i + 1) & 1] : nullptr;
-        p.tile_counter = a.tile_counters + i;
-        p.err = a.err;
-        p.shift = a.lo_bit + i * kRadixBits;
-        p.bits = a.hi_bit - p.shift < kRadixBits ? a.hi_bit - p.shift : kRadixBits;
-        if (a.with_values)
-            onesweep_pass<true><<<a.grid_pass, kSortThreads, sort_pass_smem(true), s>>>(p);
-        else
-            onesweep_pass<false><<<a.grid_pass, kSortThreads, sort_pass_smem(false), s>>>(p);
-    }
+}
+
+void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
+    const PassParams p = pass_params(a, i);
+    if (a.with_values)
+        onesweep_pass<true><<<a.grid_pass, kSortThreads, sort_pass_smem(true), s>>>(p);
+    else
+        onesweep_pass<false><<<a.grid_pass, kSortThreads, sort_pass_smem(false), s>>>(p);
+}
+
+void launch_sort(const SortArgs& a, cudaStream_t s) {
+    launch_sort_histogram(a, s);
+    for (int i = 0; i < sort_passes(a.lo_bit, a.hi_bit); ++i) launch_sort_pass(a, i, s);
 }
 
 }  // namespace dagc

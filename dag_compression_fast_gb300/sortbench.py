@@ -1,0 +1,70 @@
+"""Radix-sort throughput sweeps, the GB300 counterpart of the reference's
+published CUB sort measurements (Python/constant64.csv, variable64.csv of
+Phyronnaz/DAG_Compression_Fast: 64-bit keys, throughput in G keys/s against the
+key count or the number of sorted bits).
+
+  python -m dag_compression_fast_gb300.sortbench                 # one case
+  python -m dag_compression_fast_gb300.sortbench --sweep bits    # 1..64 bits, 100M keys
+  python -m dag_compression_fast_gb300.sortbench --sweep n       # 1M..200M keys, 64 bits
+
+Each line: bits;keys;G keys/s;GB/s (algorithmic bytes: one key read for the
+histogram plus a read and a write per digit pass).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+
+import numpy as np
+
+
+def run(ctx, n: int, lo: int, hi: int, reps: int, seed: int = 1):
+    import torch
+    rng = np.random.default_rng(seed)
+    keys = torch.from_numpy(rng.integers(0, 2**63, n, dtype=np.int64)).cuda()
+    out = torch.empty_like(keys)
+    import dag_compression_fast_gb300 as D
+    lib = D.lib()
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        ctx._check(lib.dagc_sort_keys(ctx.handle, keys.data_ptr(), out.data_ptr(), n, lo, hi, s.cuda_stream))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        ctx._check(lib.dagc_sort_keys(ctx.handle, keys.data_ptr(), out.data_ptr(), n, lo, hi, s.cuda_stream))
+    e1.record(s)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / reps
+    passes = (hi - lo + 7) // 8
+    bytes_ = 8 * n + passes * 16 * n
+    return n / sec / 1e9, bytes_ / sec / 1e9
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--n", type=int, default=20_000_000)
+    p.add_argument("--lo", type=int, default=6)
+    p.add_argument("--hi", type=int, default=33)
+    p.add_argument("--reps", type=int, default=5)
+    p.add_argument("--sweep", choices=["none", "bits", "n"], default="none")
+    a = p.parse_args(argv)
+    import dag_compression_fast_gb300 as D
+    ctx = D.Context(0)
+    if a.sweep == "bits":
+        for bits in range(1, 65):
+            gk, gb = run(ctx, 100_000_000, 0, bits, a.reps)
+            print(f"{bits};{100_000_000};{gk:.3f};{gb:.1f}", flush=True)
+    elif a.sweep == "n":
+        for n in [1_000_000, 2_000_000, 5_000_000, 10_000_000, 20_000_000, 50_000_000, 100_000_000, 200_000_000]:
+            gk, gb = run(ctx, n, 0, 64, a.reps)
+            print(f"64;{n};{gk:.3f};{gb:.1f}", flush=True)
+    else:
+        gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps)
+        print(f"{a.hi - a.lo};{a.n};{gk:.3f};{gb:.1f}", flush=True)
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

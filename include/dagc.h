@@ -122,6 +122,28 @@ int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int
  * l in [0, depth-2). Returns the number of values written (<= cap). */
 int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
 
+/* ---------------------------------------------------- instrumentation ---- */
+/* Off by default. When enabled, each stage of a call is bracketed by CUDA
+ * events recorded on the call's own stream; device time, kernel launches and
+ * algorithmic bytes (the bytes each stage must read and write at minimum)
+ * accumulate per stage until dagc_profile_reset. The fragment-sort digit passes
+ * are bracketed one launch at a time. */
+#define DAGC_STAGE_FRAGMENT_HIST 0  /* histogram + key-range check of the fragment sort */
+#define DAGC_STAGE_FRAGMENT_PASS 1  /* one 8-bit digit pass of the fragment sort */
+#define DAGC_STAGE_LEAF_BUILD 2     /* fused unique + 4x4x4 leaf build */
+#define DAGC_STAGE_LEAF_DEDUP 3     /* leaf sort + unique */
+#define DAGC_STAGE_LEVELS 4         /* every inner level: extract, hash, sort, unique */
+#define DAGC_STAGE_MATERIALISE 5    /* copy of the level outputs into the DAG */
+#define DAGC_STAGE_FINAL 6          /* final word layout */
+#define DAGC_STAGE_MERGE 7          /* MergeDAGs */
+#define DAGC_NUM_STAGES 8
+int dagc_profile_enable(dagc_context ctx, int enable);
+int dagc_profile_reset(dagc_context ctx);
+int dagc_profile_read(dagc_context ctx, int stage, double* device_ms, uint64_t* launches,
+                      uint64_t* bytes);
+/* Total kernels this context has launched since it was created. */
+int dagc_kernel_launches(dagc_context ctx, uint64_t* launches);
+
 /* ------------------------------------------------------------- sorting ---- */
 /* The fragment sort as a standalone primitive: stable LSD radix sort of n
  * uint64 keys on bits [lo_bit, hi_bit), d_in -> d_out (may not alias). The
