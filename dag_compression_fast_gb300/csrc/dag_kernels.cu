@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = scan_tiles(n);
+    if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = scan_tiles(n);
+    if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
@@ -280,6 +282,7 @@ __global__ void __launch_bounds__(kT) unique_runs(UniqueArgs a) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = scan_tiles(n);
+    if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
@@ -370,6 +373,157 @@ __global__ void __launch_bounds__(kT) unique_runs(UniqueArgs a) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Tail: all levels with at most kTailCap nodes, in one CTA.
+// ---------------------------------------------------------------------------
+struct TailSmem {
+    uint64_t code[2][kTailCap];   // node codes of the level being built / its children
+    uint64_t key[kTailCap];       // node hashes, sorted with idx
+    uint32_t idx[kTailCap];
+    uint32_t map[2][kTailCap];    // node -> unique id, per level (ping-pong)
+    uint8_t mask[kTailCap];
+    uint32_t scan[34];
+    uint32_t flags;
+};
+
+__device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb, uint32_t ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+__global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TailSmem& S = *reinterpret_cast<TailSmem*>(smem_raw);
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) S.flags = 0;
+    const uint64_t* cc = a.child_codes;
+    const uint32_t* cm = a.child_map;
+    const uint64_t* ch = a.child_hashes;
+    uint64_t nc = *a.d_child_n;
+    int ping = 0;
+    __syncthreads();
+    for (int l = a.first_level; l >= 0; --l) {
+        const TailLevelOut& out = a.lv[l];
+        const uint64_t cap = out.capacity < (uint64_t)kTailCap ? out.capacity : (uint64_t)kTailCap;
+        uint64_t* node_code = S.code[ping];
+        uint32_t* node_map = S.map[ping];
+        // Extract + hash: one node per distinct child code >> 3, built by the
+        // first child of its run.
+        uint64_t nn = 0;
+        for (uint64_t c0 = 0; c0 < nc; c0 += kTailThreads) {
+            const uint64_t i = c0 + tid;
+            bool head = false;
+            uint64_t par = 0;
+            if (i < nc) {
+                par = cc[i] >> 3;
+                head = i == 0 || (cc[i - 1] >> 3) != par;
+            }
+            uint32_t total;
+            const uint32_t excl = block_exclusive_sum<uint32_t>(head ? 1u : 0u, S.scan, &total);
+            if (head) {
+                const uint64_t p = nn + excl;
+                if (p < cap) {
+                    uint32_t chd[8];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) chd[c] = kEmptyChild;
+                    uint32_t m = 0;
+                    for (int k = 0; k < 8 && i + k < nc; ++k) {
+                        const uint64_t code = cc[i + k];
+                        if ((code >> 3) != par) break;
+                        chd[code & 7] = cm[i + k];
+                        m |= 1u << (code & 7);
+                    }
+                    uint64_t h[8];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) h[c] = chd[c] == kEmptyChild ? 0 : ch[chd[c]];
+                    node_code[p] = par;
+                    S.key[p] = hash_children(h);
+                    S.idx[p] = (uint32_t)p;
+                    S.mask[p] = (uint8_t)m;
+                    uint4* dst = reinterpret_cast<uint4*>(a.scratch_children + p * 8);
+                    dst[0] = make_uint4(chd[0], chd[1], chd[2], chd[3]);
+                    dst[1] = make_uint4(chd[4], chd[5], chd[6], chd[7]);
+                } else {
+                    atomicOr(&S.flags, kErrCapacity);
+                }
+            }
+            nn += total;
+            __syncthreads();
+        }
+        const uint32_t n = (uint32_t)(nn < cap ? nn : cap);
+        // Bitonic sort of (hash, node) pairs, padded to a power of two with
+        // (max, max) which sorts after every real pair.
+        uint32_t P = 1;
+        while (P < n) P <<= 1;
+        for (uint32_t i = n + tid; i < P; i += kTailThreads) { S.key[i] = ~0ull; S.idx[i] = 0xFFFFFFFFu; }
+        __syncthreads();
+        for (uint32_t size = 2; size <= P; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t t = tid; t < P / 2; t += kTailThreads) {
+                    const uint32_t lo = 2 * t - (t & (stride - 1));
+                    const uint32_t hi = lo + stride;
+                    const bool up = (lo & size) == 0;
+                    const uint64_t ka = S.key[lo], kb = S.key[hi];
+                    const uint32_t ia = S.idx[lo], ib = S.idx[hi];
+                    if (pair_less(kb, ib, ka, ia) == up) {
+                        S.key[lo] = kb; S.key[hi] = ka;
+                        S.idx[lo] = ib; S.idx[hi] = ia;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // Unique with the full compare; node -> unique id into node_map.
+        uint64_t uid_base = 0;
+        for (uint32_t c0 = 0; c0 < n; c0 += kTailThreads) {
+            const uint32_t i = c0 + tid;
+            bool head = false;
+            if (i < n) {
+                head = i == 0 || S.key[i] != S.key[i - 1];
+                if (!head) {
+                    const uint32_t x = S.idx[i], y = S.idx[i - 1];
+                    const uint4* cx = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)x * 8);
+                    const uint4* cy = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)y * 8);
+                    const uint4 x0 = cx[0], x1 = cx[1], y0 = cy[0], y1 = cy[1];
+                    const bool same = S.mask[x] == S.mask[y] && x0.x == y0.x && x0.y == y0.y && x0.z == y0.z &&
+                                      x0.w == y0.w && x1.x == y1.x && x1.y == y1.y && x1.z == y1.z && x1.w == y1.w;
+                    if (!same) atomicOr(&S.flags, kErrCollision);
+                }
+            }
+            uint32_t total;
+            const uint32_t excl = block_exclusive_sum<uint32_t>(head ? 1u : 0u, S.scan, &total);
+            if (i < n) {
+                // Items before the chunk's first head continue the previous run.
+                const uint64_t uid = uid_base + excl + (head ? 1 : 0) - 1;
+                const uint32_t x = S.idx[i];
+                node_map[x] = (uint32_t)uid;
+                if (head && uid < out.capacity) {
+                    out.hashes[uid] = S.key[i];
+                    out.masks[uid] = S.mask[x];
+                    const uint4* src = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)x * 8);
+                    uint4* dst = reinterpret_cast<uint4*>(out.children + uid * 8);
+                    dst[0] = src[0];
+                    dst[1] = src[1];
+                }
+            }
+            uid_base += total;
+            __syncthreads();
+        }
+        if (tid == 0) {
+            *out.d_nodes = n;
+            *out.d_unique = uid_base;
+        }
+        // The next level's children are this level's nodes.
+        cc = node_code;
+        cm = node_map;
+        ch = out.hashes;
+        nc = n;
+        ping ^= 1;
+        __syncthreads();
+    }
+    if (tid == 0 && S.flags) atomicOr(a.err, S.flags);
+}
+
 // ---------------------------------------------------------------------------
 // Final layout.
 // ---------------------------------------------------------------------------
@@ -385,6 +539,7 @@ __global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = a.num_nodes;
     const uint32_t ntiles = scan_tiles(n);
+    if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
@@ -483,6 +638,7 @@ void kernels_configure() {
     cudaFuncSetAttribute(leaf_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LeafSmem));
     cudaFuncSetAttribute(extract_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
     cudaFuncSetAttribute(unique_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(UniqueSmem));
+    cudaFuncSetAttribute(tail_levels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TailSmem));
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -516,6 +672,9 @@ void launch_extract(const ExtractArgs& a, cudaStream_t s) {
 }
 void launch_unique(const UniqueArgs& a, cudaStream_t s) {
     unique_runs<<<a.grid, kT, sizeof(UniqueSmem), s>>>(a);
+}
+void launch_tail(const TailArgs& a, cudaStream_t s) {
+    tail_levels<<<1, kTailThreads, sizeof(TailSmem), s>>>(a);
 }
 void launch_final_positions(const FinalArgs& a, cudaStream_t s) {
     final_positions<<<a.grid_scan, kT, 0, s>>>(a);

@@ -447,7 +447,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     const size_t o_NC0 = L.take<uint64_t>(capmax);
     const size_t o_NC1 = L.take<uint64_t>(capmax);
     const size_t o_NM = L.take<uint8_t>(capmax);
-    const size_t o_NCH = L.take<uint32_t>(capmax * 8);
+    const size_t o_NCH = L.take<uint32_t>(std::max<uint64_t>(capmax, kTailCap) * 8);
     const size_t o_NH = L.take<uint64_t>(capmax);
     const size_t o_PL = L.take<uint64_t>(p0cap);
     std::vector<size_t> o_ph(nl), o_pc(nl), o_pm(nl);
@@ -530,7 +530,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     uint64_t child_bound = p0cap;
     uint64_t* node_codes[2] = {P64(o_NC0), P64(o_NC1)};
     uint32_t* maps[2] = {P32(o_M1), P32(o_M0)};
-    for (int l = nl - 1, it = 0; l >= 0; --l, ++it) {
+    // Levels whose node bound fits one CTA's shared memory go to the tail
+    // kernel; the bound only grows with the level index, so they are the top
+    // tail_first + 1 levels.
+    int tail_first = -1;
+    while (tail_first + 1 < nl && tail_first + 1 < kMaxTailLevels && cap[tail_first + 1] <= (uint64_t)kTailCap)
+        ++tail_first;
+    for (int l = nl - 1, it = 0; l > tail_first; --l, ++it) {
         ExtractArgs e{};
         e.child_codes = child_codes;
         e.child_map = child_map;
@@ -581,6 +587,27 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         child_hashes = P64(o_ph[l]);
         d_child_n = cs.count(kCntNodes + l);
         child_bound = cap[l];
+    }
+    if (tail_first >= 0) {
+        TailArgs ta{};
+        ta.first_level = tail_first;
+        ta.child_codes = child_codes;
+        ta.child_map = child_map;
+        ta.child_hashes = child_hashes;
+        ta.d_child_n = d_child_n;
+        ta.scratch_children = P32(o_NCH);
+        for (int l = 0; l <= tail_first; ++l) {
+            ta.lv[l].hashes = P64(o_ph[l]);
+            ta.lv[l].masks = P8(o_pm[l]);
+            ta.lv[l].children = P32(o_pc[l]);
+            ta.lv[l].capacity = cap[l];
+            ta.lv[l].d_nodes = cs.count(kCntNodes + l);
+            ta.lv[l].d_unique = cs.count(kCntUnique + l);
+        }
+        ta.err = err;
+        launch_tail(ta, s);
+        ++ctx->launches;
+        DAGC_LAUNCHED(ctx);
     }
 
     t_levels.stop();

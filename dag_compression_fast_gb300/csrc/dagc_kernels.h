@@ -116,6 +116,25 @@ struct ExtractArgs {
 };
 void launch_extract(const ExtractArgs& a, cudaStream_t s);
 
+// The top levels in one single-CTA launch: every level l <= first_level has at
+// most kTailCap nodes, so extract + hash + sort + unique run in shared memory.
+constexpr int kTailThreads = 1024;
+constexpr int kTailCap = 4096;
+constexpr int kMaxTailLevels = 8;
+struct TailLevelOut {
+    uint64_t* hashes; uint8_t* masks; uint32_t* children; uint64_t capacity;
+    uint64_t* d_nodes; uint64_t* d_unique;
+};
+struct TailArgs {
+    int first_level;
+    const uint64_t* child_codes; const uint32_t* child_map; const uint64_t* child_hashes;
+    const uint64_t* d_child_n;
+    uint32_t* scratch_children;  // kTailCap * 8 words
+    TailLevelOut lv[kMaxTailLevels];
+    uint32_t* err;
+};
+void launch_tail(const TailArgs& a, cudaStream_t s);
+
 // Final layout: word position of every node (exclusive scan of popc+1 over all
 // levels concatenated), then headers, child pointers and leaves.
 struct FinalArgs {

@@ -24,9 +24,13 @@ namespace {
 constexpr uint32_t kSAgg = 1u << 30;
 constexpr uint32_t kSInc = 2u << 30;
 constexpr uint32_t kSVal = (1u << 30) - 1;
-constexpr int kWarps = kSortThreads / 32;
 constexpr int kRadix = 1 << kRadixBits;
-static_assert(kSortThreads == kRadix, "one thread per digit");
+
+// Pass kernel shapes: 256 threads (one per digit) x 16 items, 4096-key tiles,
+// for keys alone and for key/value pairs.
+constexpr int kKeyThreads = 256, kKeyItems = 16;
+constexpr int kPairThreads = 256, kPairItems = 16;
+static_assert(kKeyThreads * kKeyItems == kSortTile && kPairThreads * kPairItems == kSortTile, "tile");
 
 __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
     return d_n ? *d_n : n;
@@ -81,130 +85,187 @@ struct PassParams {
     int shift, bits;
 };
 
-template <bool kValues>
-__global__ void __launch_bounds__(kSortThreads, 2) onesweep_pass(PassParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint64_t* s_keys = reinterpret_cast<uint64_t*>(smem);                        // kSortTile
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + kSortTile);          // kSortTile if kValues
-    uint32_t* s_whist = s_vals + (kValues ? kSortTile : 0);                      // kWarps * 256
-    uint32_t* s_gbase = s_whist + kWarps * kRadix;                               // 256
-    uint32_t* s_adj = s_gbase + kRadix;                                          // 256
-    uint32_t* s_local = s_adj + kRadix;                                          // 256
-    uint32_t* s_scan = s_local + kRadix;                                         // 33
-    uint32_t* s_tile = s_scan + 33;                                              // 1
+// Exclusive prefix of one digit over the tiles before `tile`: walks back over
+// their published counts 8 tiles per round trip, stopping at the first
+// inclusive prefix; waits (bounded) on tiles that have published nothing yet.
+__device__ __forceinline__ uint32_t lookback_digit(const uint32_t* status, uint32_t tile, uint32_t d,
+                                                   uint32_t* err) {
+    constexpr int kLB = 8;
+    uint32_t excl = 0, iter = 0;
+    int64_t t = (int64_t)tile - 1;
+    while (true) {
+        uint32_t st[kLB];
+#pragma unroll
+        for (int k = 0; k < kLB; ++k)
+            st[k] = t - k >= 0 ? ld_relaxed(status + (uint64_t)(t - k) * kRadix + d) : kSInc;
+        int consumed = kLB;
+        bool done = false;
+#pragma unroll
+        for (int k = 0; k < kLB; ++k) {
+            if (done || k >= consumed) continue;
+            const uint32_t f = st[k] >> 30;
+            if (f == 0) {
+                consumed = k;  // not published yet: resume here
+            } else {
+                excl += st[k] & kSVal;
+                done = f == 2;
+            }
+        }
+        if (done) break;
+        t -= consumed;
+        if (consumed == 0) {
+            if (++iter > kSpinLimit) { atomicOr(err, kErrTimeout); break; }
+            backoff(iter);
+        }
+    }
+    return excl;
+}
+
+// Shared memory of one onesweep CTA: the staging tile, per-warp digit
+// counters (turned into per-warp output offsets) and per-digit offsets.
+template <int kThreads, int kItems, bool kValues>
+struct PassSmem {
+    static constexpr int kTile = kThreads * kItems;
+    static constexpr int kWarpsPerCta = kThreads / 32;
+    uint64_t keys[kTile];
+    uint32_t vals[kValues ? kTile : 4];
+    uint32_t whist[kWarpsPerCta][kRadix];
+    uint32_t gbase[kRadix];
+    uint32_t adj[kRadix];
+    uint32_t scan[34];
+    uint32_t tile_id;
+};
+
+// One 8-bit digit pass. Tiles of kTile keys are taken in increasing order from
+// an atomic counter by a persistent grid. Per tile:
+//   1. each thread loads its keys straight into registers (warp-striped,
+//      coalesced), so shared memory only carries the counters and the
+//      staged output;
+//   2. each warp ranks its 32*kItems keys stably with __match_any_sync and a
+//      warp-private counter per digit;
+//   3. thread d sums digit d over the warps, publishes the tile count for the
+//      decoupled look-back, and a block scan gives the tile-local offsets;
+//      the per-warp counters become per-warp output offsets in place;
+//   4. thread d looks back over earlier tiles (8 per round trip, bounded
+//      waits) for digit d's global offset and publishes the inclusive prefix;
+//   5. keys are staged in digit order and written out so that equal digits
+//      form contiguous runs.
+template <int kThreads, int kItems, bool kValues>
+__global__ void __launch_bounds__(kThreads, 3) onesweep_pass(PassParams p) {
+    using Smem = PassSmem<kThreads, kItems, kValues>;
+    constexpr int kTile = Smem::kTile;
+    constexpr int kW = Smem::kWarpsPerCta;
+    static_assert(kThreads == kRadix, "one thread per digit");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem& S = *reinterpret_cast<Smem*>(smem_raw);
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n64 = load_n(p.d_n, p.n_host);
     const uint32_t n = (uint32_t)n64;
-    const uint32_t ntiles = sort_tiles(n64);
+    const uint32_t ntiles = (uint32_t)((n64 + kTile - 1) / kTile);
+    // CTAs beyond the live tile count leave at once (grids are sized by an
+    // upper bound when the count is device-resident).
+    const uint32_t active = min(gridDim.x, max(ntiles, 1u));
+    if (blockIdx.x >= active) return;
     const uint32_t dmask = (1u << p.bits) - 1u;
 
     if (p.status_clear) {
         const uint64_t words = (uint64_t)ntiles * kRadix;
-        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + tid; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+        for (uint64_t i = (uint64_t)blockIdx.x * kThreads + tid; i < words; i += (uint64_t)active * kThreads)
             p.status_clear[i] = 0;
     }
     {
         uint32_t total;
-        const uint32_t c = p.hist[tid];
-        s_gbase[tid] = block_exclusive_sum<uint32_t>(c, s_scan, &total);
+        S.gbase[tid] = block_exclusive_sum<uint32_t>(p.hist[tid], S.scan, &total);
     }
-
+    uint32_t* wh = S.whist[warp];
     while (true) {
-        if (tid == 0) *s_tile = atomicAdd(p.tile_counter, 1u);
-        for (int i = tid; i < kWarps * kRadix; i += kSortThreads) s_whist[i] = 0;
+        if (tid == 0) S.tile_id = atomicAdd(p.tile_counter, 1u);
+        for (int i = tid; i < kW * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
         __syncthreads();
-        const uint32_t tile = *s_tile;
+        const uint32_t tile = S.tile_id;
         if (tile >= ntiles) break;
-        const uint32_t base = tile * kSortTile;
-        const uint32_t tile_n = min((uint32_t)kSortTile, n - base);
-        const uint32_t wbase = base + warp * (kSortItems * 32);
+        const uint32_t base = tile * kTile;
+        const uint32_t tile_n = min((uint32_t)kTile, n - base);
+        const uint32_t wofs = warp * (kItems * 32);
 
-        uint64_t k[kSortItems];
-        uint32_t v[kValues ? kSortItems : 1];
+        uint64_t k[kItems];
 #pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            const uint32_t idx = wbase + j * 32 + lane;
-            if (idx < n) {
-                k[j] = p.keys_in[idx];
-                if (kValues) v[j] = p.vals_in ? p.vals_in[idx] : idx;
-            }
+        for (int j = 0; j < kItems; ++j) {
+            const uint32_t i = wofs + j * 32 + lane;
+            if (i < tile_n) k[j] = p.keys_in[base + i];
         }
-        // Warp-level multisplit ranking (stable: item order = (j, lane)).
-        uint32_t rank[kSortItems];
-        uint32_t* wh = s_whist + warp * kRadix;
+        // Ranks within the warp fit 16 bits: two per register.
+        uint32_t rank2[kItems / 2];
 #pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            const bool valid = wbase + j * 32 + lane < n;
+        for (int j = 0; j < kItems; ++j) {
+            const bool valid = wofs + j * 32 + lane < tile_n;
             const uint32_t d = valid ? ((uint32_t)(k[j] >> p.shift) & dmask) : 0xFFFFFFFFu;
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-            uint32_t prior = 0;
+            uint32_t prior = 0, r = 0;
             if (valid) {
                 prior = wh[d];
-                rank[j] = prior + __popc(peers & lanemask_lt());
+                r = prior + __popc(peers & lanemask_lt());
             }
+            if (j & 1) rank2[j / 2] |= r << 16;
+            else rank2[j / 2] = r;
             __syncwarp();
             if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = prior + __popc(peers);
             __syncwarp();
         }
         __syncthreads();
 
-        // Per digit (thread tid = digit): exclusive over warps, tile count,
-        // publish, local offset, look-back.
-        {
-            const uint32_t d = tid;
-            uint32_t cnt = 0;
+        // Digit d = tid: count over the warps, publish the tile count, block
+        // scan for the tile-local offsets; the per-warp counters become
+        // per-warp output offsets in place.
+        uint32_t cnt = 0;
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                const uint32_t c = s_whist[w * kRadix + d];
-                s_whist[w * kRadix + d] = cnt;
-                cnt += c;
-            }
-            uint32_t* st = p.status + (uint64_t)tile * kRadix + d;
-            st_relaxed(st, (tile == 0 ? kSInc : kSAgg) | cnt);
-            uint32_t total;
-            const uint32_t local = block_exclusive_sum<uint32_t>(cnt, s_scan, &total);
-            uint32_t excl = 0;
-            if (tile > 0) {
-                int64_t t = (int64_t)tile - 1;
-                uint32_t iter = 0;
-                while (t >= 0) {
-                    const uint32_t s = ld_relaxed(p.status + (uint64_t)t * kRadix + d);
-                    const uint32_t flag = s >> 30;
-                    if (flag == 0) {
-                        if (++iter > kSpinLimit) { atomicOr(p.err, kErrTimeout); break; }
-                        backoff(iter);
-                        continue;
-                    }
-                    excl += s & kSVal;
-                    if (flag == 2) break;
-                    --t;
-                }
-                st_relaxed(st, kSInc | (excl + cnt));
-            }
-            s_local[d] = local;
-            s_adj[d] = s_gbase[d] + excl - local;
+        for (int w = 0; w < kW; ++w) {
+            const uint32_t c = S.whist[w][tid];
+            S.whist[w][tid] = cnt;
+            cnt += c;
         }
-        __syncthreads();
-
-        // Stage in local digit order.
+        uint32_t* my = p.status + (uint64_t)tile * kRadix + tid;
+        st_relaxed(my, (tile == 0 ? kSInc : kSAgg) | cnt);
+        uint32_t total;
+        const uint32_t local = block_exclusive_sum<uint32_t>(cnt, S.scan, &total);
 #pragma unroll
-        for (int j = 0; j < kSortItems; ++j) {
-            if (wbase + j * 32 + lane < n) {
-                const uint32_t d = (uint32_t)(k[j] >> p.shift) & dmask;
-                const uint32_t pos = s_local[d] + s_whist[warp * kRadix + d] + rank[j];
-                s_keys[pos] = k[j];
-                if (kValues) s_vals[pos] = v[j];
+        for (int w = 0; w < kW; ++w) S.whist[w][tid] += local;
+        __syncthreads();
+        // Stage in tile-local digit order; values (if any) are fetched here,
+        // they play no part in the ranking.
+#pragma unroll
+        for (int j = 0; j < kItems; ++j) {
+            const uint32_t i = wofs + j * 32 + lane;
+            if (i < tile_n) {
+                const uint32_t r = (rank2[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
+                const uint32_t pos = wh[(uint32_t)(k[j] >> p.shift) & dmask] + r;
+                S.keys[pos] = k[j];
+                if (kValues) S.vals[pos] = p.vals_in ? p.vals_in[base + i] : base + i;
             }
         }
-        __syncthreads();
-        for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
-            const uint64_t key = s_keys[i];
-            const uint32_t d = (uint32_t)(key >> p.shift) & dmask;
-            const uint32_t dst = s_adj[d] + i;
-            p.keys_out[dst] = key;
-            if (kValues) p.vals_out[dst] = s_vals[i];
+        // Look back for digit d's offset among earlier tiles, publish the
+        // inclusive prefix.
+        uint32_t excl = 0;
+        if (tile > 0) {
+            excl = lookback_digit(p.status, tile, tid, p.err);
+            st_relaxed(my, kSInc | (excl + cnt));
         }
+        S.adj[tid] = S.gbase[tid] + excl - local;
+        __syncthreads();
+        bool oob = false;
+#pragma unroll 4
+        for (uint32_t i = tid; i < tile_n; i += kThreads) {
+            const uint64_t key = S.keys[i];
+            const uint32_t dst = S.adj[(uint32_t)(key >> p.shift) & dmask] + i;
+            if (dst < n) {
+                p.keys_out[dst] = key;
+                if (kValues) p.vals_out[dst] = S.vals[i];
+            } else {
+                oob = true;  // only after a timed-out wait; never writes out of bounds
+            }
+        }
+        if (oob) atomicOr(p.err, kErrCapacity);
         __syncthreads();
     }
 }
@@ -221,23 +282,25 @@ __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin
 }  // namespace
 
 size_t sort_pass_smem(bool with_values) {
-    return (size_t)kSortTile * 8 + (with_values ? (size_t)kSortTile * 4 : 0) +
-           (size_t)(kWarps * kRadix + 3 * kRadix + 34) * 4;
+    return with_values ? sizeof(PassSmem<kPairThreads, kPairItems, true>)
+                       : sizeof(PassSmem<kKeyThreads, kKeyItems, false>);
 }
 
 void sort_configure() {
-    cudaFuncSetAttribute(onesweep_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(onesweep_pass<kPairThreads, kPairItems, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sort_pass_smem(true));
-    cudaFuncSetAttribute(onesweep_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(onesweep_pass<kKeyThreads, kKeyItems, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sort_pass_smem(false));
 }
 
 int occupancy_sort_pass(bool with_values) {
     int occ = 0;
     if (with_values)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<true>, kSortThreads, sort_pass_smem(true));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<kPairThreads, kPairItems, true>,
+                                                      kPairThreads, sort_pass_smem(true));
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<false>, kSortThreads, sort_pass_smem(false));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<kKeyThreads, kKeyItems, false>,
+                                                      kKeyThreads, sort_pass_smem(false));
     return occ;
 }
 
@@ -276,9 +339,9 @@ void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
 void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
     const PassParams p = pass_params(a, i);
     if (a.with_values)
-        onesweep_pass<true><<<a.grid_pass, kSortThreads, sort_pass_smem(true), s>>>(p);
+        onesweep_pass<kPairThreads, kPairItems, true><<<a.grid_pass, kPairThreads, sort_pass_smem(true), s>>>(p);
     else
-        onesweep_pass<false><<<a.grid_pass, kSortThreads, sort_pass_smem(false), s>>>(p);
+        onesweep_pass<kKeyThreads, kKeyItems, false><<<a.grid_pass, kKeyThreads, sort_pass_smem(false), s>>>(p);
 }
 
 void launch_sort(const SortArgs& a, cudaStream_t s) {
