@@ -26,6 +26,10 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIBDAGC_PATH = os.path.join(LIB_DIR, "libdagc.so")
 LIBGEN_PATH = os.path.join(LIB_DIR, "libdagc_gen.so")
 
+OPT_SORT_SHAPE_KEYS = 1
+OPT_SORT_SHAPE_PAIRS = 2
+NUM_SORT_SHAPES = 8
+
 OK = 0
 ERR_INVALID_ARGUMENT = 1
 ERR_OUT_OF_MEMORY = 2
@@ -43,7 +47,7 @@ DAGC_SYMBOLS = [
     "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_free",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
-    "dagc_compress", "dagc_last_counts", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_compress", "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
 ]
 
@@ -106,6 +110,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_compress_host.argtypes = [vp, vp, u64, i32, vp, vp, u64, pu64]
         L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
+        L.dagc_set_option.argtypes = [vp, i32, i32]
         L.dagc_profile_enable.argtypes = [vp, i32]
         L.dagc_profile_reset.argtypes = [vp]
         L.dagc_profile_read.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double), pu64, pu64]
@@ -364,6 +369,10 @@ class Context:
     def free_all(self):
         """DAGCompression::FreeAll."""
         self._check(lib().dagc_free_all(self.handle))
+
+    def set_option(self, option: int, value: int):
+        """dagc_set_option: OPT_SORT_SHAPE_KEYS / OPT_SORT_SHAPE_PAIRS."""
+        self._check(lib().dagc_set_option(self.handle, option, value))
 
     def profile(self, enable: bool = True):
         """Turns per-stage CUDA-event timing on or off (see include/dagc.h)."""

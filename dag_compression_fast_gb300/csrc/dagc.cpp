@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -166,6 +167,8 @@ struct PendingTiming {
 struct dagc_context_t {
     int device = 0;
     bool profiling = false;
+    int shape_keys = 5, shape_pairs = 3;  // digit-pass shapes (see dagc_set_option), tuned on GB300
+    int occ_keys[kNumSortShapes] = {}, occ_pairs[kNumSortShapes] = {};
     StageStats stages[DAGC_NUM_STAGES];
     std::vector<cudaEvent_t> free_events;
     std::vector<PendingTiming> pending;
@@ -344,8 +347,10 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     a.err = &cs.h->err;
     const uint64_t tiles = sort_tiles(n_bound);
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
-    a.grid_pass = grid_for((with_values ? ctx->grid_pass_kv : ctx->grid_pass_k) / std::max(ctx->sms, 1),
-                           ctx->sms, tiles);
+    a.shape = with_values ? ctx->shape_pairs : ctx->shape_keys;
+    const int occ = with_values ? ctx->occ_pairs[a.shape] : ctx->occ_keys[a.shape];
+    const uint64_t shape_tiles = (n_bound + 256ull * sort_shape_items(a.shape) - 1) / (256ull * sort_shape_items(a.shape));
+    a.grid_pass = grid_for(occ, ctx->sms, std::min<uint64_t>(tiles, shape_tiles));
     const int passes = sort_passes(lo, hi);
     const uint64_t kv = with_values ? 12 : 8;
     {
@@ -1042,8 +1047,12 @@ int dagc_context_create(int device, dagc_context* out) {
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
     int occ = 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
-    occ = occupancy_sort_pass(true);  c->grid_pass_kv = std::max(1, occ) * c->sms;
-    occ = occupancy_sort_pass(false); c->grid_pass_k = std::max(1, occ) * c->sms;
+    for (int sh = 0; sh < kNumSortShapes; ++sh) {
+        c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
+        c->occ_pairs[sh] = std::max(1, occupancy_sort_shape(sh, true));
+    }
+    if (const char* e = std::getenv("DAGC_SORT_SHAPE_KEYS")) c->shape_keys = std::atoi(e) % kNumSortShapes;
+    if (const char* e = std::getenv("DAGC_SORT_SHAPE_PAIRS")) c->shape_pairs = std::atoi(e) % kNumSortShapes;
     c->grid_hist = 8 * c->sms;
     c->grid_leaf = std::max(1, occupancy_kernel(0)) * c->sms;
     c->grid_extract = std::max(1, occupancy_kernel(1)) * c->sms;
@@ -1299,6 +1308,23 @@ int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n
     }
     dagc_free_words(ctx, w, stream);
     return h_words && capacity < nw ? set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "word buffer too small") : DAGC_OK;
+}
+
+int dagc_set_option(dagc_context ctx, int option, int value) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    switch (option) {
+        case DAGC_OPT_SORT_SHAPE_KEYS:
+            if (value < 0 || value >= kNumSortShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
+            ctx->shape_keys = value;
+            return DAGC_OK;
+        case DAGC_OPT_SORT_SHAPE_PAIRS:
+            if (value < 0 || value >= kNumSortShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
+            ctx->shape_pairs = value;
+            return DAGC_OK;
+        default:
+            return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "unknown option");
+    }
 }
 
 int dagc_profile_enable(dagc_context ctx, int enable) {

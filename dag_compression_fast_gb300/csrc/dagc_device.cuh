@@ -20,6 +20,12 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+__device__ __forceinline__ uint32_t lanemask_le() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+    return m;
+}
+
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
     uint32_t v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

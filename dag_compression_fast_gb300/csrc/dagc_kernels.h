@@ -26,8 +26,9 @@ constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;
 
 // ---------------------------------------------------------------- sort ----
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // keys per tile
+// Digit-pass tiles hold 256 threads x (8..16) keys; status arrays are sized
+// for the smallest tile so that every pass shape fits.
+constexpr int kSortTile = 2048;
 constexpr int kRadixBits = 8;
 constexpr int kMaxPasses = 8;
 
@@ -53,7 +54,16 @@ struct SortArgs {
     uint32_t* tile_counters;  // kMaxPasses words, zeroed
     uint32_t* err;
     int grid_hist, grid_pass; // persistent grid sizes
+    int shape;                // digit-pass kernel shape, see sort_shape_*
 };
+
+// Digit-pass kernel shapes (items per thread x minimum resident CTAs per SM,
+// which caps registers); the autotuner and dagc options pick one per sort.
+constexpr int kNumSortShapes = 8;
+int sort_shape_items(int shape);
+int sort_shape_min_ctas(int shape);
+// Resident CTAs per SM of a shape (occupancy query) for grid sizing.
+int occupancy_sort_shape(int shape, bool with_values);
 
 // Number of digit passes for a bit range.
 DAGC_HD int sort_passes(int lo_bit, int hi_bit) {

@@ -18,6 +18,8 @@
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
 
+#include <algorithm>
+
 namespace dagc {
 namespace {
 
@@ -26,11 +28,7 @@ constexpr uint32_t kSInc = 2u << 30;
 constexpr uint32_t kSVal = (1u << 30) - 1;
 constexpr int kRadix = 1 << kRadixBits;
 
-// Pass kernel shapes: 256 threads (one per digit) x 16 items, 4096-key tiles,
-// for keys alone and for key/value pairs.
-constexpr int kKeyThreads = 256, kKeyItems = 16;
-constexpr int kPairThreads = 256, kPairItems = 16;
-static_assert(kKeyThreads * kKeyItems == kSortTile && kPairThreads * kPairItems == kSortTile, "tile");
+constexpr int kPassThreads = 256;  // one thread per digit
 
 __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
     return d_n ? *d_n : n;
@@ -150,8 +148,11 @@ struct PassSmem {
 //      waits) for digit d's global offset and publishes the inclusive prefix;
 //   5. keys are staged in digit order and written out so that equal digits
 //      form contiguous runs.
-template <int kThreads, int kItems, bool kValues>
-__global__ void __launch_bounds__(kThreads, 3) onesweep_pass(PassParams p) {
+// kMatch: how lanes with equal digits are found. 0: one ballot per digit bit
+// (ALU pipe), 1: match.any (ADU pipe), 2: alternate per item, which spreads
+// the work over both pipes.
+template <int kThreads, int kItems, bool kValues, int kMinCtas, int kMatch>
+__global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p) {
     using Smem = PassSmem<kThreads, kItems, kValues>;
     constexpr int kTile = Smem::kTile;
     constexpr int kW = Smem::kWarpsPerCta;
@@ -200,18 +201,36 @@ __global__ void __launch_bounds__(kThreads, 3) onesweep_pass(PassParams p) {
 #pragma unroll
         for (int j = 0; j < kItems; ++j) {
             const bool valid = wofs + j * 32 + lane < tile_n;
-            const uint32_t d = valid ? ((uint32_t)(k[j] >> p.shift) & dmask) : 0xFFFFFFFFu;
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-            uint32_t prior = 0, r = 0;
-            if (valid) {
-                prior = wh[d];
-                r = prior + __popc(peers & lanemask_lt());
+            const uint32_t d = (uint32_t)(k[j] >> p.shift) & dmask;
+            // Lanes holding the same digit. Every warp collective below is
+            // executed by all 32 lanes (valid or not); only the results are
+            // masked, never the calls.
+            uint32_t peers;
+            if (kMatch == 1 || (kMatch == 2 && (j & 1))) {
+                peers = __match_any_sync(0xFFFFFFFFu, valid ? d : 0xFFFFFFFFu);
+            } else {
+                // One ballot per digit bit; bits above p.bits are zero in every
+                // lane's digit, so their ballot leaves `peers` unchanged.
+                const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
+                peers = vmask;
+#pragma unroll
+                for (int b = 0; b < kRadixBits; ++b) {
+                    const bool bit = (d >> b) & 1u;
+                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                    peers &= bit ? m : ~m;
+                }
+                if (!valid) peers = ~vmask;  // invalid lanes: a group of their own, unused
             }
+            // The highest peer adds the group's size to the warp's digit
+            // counter and broadcasts the count before it.
+            const uint32_t upto = __popc(peers & lanemask_le());
+            const uint32_t leader = 31 - __clz(peers);
+            uint32_t prior = 0;
+            if (valid && lane == leader) prior = atomicAdd(&wh[d], upto);
+            prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
+            const uint32_t r = prior + upto - 1;
             if (j & 1) rank2[j / 2] |= r << 16;
             else rank2[j / 2] = r;
-            __syncwarp();
-            if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = prior + __popc(peers);
-            __syncwarp();
         }
         __syncthreads();
 
@@ -281,28 +300,50 @@ __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin
 
 }  // namespace
 
+// Shape table: (items per thread, minimum CTAs per SM, match mode).
+#define DAGC_SORT_SHAPES(X) \
+    X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2)
+
+namespace {
+struct ShapeEntry {
+    int items, min_ctas;
+    void (*keys)(PassParams);
+    void (*pairs)(PassParams);
+    size_t smem_keys, smem_pairs;
+};
+#define DAGC_SHAPE_ENTRY(id, items, ctas, match)                                                     \
+    {items, ctas, onesweep_pass<kPassThreads, items, false, ctas, match>,                             \
+     onesweep_pass<kPassThreads, items, true, ctas, match>, sizeof(PassSmem<kPassThreads, items, false>), \
+     sizeof(PassSmem<kPassThreads, items, true>)},
+const ShapeEntry kShapes[kNumSortShapes] = {DAGC_SORT_SHAPES(DAGC_SHAPE_ENTRY)};
+#undef DAGC_SHAPE_ENTRY
+}  // namespace
+
+int sort_shape_items(int shape) { return kShapes[shape].items; }
+int sort_shape_min_ctas(int shape) { return kShapes[shape].min_ctas; }
+
 size_t sort_pass_smem(bool with_values) {
-    return with_values ? sizeof(PassSmem<kPairThreads, kPairItems, true>)
-                       : sizeof(PassSmem<kKeyThreads, kKeyItems, false>);
+    size_t m = 0;
+    for (const ShapeEntry& e : kShapes) m = std::max(m, with_values ? e.smem_pairs : e.smem_keys);
+    return m;
 }
 
 void sort_configure() {
-    cudaFuncSetAttribute(onesweep_pass<kPairThreads, kPairItems, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sort_pass_smem(true));
-    cudaFuncSetAttribute(onesweep_pass<kKeyThreads, kKeyItems, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sort_pass_smem(false));
+    for (const ShapeEntry& e : kShapes) {
+        cudaFuncSetAttribute(e.keys, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem_keys);
+        cudaFuncSetAttribute(e.pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem_pairs);
+    }
 }
 
-int occupancy_sort_pass(bool with_values) {
+int occupancy_sort_shape(int shape, bool with_values) {
+    const ShapeEntry& e = kShapes[shape];
     int occ = 0;
-    if (with_values)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<kPairThreads, kPairItems, true>,
-                                                      kPairThreads, sort_pass_smem(true));
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, onesweep_pass<kKeyThreads, kKeyItems, false>,
-                                                      kKeyThreads, sort_pass_smem(false));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, with_values ? e.pairs : e.keys, kPassThreads,
+                                                  with_values ? e.smem_pairs : e.smem_keys);
     return occ;
 }
+
+int occupancy_sort_pass(bool with_values) { return occupancy_sort_shape(1, with_values); }
 
 // Launch parameters of digit pass i: the passes ping-pong so that the last
 // one always writes keys_out (pass i writes keys_out when passes-1-i is even).
@@ -338,10 +379,10 @@ void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
 
 void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
     const PassParams p = pass_params(a, i);
-    if (a.with_values)
-        onesweep_pass<kPairThreads, kPairItems, true><<<a.grid_pass, kPairThreads, sort_pass_smem(true), s>>>(p);
-    else
-        onesweep_pass<kKeyThreads, kKeyItems, false><<<a.grid_pass, kKeyThreads, sort_pass_smem(false), s>>>(p);
+    const ShapeEntry& e = kShapes[a.shape < 0 || a.shape >= kNumSortShapes ? 1 : a.shape];
+    void* args[] = {const_cast<PassParams*>(&p)};
+    cudaLaunchKernel(a.with_values ? (const void*)e.pairs : (const void*)e.keys, dim3(a.grid_pass),
+                     dim3(kPassThreads), args, a.with_values ? e.smem_pairs : e.smem_keys, s);
 }
 
 void launch_sort(const SortArgs& a, cudaStream_t s) {

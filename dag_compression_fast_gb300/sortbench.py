@@ -18,26 +18,36 @@ import sys
 import numpy as np
 
 
-def run(ctx, n: int, lo: int, hi: int, reps: int, seed: int = 1):
+def run(ctx, n: int, lo: int, hi: int, reps: int, seed: int = 1, pairs: bool = False):
     import torch
     rng = np.random.default_rng(seed)
     keys = torch.from_numpy(rng.integers(0, 2**63, n, dtype=np.int64)).cuda()
     out = torch.empty_like(keys)
+    vout = torch.empty(n, dtype=torch.int32, device=keys.device)
     import dag_compression_fast_gb300 as D
     lib = D.lib()
     s = torch.cuda.current_stream()
+
+    def once():
+        if pairs:
+            ctx._check(lib.dagc_sort_pairs(ctx.handle, keys.data_ptr(), out.data_ptr(), None, vout.data_ptr(), n,
+                                           lo, hi, s.cuda_stream))
+        else:
+            ctx._check(lib.dagc_sort_keys(ctx.handle, keys.data_ptr(), out.data_ptr(), n, lo, hi, s.cuda_stream))
+
     for _ in range(2):
-        ctx._check(lib.dagc_sort_keys(ctx.handle, keys.data_ptr(), out.data_ptr(), n, lo, hi, s.cuda_stream))
+        once()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
     for _ in range(reps):
-        ctx._check(lib.dagc_sort_keys(ctx.handle, keys.data_ptr(), out.data_ptr(), n, lo, hi, s.cuda_stream))
+        once()
     e1.record(s)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / reps
     passes = (hi - lo + 7) // 8
-    bytes_ = 8 * n + passes * 16 * n
+    kv = 12 if pairs else 8
+    bytes_ = 8 * n + passes * 2 * kv * n
     return n / sec / 1e9, bytes_ / sec / 1e9
 
 
@@ -47,11 +57,21 @@ def main(argv=None):
     p.add_argument("--lo", type=int, default=6)
     p.add_argument("--hi", type=int, default=33)
     p.add_argument("--reps", type=int, default=5)
-    p.add_argument("--sweep", choices=["none", "bits", "n"], default="none")
+    p.add_argument("--sweep", choices=["none", "bits", "n", "shapes"], default="none")
+    p.add_argument("--pairs", action="store_true", help="key/value pairs (values = input positions)")
+    p.add_argument("--shape", type=int, default=-1, help="digit-pass kernel shape (dagc_set_option)")
     a = p.parse_args(argv)
     import dag_compression_fast_gb300 as D
     ctx = D.Context(0)
-    if a.sweep == "bits":
+    opt = D.OPT_SORT_SHAPE_PAIRS if a.pairs else D.OPT_SORT_SHAPE_KEYS
+    if a.shape >= 0:
+        ctx.set_option(opt, a.shape)
+    if a.sweep == "shapes":
+        for sh in range(D.NUM_SORT_SHAPES):
+            ctx.set_option(opt, sh)
+            gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps, pairs=a.pairs)
+            print(f"shape={sh};{'pairs' if a.pairs else 'keys'};{a.hi - a.lo};{a.n};{gk:.3f};{gb:.1f}", flush=True)
+    elif a.sweep == "bits":
         for bits in range(1, 65):
             gk, gb = run(ctx, 100_000_000, 0, bits, a.reps)
             print(f"{bits};{100_000_000};{gk:.3f};{gb:.1f}", flush=True)
@@ -60,7 +80,7 @@ def main(argv=None):
             gk, gb = run(ctx, n, 0, 64, a.reps)
             print(f"64;{n};{gk:.3f};{gb:.1f}", flush=True)
     else:
-        gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps)
+        gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps, pairs=a.pairs)
         print(f"{a.hi - a.lo};{a.n};{gk:.3f};{gb:.1f}", flush=True)
     ctx.close()
     return 0

@@ -122,6 +122,16 @@ int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int
  * l in [0, depth-2). Returns the number of values written (<= cap). */
 int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
 
+/* ------------------------------------------------------------ options ---- */
+/* Kernel-shape options (the autotuner's knobs). Shapes of the digit-pass
+ * kernel, as (keys per thread, resident CTAs per SM, equal-digit matching by
+ * ballots / match.any / alternating): 0 = (16, 2, ballot), 1 = (16, 3, ballot),
+ * 2 = (12, 3, ballot), 3 = (8, 4, ballot), 4 = (16, 3, match),
+ * 5 = (16, 3, alternate), 6 = (16, 2, alternate), 7 = (12, 3, alternate). */
+#define DAGC_OPT_SORT_SHAPE_KEYS 1   /* keys-only sorts (the fragment sort) */
+#define DAGC_OPT_SORT_SHAPE_PAIRS 2  /* key/value sorts (leaf and node hashes) */
+int dagc_set_option(dagc_context ctx, int option, int value);
+
 /* ---------------------------------------------------- instrumentation ---- */
 /* Off by default. When enabled, each stage of a call is bracketed by CUDA
  * events recorded on the call's own stream; device time, kernel launches and
