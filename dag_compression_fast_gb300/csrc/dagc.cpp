@@ -1045,7 +1045,6 @@ int dagc_context_create(int device, dagc_context* out) {
     kernels_configure();
     e = cudaMallocHost(&c->h_stage, 4096);
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
-    int occ = 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumSortShapes; ++sh) {
         c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
