@@ -49,6 +49,7 @@ DAGC_SYMBOLS = [
     "dagc_compress_host",
     "dagc_compress", "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
+    "dagc_sort_keys_noalloc",
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
@@ -117,6 +118,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_kernel_launches.argtypes = [vp, pu64]
         L.dagc_sort_keys.argtypes = [vp, vp, vp, u64, i32, i32, vp]
         L.dagc_sort_pairs.argtypes = [vp, vp, vp, vp, vp, u64, i32, i32, vp]
+        L.dagc_sort_keys_noalloc.argtypes = [vp, vp, u64, i32, i32, vp]
         _lib = L
     return _lib
 

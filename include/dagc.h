@@ -167,6 +167,20 @@ int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_key
                     const uint32_t* d_vals_in, uint32_t* d_vals_out, uint64_t n, int lo_bit,
                     int hi_bit, void* stream);
 
+/* No counterpart in the reference. The key sort of dagc_sort_keys without any
+ * allocation, for callers that must not allocate device memory once running:
+ * engines and servers that reserve the device through their own allocator
+ * (an ad-hoc cudaMalloc would fail or fragment that reservation) and callers
+ * that cannot take cudaMalloc's implicit device synchronisation. Scratch is a
+ * fixed ~9.1 MB device array inside the library, present on every GPU that
+ * loads it until the process exits. n <= 1048576 keys (else
+ * DAGC_ERR_TOO_LARGE, nothing touched); d_in is left intact; no context. The
+ * first call on a device sets the array up: make it before any stream
+ * capture. Calls share the array, so calls whose GPU work overlaps race.
+ * Synchronous on return; returns a dagc status. */
+int dagc_sort_keys_noalloc(const uint64_t* d_in, uint64_t* d_out, uint64_t n, int lo_bit,
+                           int hi_bit, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
