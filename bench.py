@@ -75,7 +75,7 @@ def measured_peaks():
 def traffic_per_pass_bytes(n_keys: int):
     """DRAM bytes of one fragment-sort digit pass, from the committed ncu summary
     (bytes per key, measured on a smaller case and scaled by the key count)."""
-    path = os.path.join(REPO, "profiles", "onesweep_pass_terrain_d11.md")
+    path = os.path.join(REPO, "profiles", "onesweep_pass_keys_20M_27bit.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -216,10 +216,9 @@ def main():
             dist.barrier()
 
     # ---- timed region: device-resident fragments -> device-resident DAG ----
+    # (the production path: each call's kernel sequence replays as a CUDA graph)
     sampler = ClockSampler(local)
     sampler.start()
-    ctx.profile(True)
-    ctx.profile_reset()
     launches0 = ctx.kernel_launches()
     barrier()
     torch.cuda.synchronize()
@@ -232,8 +231,6 @@ def main():
     barrier()
     ms = e0.elapsed_time(e1)
     launches = ctx.kernel_launches() - launches0
-    ctx.profile(False)
-    prof = ctx.profile_read()
     clocks = sampler.stop()
     if world > 1:
         import torch.distributed as dist
@@ -241,6 +238,15 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = n * args.steps * world / (ms / 1e3)
+
+    # ---- the same steps with CUDA events around every stage and digit pass ----
+    ctx.profile(True)
+    ctx.profile_reset()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    ctx.profile(False)
+    prof = ctx.profile_read()
 
     # ---- end to end: pinned host fragments -> host words, copies included ----
     h_codes = torch.from_numpy(codes.view(np.int64)).pin_memory()
@@ -279,7 +285,9 @@ def main():
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": per_launch_traffic,
                 "algorithmic_bytes_per_launch": pass_bytes // max(pass_launches, 1),
-                "avg_launch_ms": pass_ms / max(pass_launches, 1), "launches": pass_launches}
+                "avg_launch_ms": pass_ms / max(pass_launches, 1), "launches": pass_launches,
+                "timing": "CUDA events around each launch on the call's stream, over --steps profiled "
+                          "steps run right after the timed region (same workload)"}
     stages = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
                   "gbs": round((v[2] / 1e9) / (v[0] / 1e3), 1) if v[0] > 0 and v[2] else None}
               for k, v in prof.items() if v[1]}

@@ -28,6 +28,7 @@ LIBGEN_PATH = os.path.join(LIB_DIR, "libdagc_gen.so")
 
 OPT_SORT_SHAPE_KEYS = 1
 OPT_SORT_SHAPE_PAIRS = 2
+OPT_GRAPHS = 3
 NUM_SORT_SHAPES = 8
 
 OK = 0
@@ -42,7 +43,7 @@ ERR_TOO_LARGE = 7
 # Every symbol of include/dagc.h, in declaration order.
 DAGC_SYMBOLS = [
     "dagc_context_create", "dagc_context_destroy", "dagc_last_error", "dagc_status_string",
-    "dagc_version", "dagc_create", "dagc_dag_num_levels", "dagc_dag_level_size",
+    "dagc_version", "dagc_create", "dagc_create_batched", "dagc_dag_num_levels", "dagc_dag_level_size",
     "dagc_dag_num_leaves", "dagc_dag_level_device", "dagc_dag_leaves_device",
     "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_free",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
@@ -93,6 +94,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_status_string.argtypes = [i32]
         L.dagc_status_string.restype = ctypes.c_char_p
         L.dagc_create.argtypes = [vp, vp, u64, i32, vp, pvp]
+        L.dagc_create_batched.argtypes = [vp, vp, vp, vp, u64, i32, i32, vp, pvp]
         L.dagc_dag_num_levels.argtypes = [vp, ctypes.POINTER(i32)]
         L.dagc_dag_level_size.argtypes = [vp, i32, pu64]
         L.dagc_dag_num_leaves.argtypes = [vp, pu64]
@@ -306,6 +308,25 @@ class Context:
         ptr, n, keep = _device_u64(fragments, self.device)
         out = ctypes.c_void_p()
         st = lib().dagc_create(self.handle, ptr, n, depth, _stream_handle(stream), ctypes.byref(out))
+        del keep
+        self._check(st)
+        return Dag(self, out.value)
+
+    def create_dag_batched(self, fragments, chunk_counts, chunk_morton, chunk_depth: int, top_levels: int,
+                           stream=None) -> Dag:
+        """Batched CreateDAG + MergeDAGs: chunk-local fragments of k chunks back to
+        back (chunk_counts[i] each), chunks in ascending Morton order
+        chunk_morton[i] of a 2^top_levels-per-side chunk grid."""
+        ptr, n, keep = _device_u64(fragments, self.device)
+        counts = np.ascontiguousarray(chunk_counts, np.uint64)
+        offsets = np.zeros(counts.size + 1, np.uint64)
+        offsets[1:] = np.cumsum(counts, dtype=np.uint64)
+        morton = np.ascontiguousarray(chunk_morton, np.uint64)
+        if int(offsets[-1]) != n:
+            raise DagcError(ERR_INVALID_ARGUMENT, "chunk counts do not add up to the fragment count")
+        out = ctypes.c_void_p()
+        st = lib().dagc_create_batched(self.handle, ptr, _np_ptr(offsets), _np_ptr(morton), counts.size,
+                                       chunk_depth, top_levels, _stream_handle(stream), ctypes.byref(out))
         del keep
         self._check(st)
         return Dag(self, out.value)

@@ -42,13 +42,24 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* counter, uint32_t* s_slo
 struct LeafSmem {
     uint64_t keys[kPadded];
     uint64_t run_or[kTile];
-    uint64_t run_par[kTile];
+    uint16_t run_head[kTile];  // tile-local index of each run's first key
     uint32_t scan[34];
     uint32_t slot;
-    uint64_t tail_or;
+    uint64_t lead_or;
     uint64_t p_base;
 };
 
+// Batched input: (segment << seg_shift) | local -> (seg_code[segment] << seg_shift) | local.
+__device__ __forceinline__ uint64_t global_code(const LeafBuildArgs& a, uint64_t key) {
+    if (!a.seg_code) return key;
+    const uint64_t local = key & ((1ull << a.seg_shift) - 1);
+    return (__ldg(a.seg_code + (key >> a.seg_shift)) << a.seg_shift) | local;
+}
+
+// Fused unique + leaf build. Each tile emits the runs that START in it (one
+// (parent, mask) pair per distinct code >> 6); keys before the tile's first
+// head continue a run owned by an earlier tile: their OR goes to lead_or[tile]
+// and leaf_fixup folds it into that run's mask after this kernel.
 __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LeafSmem& S = *reinterpret_cast<LeafSmem*>(smem_raw);
@@ -62,44 +73,46 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
         const uint64_t base = (uint64_t)tile * kTile;
         const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
         for (int i = tid; i < kTile; i += kT) {
-            if (i < (int)tile_n) S.keys[pad8(i)] = a.sorted[base + i];
+            if (i < (int)tile_n) S.keys[pad8(i)] = global_code(a, a.sorted[base + i]);
             S.run_or[i] = 0;
         }
+        if (tid == 0) S.lead_or = 0;
         __syncthreads();
 
+        // Head flags of this thread's kI consecutive keys.
         const int i0 = tid * kI;
-        uint64_t prev;
-        bool have_prev;
-        if (i0 == 0) {
-            have_prev = base > 0;
-            prev = have_prev ? (a.sorted[base - 1] >> 6) : 0;
-        } else {
-            have_prev = true;
-            prev = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0;
-        }
+        bool hp;
+        uint64_t pv;
+        if (i0 == 0) { hp = base > 0; pv = hp ? (global_code(a, a.sorted[base - 1]) >> 6) : 0; }
+        else { hp = true; pv = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0; }
+        const bool hp0 = hp;
+        const uint64_t pv0 = pv;
         uint32_t heads = 0;
 #pragma unroll
         for (int j = 0; j < kI; ++j) {
             const int i = i0 + j;
             if (i < (int)tile_n) {
                 const uint64_t par = S.keys[pad8(i)] >> 6;
-                if (!have_prev || par != prev) ++heads;
-                prev = par;
-                have_prev = true;
+                if (!hp || par != pv) ++heads;
+                pv = par;
+                hp = true;
             }
         }
         uint32_t total_heads;
         const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
 
-        // Accumulate run ORs; runs are tile-local indices, -1 = the previous
-        // tile's open run (handled by that tile's read-ahead).
+        // Warp 0 looks back first, so that the wait overlaps the other warps'
+        // run accumulation; it accumulates its own runs afterwards.
+        if (warp == 0) {
+            const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
+            if (lane == 0) S.p_base = pb;
+        }
+        // Accumulate run ORs; run -1 = keys before the tile's first head.
         {
             int run = (int)excl - 1;
             uint64_t acc = 0;
-            bool hp = false;
-            uint64_t pv = 0;
-            if (i0 == 0) { hp = base > 0; pv = hp ? (a.sorted[base - 1] >> 6) : 0; }
-            else { hp = true; pv = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0; }
+            hp = hp0;
+            pv = pv0;
 #pragma unroll
             for (int j = 0; j < kI; ++j) {
                 const int i = i0 + j;
@@ -107,61 +120,55 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
                     const uint64_t key = S.keys[pad8(i)];
                     const uint64_t par = key >> 6;
                     if (!hp || par != pv) {
-                        if (run >= 0 && acc) atomicOr((unsigned long long*)&S.run_or[run], (unsigned long long)acc);
+                        if (acc) atomicOr((unsigned long long*)(run >= 0 ? &S.run_or[run] : &S.lead_or),
+                                          (unsigned long long)acc);
                         ++run;
                         acc = 0;
-                        S.run_par[run] = par;
+                        S.run_head[run] = (uint16_t)i;
                     }
                     acc |= 1ull << (key & 63);
                     pv = par;
                     hp = true;
                 }
             }
-            if (run >= 0 && acc) atomicOr((unsigned long long*)&S.run_or[run], (unsigned long long)acc);
-        }
-        if (tid == 0) S.tail_or = 0;
-        __syncthreads();
-
-        if (warp == 0) {
-            const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
-            if (lane == 0) S.p_base = pb;
-        } else if (warp == 1 && total_heads > 0 && base + tile_n < n) {
-            // Read ahead: the tile's last run may continue into later tiles.
-            const uint64_t last_par = S.run_par[total_heads - 1];
-            uint64_t acc = 0;
-            for (uint64_t pos = base + tile_n;; pos += 32) {
-                const uint64_t i = pos + lane;
-                const bool in = i < n;
-                const uint64_t key = in ? a.sorted[i] : 0;
-                const bool match = in && (key >> 6) == last_par;
-                const uint32_t m = __ballot_sync(0xFFFFFFFFu, match);
-                const uint32_t run_len = __ffs(~m) ? (uint32_t)(__ffs(~m) - 1) : 32u;
-                if (lane < run_len) acc |= 1ull << (key & 63);
-                if (run_len < 32) break;
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-            if (lane == 0) S.tail_or = acc;
+            if (acc) atomicOr((unsigned long long*)(run >= 0 ? &S.run_or[run] : &S.lead_or), (unsigned long long)acc);
         }
         __syncthreads();
         const uint64_t p_base = S.p_base;
         bool overflow = false;
         for (uint32_t r = tid; r < total_heads; r += kT) {
-            uint64_t m = S.run_or[r];
-            if (r == total_heads - 1) m |= S.tail_or;
             if (p_base + r < a.out_capacity) {
-                a.parents[p_base + r] = S.run_par[r];
-                a.leaves[p_base + r] = m;
+                a.parents[p_base + r] = S.keys[pad8(S.run_head[r])] >> 6;
+                a.leaves[p_base + r] = S.run_or[r];
             } else {
                 overflow = true;
             }
         }
         if (overflow) atomicOr(a.err, kErrCapacity);
-        if (tid == 0 && base + tile_n == n) {
-            const uint64_t cnt = p_base + total_heads;
-            *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
+        if (tid == 0) {
+            // Keys continuing the previous run: folded in by leaf_fixup. Tile 0
+            // starts with a head, so it never has any.
+            a.lead_or[tile] = S.lead_or;
+            a.lead_run[tile] = p_base - 1;
+            if (base + tile_n == n) {
+                const uint64_t cnt = p_base + total_heads;
+                *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
+            }
         }
         __syncthreads();
+    }
+}
+
+// ORs every tile's leading keys into the run they continue (written by an
+// earlier tile of leaf_build, one launch before, with a plain store).
+__global__ void leaf_fixup(LeafBuildArgs a) {
+    const uint64_t n = load_count(a.d_n, a.n_bound);
+    const uint32_t ntiles = scan_tiles(n);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+        if (t == 0) continue;
+        const uint64_t m = a.lead_or[t];
+        const uint64_t r = a.lead_run[t];
+        if (m && r < a.out_capacity) atomicOr((unsigned long long*)&a.leaves[r], (unsigned long long)m);
     }
 }
 
@@ -666,6 +673,9 @@ int occupancy_kernel(int which) {
 
 void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s) {
     leaf_build<<<a.grid, kT, sizeof(LeafSmem), s>>>(a);
+    const uint64_t tiles = scan_tiles(a.n_bound);
+    const int grid = (int)std::min<uint64_t>((tiles + 255) / 256, (uint64_t)g_blocks_small);
+    leaf_fixup<<<grid > 0 ? grid : 1, 256, 0, s>>>(a);
 }
 void launch_extract(const ExtractArgs& a, cudaStream_t s) {
     extract_level<<<a.grid, kT, sizeof(ExtractSmem), s>>>(a);

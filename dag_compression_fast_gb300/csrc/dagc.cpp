@@ -164,9 +164,31 @@ struct PendingTiming {
     uint64_t bytes;
 };
 
+// A recorded CreateDAG pipeline: valid for one input pointer, size, depth,
+// arena block and pass shapes.
+struct GraphKey {
+    const void* frag;
+    uint64_t n;
+    int depth;
+    void* arena;
+    uint32_t chunks;  // batched calls: number of chunks (0 otherwise)
+    bool operator==(const GraphKey& o) const {
+        return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks;
+    }
+};
+struct GraphEntry {
+    GraphKey key;
+    int shape_keys, shape_pairs;
+    cudaGraphExec_t exec;
+    uint64_t launches;
+};
+
 struct dagc_context_t {
     int device = 0;
     bool profiling = false;
+    bool use_graphs = true;
+    cudaStream_t capture_stream = nullptr;
+    std::vector<GraphEntry> graphs;
     int shape_keys = 5, shape_pairs = 3;  // digit-pass shapes (see dagc_set_option), tuned on GB300
     int occ_keys[kNumSortShapes] = {}, occ_pairs[kNumSortShapes] = {};
     StageStats stages[DAGC_NUM_STAGES];
@@ -319,12 +341,19 @@ struct SortBuffers {
     uint32_t* status[2];
 };
 
+struct SegmentSpec {
+    const uint64_t* d_offsets;
+    uint32_t count;
+    int shift;
+};
+
 // pass_stage >= 0: time the histogram under hist_stage and every digit pass
 // separately under pass_stage (host-known n only, for the byte counts).
 int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint64_t* keys_in,
              uint64_t* keys_out, uint64_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
              uint32_t* vals_alt, bool with_values, uint64_t n_bound, const uint64_t* d_n, int lo, int hi,
-             int validate_bits, cudaStream_t s, int hist_stage = -1, int pass_stage = -1) {
+             int validate_bits, cudaStream_t s, int hist_stage = -1, int pass_stage = -1,
+             const SegmentSpec* seg = nullptr) {
     if (cs.next_hist >= kMaxSorts || cs.next_counter + kMaxPasses > kMaxTileCounters)
         return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many sorts in one call");
     SortArgs a{};
@@ -348,6 +377,11 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     const uint64_t tiles = sort_tiles(n_bound);
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
     a.shape = with_values ? ctx->shape_pairs : ctx->shape_keys;
+    if (seg && seg->d_offsets) {
+        a.seg_offsets = seg->d_offsets;
+        a.seg_count = seg->count;
+        a.seg_shift = seg->shift;
+    }
     const int occ = with_values ? ctx->occ_pairs[a.shape] : ctx->occ_keys[a.shape];
     const uint64_t shape_tiles = (n_bound + 256ull * sort_shape_items(a.shape) - 1) / (256ull * sort_shape_items(a.shape));
     a.grid_pass = grid_for(occ, ctx->sms, std::min<uint64_t>(tiles, shape_tiles));
@@ -410,6 +444,64 @@ uint64_t level_cap(int level, uint64_t n) {
     return std::min<uint64_t>(n, 1ull << (3 * level));
 }
 
+void drop_graphs(dagc_context ctx) {
+    for (GraphEntry& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    ctx->graphs.clear();
+}
+
+// Runs `enqueue` (which puts one call's whole kernel sequence on a stream).
+// With graphs on, the sequence is recorded once on the context's own capture
+// stream and replayed on `s` afterwards, which removes the per-launch host
+// cost; with profiling on (events per stage) it is launched directly.
+template <typename F>
+int run_enqueue(dagc_context ctx, const GraphKey& key, cudaStream_t s, F&& enqueue) {
+    if (!ctx->use_graphs || ctx->profiling || !ctx->capture_stream) return enqueue(s);
+    for (GraphEntry& g : ctx->graphs) {
+        if (g.key == key && g.shape_keys == ctx->shape_keys && g.shape_pairs == ctx->shape_pairs) {
+            DAGC_CUDA(ctx, cudaGraphLaunch(g.exec, s));
+            ctx->launches += g.launches;
+            return DAGC_OK;
+        }
+    }
+    // Entries made for an arena block that has since been replaced are dead.
+    for (size_t i = 0; i < ctx->graphs.size();) {
+        if (ctx->graphs[i].key.arena != key.arena) {
+            cudaGraphExecDestroy(ctx->graphs[i].exec);
+            ctx->graphs.erase(ctx->graphs.begin() + i);
+        } else {
+            ++i;
+        }
+    }
+    const uint64_t l0 = ctx->launches;
+    DAGC_CUDA(ctx, cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal));
+    const int st = enqueue(ctx->capture_stream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->capture_stream, &graph);
+    const uint64_t recorded = ctx->launches - l0;
+    ctx->launches = l0;
+    if (st != DAGC_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (st != DAGC_OK) return st;
+        return enqueue(s);  // recording failed: launch directly
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        cudaGetLastError();
+        return enqueue(s);
+    }
+    if (ctx->graphs.size() >= 8) {
+        cudaGraphExecDestroy(ctx->graphs.front().exec);
+        ctx->graphs.erase(ctx->graphs.begin());
+    }
+    ctx->graphs.push_back({key, ctx->shape_keys, ctx->shape_pairs, exec, recorded});
+    DAGC_CUDA(ctx, cudaGraphLaunch(exec, s));
+    ctx->launches += recorded;
+    return DAGC_OK;
+}
+
 // -------------------------------------------------------------- CreateDAG --
 // Output of the device pipeline before materialisation: per-level unique
 // arrays in the scratch pools (upper-bound strides) and the counts.
@@ -422,8 +514,23 @@ struct CreatePools {
     uint64_t num_leaves = 0;
 };
 
+// Batched input (see dagc_create_batched): chunk offsets into the fragment
+// array and each chunk's Morton index in the grid of chunks, host arrays.
+struct BatchSpec {
+    const uint64_t* h_offsets;  // k + 1
+    const uint64_t* h_morton;   // k, ascending
+    uint32_t k;
+    int chunk_depth;
+};
+
+int bits_for(uint64_t values) {  // bits to tell `values` values apart
+    int b = 0;
+    while (b < 64 && (values - 1) >> b) ++b;
+    return b;
+}
+
 int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
-                    CreatePools& out) {
+                    CreatePools& out, const BatchSpec* batch = nullptr) {
     const int nl = depth - 2;
     const int bits = 3 * depth;
     std::vector<uint64_t> cap(nl);
@@ -461,165 +568,193 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         o_pc[l] = L.take<uint32_t>(cap[l] * 8);
         o_pm[l] = L.take<uint8_t>(cap[l]);
     }
+    const size_t o_lead_or = L.take<uint64_t>(scan_tiles(n) + 1);
+    const size_t o_lead_run = L.take<uint64_t>(scan_tiles(n) + 1);
+    const size_t o_seg_off = L.take<uint64_t>(batch ? batch->k + 1 : 0);
+    const size_t o_seg_code = L.take<uint64_t>(batch ? batch->k : 0);
     DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
     char* b = static_cast<char*>(ctx->arena.base);
     auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
     auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
     auto P8 = [&](size_t o) { return reinterpret_cast<uint8_t*>(b + o); };
-
-    CallSlots cs;
-    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
-    cs.sv_next = P64(o_sv);
-    cs.sv_end = P64(o_sv) + sv_total;
-    SortBuffers sb{{P32(o_ss0), P32(o_ss1)}};
-    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
-    uint32_t* err = &cs.h->err;
-
-    // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
-    //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
-    int st = run_sort(ctx, cs, sb, d_frag, P64(o_A), P64(o_B), nullptr, nullptr, nullptr, false, n, nullptr,
-                      6, std::max(6, bits), bits < 64 ? bits : 0, s, DAGC_STAGE_FRAGMENT_HIST,
-                      DAGC_STAGE_FRAGMENT_PASS);
-    if (st) return st;
-
-    // 2. Fused unique + leaf build.
-    {
-        StageTimer t(ctx, DAGC_STAGE_LEAF_BUILD, s);
-        LeafBuildArgs a{};
-        a.sorted = P64(o_A);
-        a.d_n = nullptr;
-        a.n_bound = n;
-        a.parents = P64(o_P);
-        a.leaves = P64(o_LM);
-        a.out_capacity = p0cap;
-        a.d_out_n = cs.count(kCntBricks);
-        a.status = cs.sv(n);
-        a.tile_counter = cs.counter();
-        a.err = err;
-        a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, scan_tiles(n));
-        launch_leaf_build(a, s);
-        ++ctx->launches;
-        DAGC_LAUNCHED(ctx);
-        t.stop();
+    // Fragment sort bits: the brick key [6, 3*depth); batched input sorts the
+    // composite (chunk rank << 3*chunk_depth) | local code instead, whose
+    // chunk rank needs only bits_for(k) bits (the chunks are in Morton order).
+    int sort_hi = std::max(6, bits), validate = bits < 64 ? bits : 0, seg_shift = 0;
+    if (batch) {
+        seg_shift = 3 * batch->chunk_depth;
+        sort_hi = std::max(6, seg_shift + bits_for(batch->k));
+        validate = seg_shift;
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_seg_off), batch->h_offsets, (batch->k + 1) * 8,
+                                       cudaMemcpyHostToDevice, s));
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_seg_code), batch->h_morton, batch->k * 8, cudaMemcpyHostToDevice, s));
     }
-    // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
-    StageTimer t_dedup(ctx, DAGC_STAGE_LEAF_DEDUP, s);
-    st = run_sort(ctx, cs, sb, P64(o_LM), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, p0cap,
-                  cs.count(kCntBricks), 0, 64, 0, s);
-    if (st) return st;
-    {
-        UniqueArgs a{};
-        a.keys = P64(o_SK);
-        a.perm = P32(o_V);
-        a.d_n = cs.count(kCntBricks);
-        a.n_bound = p0cap;
-        a.map = P32(o_M0);
-        a.out_keys = P64(o_PL);
-        a.out_capacity = p0cap;
-        a.d_out_n = cs.count(kCntLeaves);
-        a.status = cs.sv(p0cap);
-        a.tile_counter = cs.counter();
-        a.err = err;
-        a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(p0cap));
-        launch_unique(a, s);
-        ++ctx->launches;
-        DAGC_LAUNCHED(ctx);
-    }
-    t_dedup.stop();
-    // 4. Level loop, bottom-up.
-    StageTimer t_levels(ctx, DAGC_STAGE_LEVELS, s);
-    const uint64_t* child_codes = P64(o_P);
-    const uint32_t* child_map = P32(o_M0);
-    const uint64_t* child_hashes = P64(o_PL);
-    const uint64_t* d_child_n = cs.count(kCntBricks);
-    uint64_t child_bound = p0cap;
-    uint64_t* node_codes[2] = {P64(o_NC0), P64(o_NC1)};
-    uint32_t* maps[2] = {P32(o_M1), P32(o_M0)};
-    // Levels whose node bound fits one CTA's shared memory go to the tail
-    // kernel; the bound only grows with the level index, so they are the top
-    // tail_first + 1 levels.
-    int tail_first = -1;
-    while (tail_first + 1 < nl && tail_first + 1 < kMaxTailLevels && cap[tail_first + 1] <= (uint64_t)kTailCap)
-        ++tail_first;
-    for (int l = nl - 1, it = 0; l > tail_first; --l, ++it) {
-        ExtractArgs e{};
-        e.child_codes = child_codes;
-        e.child_map = child_map;
-        e.d_n = d_child_n;
-        e.n_bound = child_bound;
-        e.child_hashes = child_hashes;
-        e.node_codes = node_codes[it & 1];
-        e.node_masks = P8(o_NM);
-        e.node_children = P32(o_NCH);
-        e.node_hashes = P64(o_NH);
-        e.out_capacity = cap[l];
-        e.d_out_n = cs.count(kCntNodes + l);
-        e.status = cs.sv(child_bound);
-        e.tile_counter = cs.counter();
-        e.err = err;
-        e.grid = grid_for(ctx->grid_extract / ctx->sms, ctx->sms, scan_tiles(child_bound));
-        launch_extract(e, s);
-        ++ctx->launches;
-        DAGC_LAUNCHED(ctx);
 
-        st = run_sort(ctx, cs, sb, P64(o_NH), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
-                      cap[l], cs.count(kCntNodes + l), 0, 64, 0, s);
+    // Everything from here to the last kernel is enqueued by one function, so
+    // that it can be recorded once as a CUDA graph and replayed.
+    auto enqueue = [&](cudaStream_t s) -> int {
+        CallSlots cs;
+        cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
+        cs.sv_next = P64(o_sv);
+        cs.sv_end = P64(o_sv) + sv_total;
+        SortBuffers sb{{P32(o_ss0), P32(o_ss1)}};
+        DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+        uint32_t* err = &cs.h->err;
+
+        // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
+        //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
+        const SegmentSpec seg{batch ? P64(o_seg_off) : nullptr, batch ? batch->k : 0u, seg_shift};
+        int st = run_sort(ctx, cs, sb, d_frag, P64(o_A), P64(o_B), nullptr, nullptr, nullptr, false, n, nullptr,
+                          6, sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg);
         if (st) return st;
 
-        UniqueArgs u{};
-        u.keys = P64(o_SK);
-        u.perm = P32(o_V);
-        u.d_n = cs.count(kCntNodes + l);
-        u.n_bound = cap[l];
-        u.masks = P8(o_NM);
-        u.children = P32(o_NCH);
-        u.map = maps[it & 1];
-        u.out_keys = P64(o_ph[l]);
-        u.out_masks = P8(o_pm[l]);
-        u.out_children = P32(o_pc[l]);
-        u.out_capacity = cap[l];
-        u.d_out_n = cs.count(kCntUnique + l);
-        u.status = cs.sv(cap[l]);
-        u.tile_counter = cs.counter();
-        u.err = err;
-        u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(cap[l]));
-        launch_unique(u, s);
-        ++ctx->launches;
-        DAGC_LAUNCHED(ctx);
-
-        child_codes = node_codes[it & 1];
-        child_map = maps[it & 1];
-        child_hashes = P64(o_ph[l]);
-        d_child_n = cs.count(kCntNodes + l);
-        child_bound = cap[l];
-    }
-    if (tail_first >= 0) {
-        TailArgs ta{};
-        ta.first_level = tail_first;
-        ta.child_codes = child_codes;
-        ta.child_map = child_map;
-        ta.child_hashes = child_hashes;
-        ta.d_child_n = d_child_n;
-        ta.scratch_children = P32(o_NCH);
-        for (int l = 0; l <= tail_first; ++l) {
-            ta.lv[l].hashes = P64(o_ph[l]);
-            ta.lv[l].masks = P8(o_pm[l]);
-            ta.lv[l].children = P32(o_pc[l]);
-            ta.lv[l].capacity = cap[l];
-            ta.lv[l].d_nodes = cs.count(kCntNodes + l);
-            ta.lv[l].d_unique = cs.count(kCntUnique + l);
+        // 2. Fused unique + leaf build.
+        {
+            StageTimer t(ctx, DAGC_STAGE_LEAF_BUILD, s);
+            LeafBuildArgs a{};
+            a.sorted = P64(o_A);
+            a.d_n = nullptr;
+            a.n_bound = n;
+            a.parents = P64(o_P);
+            a.leaves = P64(o_LM);
+            a.out_capacity = p0cap;
+            a.lead_or = P64(o_lead_or);
+            a.lead_run = P64(o_lead_run);
+            a.seg_code = batch ? P64(o_seg_code) : nullptr;
+            a.seg_shift = seg_shift;
+            a.d_out_n = cs.count(kCntBricks);
+            a.status = cs.sv(n);
+            a.tile_counter = cs.counter();
+            a.err = err;
+            a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, scan_tiles(n));
+            launch_leaf_build(a, s);
+            ctx->launches += 2;
+            DAGC_LAUNCHED(ctx);
+            t.stop();
         }
-        ta.err = err;
-        launch_tail(ta, s);
-        ++ctx->launches;
-        DAGC_LAUNCHED(ctx);
-    }
+        // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
+        StageTimer t_dedup(ctx, DAGC_STAGE_LEAF_DEDUP, s);
+        st = run_sort(ctx, cs, sb, P64(o_LM), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, p0cap,
+                      cs.count(kCntBricks), 0, 64, 0, s);
+        if (st) return st;
+        {
+            UniqueArgs a{};
+            a.keys = P64(o_SK);
+            a.perm = P32(o_V);
+            a.d_n = cs.count(kCntBricks);
+            a.n_bound = p0cap;
+            a.map = P32(o_M0);
+            a.out_keys = P64(o_PL);
+            a.out_capacity = p0cap;
+            a.d_out_n = cs.count(kCntLeaves);
+            a.status = cs.sv(p0cap);
+            a.tile_counter = cs.counter();
+            a.err = err;
+            a.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(p0cap));
+            launch_unique(a, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
+        }
+        t_dedup.stop();
+        // 4. Level loop, bottom-up.
+        StageTimer t_levels(ctx, DAGC_STAGE_LEVELS, s);
+        const uint64_t* child_codes = P64(o_P);
+        const uint32_t* child_map = P32(o_M0);
+        const uint64_t* child_hashes = P64(o_PL);
+        const uint64_t* d_child_n = cs.count(kCntBricks);
+        uint64_t child_bound = p0cap;
+        uint64_t* node_codes[2] = {P64(o_NC0), P64(o_NC1)};
+        uint32_t* maps[2] = {P32(o_M1), P32(o_M0)};
+        // Levels whose node bound fits one CTA's shared memory go to the tail
+        // kernel; the bound only grows with the level index, so they are the top
+        // tail_first + 1 levels.
+        int tail_first = -1;
+        while (tail_first + 1 < nl && tail_first + 1 < kMaxTailLevels && cap[tail_first + 1] <= (uint64_t)kTailCap)
+            ++tail_first;
+        for (int l = nl - 1, it = 0; l > tail_first; --l, ++it) {
+            ExtractArgs e{};
+            e.child_codes = child_codes;
+            e.child_map = child_map;
+            e.d_n = d_child_n;
+            e.n_bound = child_bound;
+            e.child_hashes = child_hashes;
+            e.node_codes = node_codes[it & 1];
+            e.node_masks = P8(o_NM);
+            e.node_children = P32(o_NCH);
+            e.node_hashes = P64(o_NH);
+            e.out_capacity = cap[l];
+            e.d_out_n = cs.count(kCntNodes + l);
+            e.status = cs.sv(child_bound);
+            e.tile_counter = cs.counter();
+            e.err = err;
+            e.grid = grid_for(ctx->grid_extract / ctx->sms, ctx->sms, scan_tiles(child_bound));
+            launch_extract(e, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
 
-    t_levels.stop();
-    if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
+            st = run_sort(ctx, cs, sb, P64(o_NH), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
+                          cap[l], cs.count(kCntNodes + l), 0, 64, 0, s);
+            if (st) return st;
+
+            UniqueArgs u{};
+            u.keys = P64(o_SK);
+            u.perm = P32(o_V);
+            u.d_n = cs.count(kCntNodes + l);
+            u.n_bound = cap[l];
+            u.masks = P8(o_NM);
+            u.children = P32(o_NCH);
+            u.map = maps[it & 1];
+            u.out_keys = P64(o_ph[l]);
+            u.out_masks = P8(o_pm[l]);
+            u.out_children = P32(o_pc[l]);
+            u.out_capacity = cap[l];
+            u.d_out_n = cs.count(kCntUnique + l);
+            u.status = cs.sv(cap[l]);
+            u.tile_counter = cs.counter();
+            u.err = err;
+            u.grid = grid_for(ctx->grid_unique / ctx->sms, ctx->sms, scan_tiles(cap[l]));
+            launch_unique(u, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
+
+            child_codes = node_codes[it & 1];
+            child_map = maps[it & 1];
+            child_hashes = P64(o_ph[l]);
+            d_child_n = cs.count(kCntNodes + l);
+            child_bound = cap[l];
+        }
+        if (tail_first >= 0) {
+            TailArgs ta{};
+            ta.first_level = tail_first;
+            ta.child_codes = child_codes;
+            ta.child_map = child_map;
+            ta.child_hashes = child_hashes;
+            ta.d_child_n = d_child_n;
+            ta.scratch_children = P32(o_NCH);
+            for (int l = 0; l <= tail_first; ++l) {
+                ta.lv[l].hashes = P64(o_ph[l]);
+                ta.lv[l].masks = P8(o_pm[l]);
+                ta.lv[l].children = P32(o_pc[l]);
+                ta.lv[l].capacity = cap[l];
+                ta.lv[l].d_nodes = cs.count(kCntNodes + l);
+                ta.lv[l].d_unique = cs.count(kCntUnique + l);
+            }
+            ta.err = err;
+            launch_tail(ta, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
+        }
+
+        t_levels.stop();
+        if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
+    return DAGC_OK;
+    };
+    int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u}, s, enqueue);
+    if (st) return st;
+    CallHeader* hdr = reinterpret_cast<CallHeader*>(b + o_hdr);
     // 5. One read-back of every count and the error word.
     static_assert(sizeof(CallHeader) >= 8 * 65, "header");
-    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, cs.h, 8 + 8 * 64, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, hdr, 8 + 8 * 64, cudaMemcpyDeviceToHost, s));
     DAGC_CUDA(ctx, cudaStreamSynchronize(s));
     const uint32_t e32 = (uint32_t)(ctx->h_stage[0] & 0xFFFFFFFFu);
     const uint64_t* counts = ctx->h_stage + 1;
@@ -1045,15 +1180,30 @@ int dagc_context_create(int device, dagc_context* out) {
     kernels_configure();
     e = cudaMallocHost(&c->h_stage, 4096);
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+    if (cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        c->capture_stream = nullptr;  // graphs off; calls launch directly
+    }
+    if (const char* g = std::getenv("DAGC_GRAPHS")) c->use_graphs = std::atoi(g) != 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumSortShapes; ++sh) {
         c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
         c->occ_pairs[sh] = std::max(1, occupancy_sort_shape(sh, true));
     }
+    // Resident-CTA caps for the persistent grids (tuning experiments).
+    if (const char* e = std::getenv("DAGC_PASS_CTAS_PER_SM")) {
+        const int cap = std::max(1, std::atoi(e));
+        for (int sh = 0; sh < kNumSortShapes; ++sh) {
+            c->occ_keys[sh] = std::min(c->occ_keys[sh], cap);
+            c->occ_pairs[sh] = std::min(c->occ_pairs[sh], cap);
+        }
+    }
     if (const char* e = std::getenv("DAGC_SORT_SHAPE_KEYS")) c->shape_keys = std::atoi(e) % kNumSortShapes;
     if (const char* e = std::getenv("DAGC_SORT_SHAPE_PAIRS")) c->shape_pairs = std::atoi(e) % kNumSortShapes;
     c->grid_hist = 8 * c->sms;
     c->grid_leaf = std::max(1, occupancy_kernel(0)) * c->sms;
+    if (const char* e = std::getenv("DAGC_SCAN_CTAS_PER_SM"))
+        c->grid_leaf = std::min(c->grid_leaf, std::max(1, std::atoi(e)) * c->sms);
     c->grid_extract = std::max(1, occupancy_kernel(1)) * c->sms;
     c->grid_unique = std::max(1, occupancy_kernel(2)) * c->sms;
     c->grid_scan = std::max(1, occupancy_kernel(3)) * c->sms;
@@ -1068,6 +1218,8 @@ void dagc_context_destroy(dagc_context ctx) {
     cudaDeviceSynchronize();
     settle_profile(ctx);
     for (cudaEvent_t e : ctx->free_events) cudaEventDestroy(e);
+    drop_graphs(ctx);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     ctx->arena.release();
     ctx->pool.trim();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -1093,6 +1245,42 @@ int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int d
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     CreatePools p;
     int st = create_pipeline(ctx, d_fragments, n, depth, s, p);
+    if (st) return st;
+    return materialise(ctx, p, nl, s, out);
+}
+
+int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uint64_t* h_chunk_offsets,
+                        const uint64_t* h_chunk_morton, uint64_t k, int chunk_depth, int top_levels, void* stream,
+                        dagc_dag* out) {
+    if (!valid_ctx(ctx) || !out || !h_chunk_offsets || (k && !h_chunk_morton)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    const int depth = chunk_depth + top_levels;
+    if (chunk_depth < 2 || top_levels < 0 || depth > kMaxDepth)
+        return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "need chunk_depth >= 2 and chunk_depth + top_levels <= 21");
+    if (k == 0 || k > (1ull << (3 * top_levels)) || k > (1u << 20))
+        return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "chunk count must be in [1, 8^top_levels]");
+    if (h_chunk_offsets[0] != 0) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "chunk offsets must start at 0");
+    for (uint64_t i = 0; i < k; ++i) {
+        if (h_chunk_offsets[i + 1] < h_chunk_offsets[i])
+            return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "chunk offsets must not decrease");
+        if (h_chunk_morton[i] >> (3 * top_levels) || (i && h_chunk_morton[i] <= h_chunk_morton[i - 1]))
+            return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "chunk Morton indices must ascend inside the grid");
+    }
+    const uint64_t n = h_chunk_offsets[k];
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+    if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
+    if (3 * chunk_depth + bits_for(k) > 64) return set_error(ctx, DAGC_ERR_TOO_LARGE, "composite key exceeds 64 bits");
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int nl = depth - 2;
+    if (n == 0) {
+        ctx->last_counts.assign(3 + nl, 0);
+        return empty_dag(ctx, nl, out);
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const BatchSpec batch{h_chunk_offsets, h_chunk_morton, (uint32_t)k, chunk_depth};
+    CreatePools p;
+    int st = create_pipeline(ctx, d_fragments, n, depth, s, p, &batch);
     if (st) return st;
     return materialise(ctx, p, nl, s, out);
 }
@@ -1259,6 +1447,7 @@ int dagc_free_all(dagc_context ctx) {
     std::lock_guard<std::mutex> lock(ctx->mu);
     DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
     DAGC_CUDA(ctx, cudaDeviceSynchronize());
+    drop_graphs(ctx);
     ctx->arena.release();
     ctx->pool.trim();
     return DAGC_OK;
@@ -1320,6 +1509,10 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
         case DAGC_OPT_SORT_SHAPE_PAIRS:
             if (value < 0 || value >= kNumSortShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
             ctx->shape_pairs = value;
+            return DAGC_OK;
+        case DAGC_OPT_GRAPHS:
+            ctx->use_graphs = value != 0;
+            if (!ctx->use_graphs) drop_graphs(ctx);
             return DAGC_OK;
         default:
             return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "unknown option");

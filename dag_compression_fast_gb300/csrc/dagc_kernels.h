@@ -55,6 +55,14 @@ struct SortArgs {
     uint32_t* err;
     int grid_hist, grid_pass; // persistent grid sizes
     int shape;                // digit-pass kernel shape, see sort_shape_*
+    // Segmented input (batched chunks): when seg_offsets is non-null, the key at
+    // position i of keys_in belongs to segment s with seg_offsets[s] <= i <
+    // seg_offsets[s+1] (seg_count + 1 ascending entries) and is sorted as the
+    // composite (s << seg_shift) | key. Only the histogram and the first pass
+    // read keys_in; they build the composite, later passes move it.
+    const uint64_t* seg_offsets;
+    uint32_t seg_count;
+    int seg_shift;
 };
 
 // Digit-pass kernel shapes (items per thread x minimum resident CTAs per SM,
@@ -89,10 +97,14 @@ DAGC_HD uint32_t scan_tiles(uint64_t n) { return (uint32_t)((n + kScanTile - 1) 
 // parent; *d_out_n = number of parents.
 struct LeafBuildArgs {
     const uint64_t* sorted; const uint64_t* d_n; uint64_t n_bound;
+    // Batched input: sorted keys are (segment << seg_shift) | local code; the
+    // global code is (seg_code[segment] << seg_shift) | local code.
+    const uint64_t* seg_code; int seg_shift;
     uint64_t* parents; uint64_t* leaves; uint64_t out_capacity; uint64_t* d_out_n;
+    uint64_t* lead_or; uint64_t* lead_run;  // per tile: OR of keys continuing an earlier run, its run id
     uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
 };
-void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s);
+void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s);  // two launches (build + fix-up)
 
 // Unique over (key, perm) sorted by key: uid = rank of the key among distinct
 // keys; map[perm[i]] = uid; for the first of each run, out_keys[uid] = key and

@@ -34,10 +34,25 @@ __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
     return d_n ? *d_n : n;
 }
 
+// Segment of position i (seg_offsets ascending, count + 1 entries): binary
+// search for the first position of a block, then `segment_from` walks forward.
+__device__ __forceinline__ uint32_t segment_search(const uint64_t* off, uint32_t count, uint64_t i) {
+    uint32_t lo = 0, hi = count;  // invariant: off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t segment_from(const uint64_t* off, uint32_t count, uint64_t i, uint32_t hint) {
+    while (hint + 1 < count && __ldg(off + hint + 1) <= i) ++hint;
+    return hint;
+}
+
 __global__ void __launch_bounds__(kSortThreads)
 radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t n_host, int lo_bit,
                 int hi_bit, int validate_bits, uint32_t* __restrict__ hist, uint32_t* status0,
-                uint32_t* err) {
+                uint32_t* err, const uint64_t* seg_offsets, uint32_t seg_count, int seg_shift) {
     __shared__ uint32_t s_hist[kMaxPasses][kRadix];
     const uint64_t n = load_n(d_n, n_host);
     const int passes = sort_passes(lo_bit, hi_bit);
@@ -49,15 +64,29 @@ radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t
     for (uint64_t i = gtid; i < status_words; i += gstride) status0[i] = 0;
     __syncthreads();
 
+    // Four independent loads in flight per thread (grid-stride, unrolled).
     uint64_t bad = 0;
-    for (uint64_t i = gtid; i < n; i += gstride) {
-        const uint64_t k = __ldg(keys + i);
-        if (validate_bits > 0 && validate_bits < 64) bad |= k >> validate_bits;
-        for (int p = 0; p < passes; ++p) {
-            const int shift = lo_bit + p * kRadixBits;
-            const int bits = min(kRadixBits, hi_bit - shift);
-            const uint32_t d = (uint32_t)(k >> shift) & ((1u << bits) - 1u);
-            atomicAdd(&s_hist[p][d], 1u);
+    for (uint64_t i0 = gtid; i0 < n; i0 += 4 * gstride) {
+        uint64_t k[4];
+        bool in[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint64_t i = i0 + u * gstride;
+            in[u] = i < n;
+            k[u] = in[u] ? __ldg(keys + i) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!in[u]) continue;
+            if (validate_bits > 0 && validate_bits < 64) bad |= k[u] >> validate_bits;
+            if (seg_offsets)
+                k[u] |= (uint64_t)segment_search(seg_offsets, seg_count, i0 + u * gstride) << seg_shift;
+            for (int p = 0; p < passes; ++p) {
+                const int shift = lo_bit + p * kRadixBits;
+                const int bits = min(kRadixBits, hi_bit - shift);
+                const uint32_t d = (uint32_t)(k[u] >> shift) & ((1u << bits) - 1u);
+                atomicAdd(&s_hist[p][d], 1u);
+            }
         }
     }
     if (__any_sync(0xFFFFFFFFu, bad != 0) && (threadIdx.x & 31) == 0) atomicOr(err, kErrBadInput);
@@ -81,14 +110,19 @@ struct PassParams {
     uint32_t* tile_counter;
     uint32_t* err;
     int shift, bits;
+    const uint64_t* seg_offsets;  // first pass of a segmented sort only
+    uint32_t seg_count;
+    int seg_shift;
 };
 
 // Exclusive prefix of one digit over the tiles before `tile`: walks back over
-// their published counts 8 tiles per round trip, stopping at the first
+// their published counts 16 tiles per round trip, stopping at the first
 // inclusive prefix; waits (bounded) on tiles that have published nothing yet.
+// (When every tile of a small sort runs at once, inclusive prefixes spread
+// about one window per round trip, so the window width sets the latency.)
 __device__ __forceinline__ uint32_t lookback_digit(const uint32_t* status, uint32_t tile, uint32_t d,
                                                    uint32_t* err) {
-    constexpr int kLB = 8;
+    constexpr int kLB = 16;
     uint32_t excl = 0, iter = 0;
     int64_t t = (int64_t)tile - 1;
     while (true) {
@@ -195,6 +229,17 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
         for (int j = 0; j < kItems; ++j) {
             const uint32_t i = wofs + j * 32 + lane;
             if (i < tile_n) k[j] = p.keys_in[base + i];
+        }
+        if (p.seg_offsets) {  // first pass of a segmented sort: build composite keys
+            uint32_t sg = segment_search(p.seg_offsets, p.seg_count, base + wofs + lane);
+#pragma unroll
+            for (int j = 0; j < kItems; ++j) {
+                const uint32_t i = wofs + j * 32 + lane;
+                if (i < tile_n) {
+                    sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
+                    k[j] |= (uint64_t)sg << p.seg_shift;
+                }
+            }
         }
         // Ranks within the warp fit 16 bits: two per register.
         uint32_t rank2[kItems / 2];
@@ -364,6 +409,9 @@ static PassParams pass_params(const SortArgs& a, int i) {
     p.err = a.err;
     p.shift = a.lo_bit + i * kRadixBits;
     p.bits = a.hi_bit - p.shift < kRadixBits ? a.hi_bit - p.shift : kRadixBits;
+    p.seg_offsets = i == 0 ? a.seg_offsets : nullptr;
+    p.seg_count = a.seg_count;
+    p.seg_shift = a.seg_shift;
     return p;
 }
 
@@ -371,7 +419,8 @@ void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
     // The histogram pass also validates the key range, so it runs even when
     // there is no digit to sort.
     radix_histogram<<<a.grid_hist, kSortThreads, 0, s>>>(a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
-                                                         a.validate_bits, a.hist, a.status[0], a.err);
+                                                         a.validate_bits, a.hist, a.status[0], a.err,
+                                                         a.seg_offsets, a.seg_count, a.seg_shift);
     if (sort_passes(a.lo_bit, a.hi_bit) == 0)
         copy_keys<<<a.grid_hist, 256, 0, s>>>(a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
                                               a.d_n, a.n);

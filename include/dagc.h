@@ -55,6 +55,23 @@ int dagc_version(void);
 int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth,
                 void* stream, dagc_dag* out);
 
+/* --------------------------------------------------- batched CreateDAG ---- */
+/* Many subvolume chunks in one call: the batched form of the reference's
+ * per-chunk CreateDAG loop followed by MergeDAGs (src/DAG_Compression_Fast.cpp
+ * :283-320). The volume is a grid of 2^top_levels chunks per side, each chunk
+ * 2^chunk_depth voxels per side; k of its chunks are given (the others are
+ * empty), in ascending Morton order of their chunk coordinates
+ * h_chunk_morton[i] < 8^top_levels. d_fragments holds every chunk's
+ * chunk-local codes (< 2^(3*chunk_depth)) back to back, chunk i at
+ * [h_chunk_offsets[i], h_chunk_offsets[i+1]). The result, a DAG of depth
+ * chunk_depth + top_levels, is bit-exact with dagc_merge over 8^top_levels
+ * dagc_create results (one per chunk slot, empty slots included). All chunks
+ * go through one segmented sort and one level loop; the per-level dedup over
+ * all chunks is the merge. Synchronous on return. */
+int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments,
+                        const uint64_t* h_chunk_offsets, const uint64_t* h_chunk_morton,
+                        uint64_t k, int chunk_depth, int top_levels, void* stream, dagc_dag* out);
+
 /* -------------------------------------------------------- DAG accessors ---- */
 int dagc_dag_num_levels(dagc_dag dag, int* num_levels);
 int dagc_dag_level_size(dagc_dag dag, int level, uint64_t* num_nodes);
@@ -130,6 +147,10 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * 5 = (16, 3, alternate), 6 = (16, 2, alternate), 7 = (12, 3, alternate). */
 #define DAGC_OPT_SORT_SHAPE_KEYS 1   /* keys-only sorts (the fragment sort) */
 #define DAGC_OPT_SORT_SHAPE_PAIRS 2  /* key/value sorts (leaf and node hashes) */
+/* 1 (default): record each CreateDAG kernel sequence once as a CUDA graph and
+ * replay it for later calls with the same input pointer, size and depth;
+ * 0: launch every kernel directly. Profiling always launches directly. */
+#define DAGC_OPT_GRAPHS 3
 int dagc_set_option(dagc_context ctx, int option, int value);
 
 /* ---------------------------------------------------- instrumentation ---- */

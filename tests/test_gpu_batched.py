@@ -1,0 +1,73 @@
+"""GPU tests of the batched form: many chunks in one call must equal the
+per-chunk CreateDAG + MergeDAGs of the same chunks, bit for bit, and the
+oracle's CreateDAG of the whole volume."""
+import numpy as np
+import pytest
+
+import dag_compression_fast_gb300 as D
+from oracle import oracle as O
+from tests.inputs import random_codes
+from tests.test_gpu_parity import assert_dag_equal
+
+pytestmark = pytest.mark.gpu
+
+
+
+
+def global_codes(local_chunks, morton, chunk_depth):
+    parts = [(np.uint64(m) << np.uint64(3 * chunk_depth)) | c for c, m in zip(local_chunks, morton) if c.size]
+    return np.concatenate(parts) if parts else np.zeros(0, np.uint64)
+
+
+def per_chunk_merge(ctx, local_chunks, morton, chunk_depth, top_levels):
+    slots = 8 ** top_levels
+    by_slot = {int(m): c for c, m in zip(local_chunks, morton)}
+    dags = [ctx.create_dag(by_slot.get(i, np.zeros(0, np.uint64)), chunk_depth) for i in range(slots)]
+    return ctx.merge_dags(dags)
+
+
+def make_chunks(chunk_depth, top_levels, k, seed):
+    rng = np.random.default_rng(seed)
+    morton = np.sort(rng.choice(8 ** top_levels, size=k, replace=False)).astype(np.uint64)
+    chunks = []
+    for i in range(k):
+        n = int(rng.integers(0, 6000)) if i % 5 else 0  # some chunks empty, sizes uneven
+        chunks.append(random_codes(chunk_depth, n, seed * 100 + i, cluster=bool(i % 2)))
+    return chunks, morton
+
+
+@pytest.mark.parametrize("chunk_depth,top_levels,k,seed", [(5, 2, 20, 1), (6, 1, 8, 2), (4, 3, 100, 3), (7, 1, 1, 4)])
+def test_batched_equals_per_chunk_merge_and_whole_volume(ctx, chunk_depth, top_levels, k, seed):
+    chunks, morton = make_chunks(chunk_depth, top_levels, k, seed)
+    counts = np.array([c.size for c in chunks], np.uint64)
+    frag = np.concatenate(chunks) if counts.sum() else np.zeros(0, np.uint64)
+    batched = ctx.create_dag_batched(frag, counts, morton, chunk_depth, top_levels).to_host()
+    merged = per_chunk_merge(ctx, chunks, morton, chunk_depth, top_levels).to_host()
+    whole = O.create_dag(global_codes(chunks, morton, chunk_depth), chunk_depth + top_levels)
+    assert_dag_equal(batched, whole)
+    assert_dag_equal(merged, whole)
+
+
+def test_batched_generator_terrain_chunks(ctx):
+    """A reduced config-4 layout: 4x4 terrain chunks of 256^3 with sponges."""
+    codes, counts, morton = D.gen_batched(chunk_depth=8, grid_xz=4, chunk_row=1, seed=11,
+                                          min_fragments=1e3, max_fragments=3e5, threads=8)
+    chunks = np.split(codes, np.cumsum(counts)[:-1].astype(np.int64))
+    batched = ctx.create_dag_batched(codes, counts, morton, 8, 2)
+    whole = O.create_dag(global_codes(chunks, morton, 8), 10, threads=8)
+    assert_dag_equal(batched.to_host(), whole)
+    words = ctx.create_final_dag(batched).to_numpy()
+    assert np.array_equal(words, O.final_dag(whole))
+
+
+def test_batched_rejects_out_of_range_local_code(ctx):
+    chunks = [np.array([1, 2, 3], np.uint64), np.array([1 << 15], np.uint64)]  # 2^15 >= 8^5
+    with pytest.raises(D.DagcError) as e:
+        ctx.create_dag_batched(np.concatenate(chunks), [3, 1], [0, 5], 5, 1)
+    assert e.value.status == D.ERR_BAD_INPUT
+
+
+def test_batched_rejects_unordered_chunks(ctx):
+    with pytest.raises(D.DagcError) as e:
+        ctx.create_dag_batched(np.array([1, 2], np.uint64), [1, 1], [5, 3], 5, 1)
+    assert e.value.status == D.ERR_INVALID_ARGUMENT

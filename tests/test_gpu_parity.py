@@ -124,6 +124,26 @@ def test_compress_host_and_fused(ctx):
     assert np.array_equal(ctx.compress(codes, depth).to_numpy(), ref_words)
 
 
+def test_graph_replay_matches_direct_launches(ctx):
+    """Repeated calls on one device buffer replay a recorded CUDA graph; the
+    result must equal the directly launched pipeline and the oracle."""
+    import torch
+    codes = random_codes(10, 400_000, 21, cluster=True)
+    t = torch.from_numpy(codes.view(np.int64)).cuda()
+    ref = O.create_dag(codes, 10)
+    for _ in range(3):  # first call records, the next two replay
+        assert_dag_equal(ctx.create_dag(t, 10).to_host(), ref)
+    ctx.set_option(D.OPT_GRAPHS, 0)
+    try:
+        assert_dag_equal(ctx.create_dag(t, 10).to_host(), ref)
+    finally:
+        ctx.set_option(D.OPT_GRAPHS, 1)
+    # A different input in the same buffer: the replay must see the new data.
+    codes2 = random_codes(10, 400_000, 22, cluster=True)
+    t.copy_(torch.from_numpy(codes2.view(np.int64)))
+    assert_dag_equal(ctx.create_dag(t, 10).to_host(), O.create_dag(codes2, 10))
+
+
 def test_input_left_unchanged(ctx):
     import torch
     codes = random_codes(8, 100_000, 12)
