@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -45,12 +46,14 @@ DAGC_SYMBOLS = [
     "dagc_context_create", "dagc_context_destroy", "dagc_last_error", "dagc_status_string",
     "dagc_version", "dagc_create", "dagc_create_batched", "dagc_dag_num_levels", "dagc_dag_level_size",
     "dagc_dag_num_leaves", "dagc_dag_level_device", "dagc_dag_leaves_device",
-    "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_free",
+    "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_copy",
+    "dagc_dag_free", "dagc_create_footprint",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
     "dagc_compress", "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
-    "dagc_sort_keys_noalloc",
+    "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
+    "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
@@ -103,6 +106,16 @@ def lib() -> ctypes.CDLL:
         L.dagc_dag_download_level.argtypes = [vp, i32, vp, vp, vp]
         L.dagc_dag_download_leaves.argtypes = [vp, vp]
         L.dagc_dag_upload.argtypes = [vp, i32, vp, vp, vp, vp, vp, u64, vp, pvp]
+        L.dagc_dag_copy.argtypes = [vp, vp, vp, pvp]
+        L.dagc_create_footprint.argtypes = [u64, i32]
+        L.dagc_create_footprint.restype = u64
+        L.dagc_server_create.argtypes = [i32, i32, u64, pvp]
+        L.dagc_server_submit.argtypes = [vp, vp, u64, i32, ctypes.c_int64, pu64]
+        L.dagc_server_wait.argtypes = [vp, u64, vp, u64, pu64, ctypes.POINTER(ctypes.c_double)]
+        L.dagc_server_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
+        L.dagc_server_shared_dag.argtypes = [vp, i32, pvp, pvp]
+        L.dagc_server_destroy.argtypes = [vp]
+        L.dagc_server_destroy.restype = None
         L.dagc_dag_free.argtypes = [vp]
         L.dagc_dag_free.restype = None
         L.dagc_merge.argtypes = [vp, vp, u64, vp, pvp]
@@ -179,6 +192,9 @@ class Dag:
     def __init__(self, ctx: "Context", handle: int):
         self.ctx = ctx
         self.handle = handle
+        live = getattr(ctx, "_live", None)
+        if live is not None:
+            live.add(self)
 
     def _live(self):
         if not self.handle:
@@ -239,6 +255,7 @@ class Words:
         self.ctx = ctx
         self.ptr = ptr
         self.n = n
+        ctx._live.add(self)
 
     def to_numpy(self) -> np.ndarray:
         out = np.zeros(self.n, np.uint32)
@@ -284,9 +301,12 @@ class Context:
         if st:
             raise DagcError(st, "dagc_context_create failed")
         self.handle = h.value
+        self._live = weakref.WeakSet()  # DAGs and word arrays to release before the context
 
     def close(self):
         if getattr(self, "handle", None):
+            for obj in list(self._live):
+                obj.free()
             lib().dagc_context_destroy(self.handle)
             self.handle = None
 
@@ -442,6 +462,92 @@ class Context:
         self._check(lib().dagc_sort_pairs(self.handle, ptr, kout.data_ptr(), vin, vout.data_ptr(), n, lo_bit, hi_bit,
                                           _stream_handle(stream)))
         return kout, vout
+
+
+class _BorrowedContext:
+    """A context owned by the library (the server's merge context)."""
+
+    def __init__(self, handle, device):
+        self.handle = handle
+        self.device = device
+
+    def _check(self, st: int):
+        if st:
+            raise DagcError(st, lib().dagc_last_error(self.handle).decode(errors="replace"))
+
+
+class Server:
+    """The serving loop (dagc_server_*): jobs admitted by device-memory
+    footprint into `slots` concurrent worker slots."""
+
+    def __init__(self, device: int = 0, slots: int = 4, hbm_budget_bytes: int = 64 << 30):
+        h = ctypes.c_void_p()
+        st = lib().dagc_server_create(device, slots, hbm_budget_bytes, ctypes.byref(h))
+        if st:
+            raise DagcError(st, "dagc_server_create failed")
+        self.handle = h.value
+        self.device = device
+        self._inputs = {}
+        self._shared = []  # DAGs on the server's merge context: freed before it
+
+    def submit(self, fragments: np.ndarray, depth: int, chunk_morton: int = -1) -> int:
+        a = np.ascontiguousarray(fragments, dtype=np.uint64)
+        t = ctypes.c_uint64(0)
+        st = lib().dagc_server_submit(self.handle, _np_ptr(a), a.size, depth, chunk_morton, ctypes.byref(t))
+        if st:
+            raise DagcError(st, "dagc_server_submit failed")
+        self._inputs[t.value] = a  # keep alive until the job is collected
+        return t.value
+
+    def wait(self, ticket: int):
+        """(words, latency_ms) of a finished job."""
+        n = ctypes.c_uint64(0)
+        lat = ctypes.c_double(0)
+        st = lib().dagc_server_wait(self.handle, ticket, None, 0, ctypes.byref(n), ctypes.byref(lat))
+        if st:
+            self._inputs.pop(ticket, None)
+            raise DagcError(st, "job failed")
+        out = np.zeros(n.value, np.uint32)
+        st = lib().dagc_server_wait(self.handle, ticket, _np_ptr(out), out.size, ctypes.byref(n), ctypes.byref(lat))
+        self._inputs.pop(ticket, None)
+        if st:
+            raise DagcError(st, "job failed")
+        return out, lat.value
+
+    def stats(self):
+        c, f, m, p = (ctypes.c_uint64(0) for _ in range(4))
+        lib().dagc_server_stats(self.handle, ctypes.byref(c), ctypes.byref(f), ctypes.byref(m), ctypes.byref(p))
+        return {"completed": c.value, "fragments": f.value, "max_concurrent": m.value, "peak_footprint": p.value}
+
+    def shared_dag(self, top_levels: int) -> Dag:
+        """Merges every chunk job so far into one device DAG."""
+        ctx = ctypes.c_void_p()
+        out = ctypes.c_void_p()
+        st = lib().dagc_server_shared_dag(self.handle, top_levels, ctypes.byref(ctx), ctypes.byref(out))
+        if st:
+            raise DagcError(st, "dagc_server_shared_dag failed")
+        d = Dag(_BorrowedContext(ctx.value, self.device), out.value)
+        self._shared.append(d)
+        return d
+
+    def close(self):
+        if getattr(self, "handle", None):
+            for d in self._shared:
+                d.free()
+            self._shared = []
+            lib().dagc_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_footprint(n: int, depth: int) -> int:
+    """Device scratch bytes of one CreateDAG call (dagc_create_footprint)."""
+    return int(lib().dagc_create_footprint(n, depth))
 
 
 # ---------------------------------------------------------------- inputs ----

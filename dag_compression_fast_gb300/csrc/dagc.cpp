@@ -529,50 +529,67 @@ int bits_for(uint64_t values) {  // bits to tell `values` values apart
     return b;
 }
 
+// Scratch layout of one CreateDAG call (also used to report its footprint).
+struct CreateLayout {
+    std::vector<uint64_t> cap;  // node bound per level
+    uint64_t capmax = 1, p0cap = 0, sv_total = 0;
+    size_t zero_bytes = 0, total = 0;
+    size_t o_hdr, o_sv, o_ss0, o_ss1, o_A, o_B, o_P, o_LM, o_SK, o_SKa, o_V, o_Va, o_M0, o_M1;
+    size_t o_NC0, o_NC1, o_NM, o_NCH, o_NH, o_PL, o_lead_or, o_lead_run, o_seg_off, o_seg_code;
+    std::vector<size_t> o_ph, o_pc, o_pm;
+    CreateLayout(uint64_t n, int depth, uint32_t k_batch) {
+        const int nl = depth - 2;
+        cap.resize(nl);
+        for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
+        p0cap = level_cap(depth - 2, n);
+        sv_total = sv_words(n) + sv_words(p0cap);
+        for (int l = nl - 1; l >= 0; --l) sv_total += sv_words(l == nl - 1 ? p0cap : cap[l + 1]) + sv_words(cap[l]);
+        Layout L;
+        o_hdr = L.take<CallHeader>(1);
+        o_sv = L.take<uint64_t>(sv_total);
+        zero_bytes = L.off;
+        o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+        o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+        o_A = L.take<uint64_t>(n);
+        o_B = L.take<uint64_t>(n);
+        o_P = L.take<uint64_t>(p0cap);
+        o_LM = L.take<uint64_t>(p0cap);
+        o_SK = L.take<uint64_t>(p0cap);
+        o_SKa = L.take<uint64_t>(p0cap);
+        o_V = L.take<uint32_t>(p0cap);
+        o_Va = L.take<uint32_t>(p0cap);
+        o_M0 = L.take<uint32_t>(p0cap);
+        o_M1 = L.take<uint32_t>(p0cap);
+        o_NC0 = L.take<uint64_t>(capmax);
+        o_NC1 = L.take<uint64_t>(capmax);
+        o_NM = L.take<uint8_t>(capmax);
+        o_NCH = L.take<uint32_t>(std::max<uint64_t>(capmax, kTailCap) * 8);
+        o_NH = L.take<uint64_t>(capmax);
+        o_PL = L.take<uint64_t>(p0cap);
+        o_ph.resize(nl); o_pc.resize(nl); o_pm.resize(nl);
+        for (int l = 0; l < nl; ++l) {
+            o_ph[l] = L.take<uint64_t>(cap[l]);
+            o_pc[l] = L.take<uint32_t>(cap[l] * 8);
+            o_pm[l] = L.take<uint8_t>(cap[l]);
+        }
+        o_lead_or = L.take<uint64_t>(scan_tiles(n) + 1);
+        o_lead_run = L.take<uint64_t>(scan_tiles(n) + 1);
+        o_seg_off = L.take<uint64_t>(k_batch ? k_batch + 1 : 0);
+        o_seg_code = L.take<uint64_t>(k_batch);
+        total = L.off;
+    }
+};
+
 int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
                     CreatePools& out, const BatchSpec* batch = nullptr) {
     const int nl = depth - 2;
     const int bits = 3 * depth;
-    std::vector<uint64_t> cap(nl);
-    uint64_t capmax = 1;
-    for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
-    const uint64_t p0cap = level_cap(depth - 2, n);
-    uint64_t sv_total = sv_words(n) + sv_words(p0cap);
-    for (int l = nl - 1; l >= 0; --l) sv_total += sv_words(l == nl - 1 ? p0cap : cap[l + 1]) + sv_words(cap[l]);
-
-    Layout L;
-    const size_t o_hdr = L.take<CallHeader>(1);
-    const size_t o_sv = L.take<uint64_t>(sv_total);
-    const size_t zero_bytes = L.off;
-    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
-    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
-    const size_t o_A = L.take<uint64_t>(n);
-    const size_t o_B = L.take<uint64_t>(n);
-    const size_t o_P = L.take<uint64_t>(p0cap);
-    const size_t o_LM = L.take<uint64_t>(p0cap);
-    const size_t o_SK = L.take<uint64_t>(p0cap);
-    const size_t o_SKa = L.take<uint64_t>(p0cap);
-    const size_t o_V = L.take<uint32_t>(p0cap);
-    const size_t o_Va = L.take<uint32_t>(p0cap);
-    const size_t o_M0 = L.take<uint32_t>(p0cap);
-    const size_t o_M1 = L.take<uint32_t>(p0cap);
-    const size_t o_NC0 = L.take<uint64_t>(capmax);
-    const size_t o_NC1 = L.take<uint64_t>(capmax);
-    const size_t o_NM = L.take<uint8_t>(capmax);
-    const size_t o_NCH = L.take<uint32_t>(std::max<uint64_t>(capmax, kTailCap) * 8);
-    const size_t o_NH = L.take<uint64_t>(capmax);
-    const size_t o_PL = L.take<uint64_t>(p0cap);
-    std::vector<size_t> o_ph(nl), o_pc(nl), o_pm(nl);
-    for (int l = 0; l < nl; ++l) {
-        o_ph[l] = L.take<uint64_t>(cap[l]);
-        o_pc[l] = L.take<uint32_t>(cap[l] * 8);
-        o_pm[l] = L.take<uint8_t>(cap[l]);
-    }
-    const size_t o_lead_or = L.take<uint64_t>(scan_tiles(n) + 1);
-    const size_t o_lead_run = L.take<uint64_t>(scan_tiles(n) + 1);
-    const size_t o_seg_off = L.take<uint64_t>(batch ? batch->k + 1 : 0);
-    const size_t o_seg_code = L.take<uint64_t>(batch ? batch->k : 0);
-    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    const CreateLayout Lo(n, depth, batch ? batch->k : 0u);
+    const std::vector<uint64_t>& cap = Lo.cap;
+    const uint64_t capmax = Lo.capmax, p0cap = Lo.p0cap, sv_total = Lo.sv_total;
+    const size_t zero_bytes = Lo.zero_bytes;
+    (void)capmax;
+    DAGC_CUDA(ctx, ctx->arena.reserve(Lo.total));
     char* b = static_cast<char*>(ctx->arena.base);
     auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
     auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
@@ -585,26 +602,26 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         seg_shift = 3 * batch->chunk_depth;
         sort_hi = std::max(6, seg_shift + bits_for(batch->k));
         validate = seg_shift;
-        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_seg_off), batch->h_offsets, (batch->k + 1) * 8,
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(Lo.o_seg_off), batch->h_offsets, (batch->k + 1) * 8,
                                        cudaMemcpyHostToDevice, s));
-        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(o_seg_code), batch->h_morton, batch->k * 8, cudaMemcpyHostToDevice, s));
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P64(Lo.o_seg_code), batch->h_morton, batch->k * 8, cudaMemcpyHostToDevice, s));
     }
 
     // Everything from here to the last kernel is enqueued by one function, so
     // that it can be recorded once as a CUDA graph and replayed.
     auto enqueue = [&](cudaStream_t s) -> int {
         CallSlots cs;
-        cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
-        cs.sv_next = P64(o_sv);
-        cs.sv_end = P64(o_sv) + sv_total;
-        SortBuffers sb{{P32(o_ss0), P32(o_ss1)}};
+        cs.h = reinterpret_cast<CallHeader*>(b + Lo.o_hdr);
+        cs.sv_next = P64(Lo.o_sv);
+        cs.sv_end = P64(Lo.o_sv) + sv_total;
+        SortBuffers sb{{P32(Lo.o_ss0), P32(Lo.o_ss1)}};
         DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
         uint32_t* err = &cs.h->err;
 
         // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
         //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
-        const SegmentSpec seg{batch ? P64(o_seg_off) : nullptr, batch ? batch->k : 0u, seg_shift};
-        int st = run_sort(ctx, cs, sb, d_frag, P64(o_A), P64(o_B), nullptr, nullptr, nullptr, false, n, nullptr,
+        const SegmentSpec seg{batch ? P64(Lo.o_seg_off) : nullptr, batch ? batch->k : 0u, seg_shift};
+        int st = run_sort(ctx, cs, sb, d_frag, P64(Lo.o_A), P64(Lo.o_B), nullptr, nullptr, nullptr, false, n, nullptr,
                           6, sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg);
         if (st) return st;
 
@@ -612,15 +629,15 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         {
             StageTimer t(ctx, DAGC_STAGE_LEAF_BUILD, s);
             LeafBuildArgs a{};
-            a.sorted = P64(o_A);
+            a.sorted = P64(Lo.o_A);
             a.d_n = nullptr;
             a.n_bound = n;
-            a.parents = P64(o_P);
-            a.leaves = P64(o_LM);
+            a.parents = P64(Lo.o_P);
+            a.leaves = P64(Lo.o_LM);
             a.out_capacity = p0cap;
-            a.lead_or = P64(o_lead_or);
-            a.lead_run = P64(o_lead_run);
-            a.seg_code = batch ? P64(o_seg_code) : nullptr;
+            a.lead_or = P64(Lo.o_lead_or);
+            a.lead_run = P64(Lo.o_lead_run);
+            a.seg_code = batch ? P64(Lo.o_seg_code) : nullptr;
             a.seg_shift = seg_shift;
             a.d_out_n = cs.count(kCntBricks);
             a.status = cs.sv(n);
@@ -634,17 +651,17 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         }
         // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
         StageTimer t_dedup(ctx, DAGC_STAGE_LEAF_DEDUP, s);
-        st = run_sort(ctx, cs, sb, P64(o_LM), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true, p0cap,
+        st = run_sort(ctx, cs, sb, P64(Lo.o_LM), P64(Lo.o_SK), P64(Lo.o_SKa), nullptr, P32(Lo.o_V), P32(Lo.o_Va), true, p0cap,
                       cs.count(kCntBricks), 0, 64, 0, s);
         if (st) return st;
         {
             UniqueArgs a{};
-            a.keys = P64(o_SK);
-            a.perm = P32(o_V);
+            a.keys = P64(Lo.o_SK);
+            a.perm = P32(Lo.o_V);
             a.d_n = cs.count(kCntBricks);
             a.n_bound = p0cap;
-            a.map = P32(o_M0);
-            a.out_keys = P64(o_PL);
+            a.map = P32(Lo.o_M0);
+            a.out_keys = P64(Lo.o_PL);
             a.out_capacity = p0cap;
             a.d_out_n = cs.count(kCntLeaves);
             a.status = cs.sv(p0cap);
@@ -658,13 +675,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         t_dedup.stop();
         // 4. Level loop, bottom-up.
         StageTimer t_levels(ctx, DAGC_STAGE_LEVELS, s);
-        const uint64_t* child_codes = P64(o_P);
-        const uint32_t* child_map = P32(o_M0);
-        const uint64_t* child_hashes = P64(o_PL);
+        const uint64_t* child_codes = P64(Lo.o_P);
+        const uint32_t* child_map = P32(Lo.o_M0);
+        const uint64_t* child_hashes = P64(Lo.o_PL);
         const uint64_t* d_child_n = cs.count(kCntBricks);
         uint64_t child_bound = p0cap;
-        uint64_t* node_codes[2] = {P64(o_NC0), P64(o_NC1)};
-        uint32_t* maps[2] = {P32(o_M1), P32(o_M0)};
+        uint64_t* node_codes[2] = {P64(Lo.o_NC0), P64(Lo.o_NC1)};
+        uint32_t* maps[2] = {P32(Lo.o_M1), P32(Lo.o_M0)};
         // Levels whose node bound fits one CTA's shared memory go to the tail
         // kernel; the bound only grows with the level index, so they are the top
         // tail_first + 1 levels.
@@ -679,9 +696,9 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             e.n_bound = child_bound;
             e.child_hashes = child_hashes;
             e.node_codes = node_codes[it & 1];
-            e.node_masks = P8(o_NM);
-            e.node_children = P32(o_NCH);
-            e.node_hashes = P64(o_NH);
+            e.node_masks = P8(Lo.o_NM);
+            e.node_children = P32(Lo.o_NCH);
+            e.node_hashes = P64(Lo.o_NH);
             e.out_capacity = cap[l];
             e.d_out_n = cs.count(kCntNodes + l);
             e.status = cs.sv(child_bound);
@@ -692,21 +709,21 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
 
-            st = run_sort(ctx, cs, sb, P64(o_NH), P64(o_SK), P64(o_SKa), nullptr, P32(o_V), P32(o_Va), true,
+            st = run_sort(ctx, cs, sb, P64(Lo.o_NH), P64(Lo.o_SK), P64(Lo.o_SKa), nullptr, P32(Lo.o_V), P32(Lo.o_Va), true,
                           cap[l], cs.count(kCntNodes + l), 0, 64, 0, s);
             if (st) return st;
 
             UniqueArgs u{};
-            u.keys = P64(o_SK);
-            u.perm = P32(o_V);
+            u.keys = P64(Lo.o_SK);
+            u.perm = P32(Lo.o_V);
             u.d_n = cs.count(kCntNodes + l);
             u.n_bound = cap[l];
-            u.masks = P8(o_NM);
-            u.children = P32(o_NCH);
+            u.masks = P8(Lo.o_NM);
+            u.children = P32(Lo.o_NCH);
             u.map = maps[it & 1];
-            u.out_keys = P64(o_ph[l]);
-            u.out_masks = P8(o_pm[l]);
-            u.out_children = P32(o_pc[l]);
+            u.out_keys = P64(Lo.o_ph[l]);
+            u.out_masks = P8(Lo.o_pm[l]);
+            u.out_children = P32(Lo.o_pc[l]);
             u.out_capacity = cap[l];
             u.d_out_n = cs.count(kCntUnique + l);
             u.status = cs.sv(cap[l]);
@@ -719,7 +736,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
 
             child_codes = node_codes[it & 1];
             child_map = maps[it & 1];
-            child_hashes = P64(o_ph[l]);
+            child_hashes = P64(Lo.o_ph[l]);
             d_child_n = cs.count(kCntNodes + l);
             child_bound = cap[l];
         }
@@ -730,11 +747,11 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             ta.child_map = child_map;
             ta.child_hashes = child_hashes;
             ta.d_child_n = d_child_n;
-            ta.scratch_children = P32(o_NCH);
+            ta.scratch_children = P32(Lo.o_NCH);
             for (int l = 0; l <= tail_first; ++l) {
-                ta.lv[l].hashes = P64(o_ph[l]);
-                ta.lv[l].masks = P8(o_pm[l]);
-                ta.lv[l].children = P32(o_pc[l]);
+                ta.lv[l].hashes = P64(Lo.o_ph[l]);
+                ta.lv[l].masks = P8(Lo.o_pm[l]);
+                ta.lv[l].children = P32(Lo.o_pc[l]);
                 ta.lv[l].capacity = cap[l];
                 ta.lv[l].d_nodes = cs.count(kCntNodes + l);
                 ta.lv[l].d_unique = cs.count(kCntUnique + l);
@@ -751,7 +768,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     };
     int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u}, s, enqueue);
     if (st) return st;
-    CallHeader* hdr = reinterpret_cast<CallHeader*>(b + o_hdr);
+    CallHeader* hdr = reinterpret_cast<CallHeader*>(b + Lo.o_hdr);
     // 5. One read-back of every count and the error word.
     static_assert(sizeof(CallHeader) >= 8 * 65, "header");
     DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, hdr, 8 + 8 * 64, cudaMemcpyDeviceToHost, s));
@@ -787,12 +804,12 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     out.masks.resize(nl);
     out.unique.resize(nl);
     for (int l = 0; l < nl; ++l) {
-        out.hashes[l] = P64(o_ph[l]);
-        out.children[l] = P32(o_pc[l]);
-        out.masks[l] = P8(o_pm[l]);
+        out.hashes[l] = P64(Lo.o_ph[l]);
+        out.children[l] = P32(Lo.o_pc[l]);
+        out.masks[l] = P8(Lo.o_pm[l]);
         out.unique[l] = counts[kCntUnique + l];
     }
-    out.leaves = P64(o_PL);
+    out.leaves = P64(Lo.o_PL);
     out.num_leaves = counts[kCntLeaves];
     return DAGC_OK;
 }
@@ -1285,6 +1302,11 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
     return materialise(ctx, p, nl, s, out);
 }
 
+uint64_t dagc_create_footprint(uint64_t n, int depth) {
+    if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
+    return CreateLayout(n, depth, 0).total;
+}
+
 int dagc_dag_num_levels(dagc_dag d, int* num_levels) {
     if (!d || !num_levels) return DAGC_ERR_INVALID_ARGUMENT;
     *num_levels = d->num_levels;
@@ -1381,6 +1403,30 @@ int dagc_dag_upload(dagc_context ctx, int num_levels, const uint64_t* sizes, con
         free_dag(d);
         cudaGetLastError();
         return set_error(ctx, cuda_status(ce), std::string("upload: ") + cudaGetErrorString(ce));
+    }
+    *out = d;
+    return DAGC_OK;
+}
+
+int dagc_dag_copy(dagc_context ctx, dagc_dag src, void* stream, dagc_dag* out) {
+    if (!valid_ctx(ctx) || !src || !out) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<uint64_t> sizes(src->num_levels);
+    for (int l = 0; l < src->num_levels; ++l) sizes[l] = src->level_offset[l + 1] - src->level_offset[l];
+    dagc_dag d = nullptr;
+    const int st = alloc_dag(ctx, src->num_levels, sizes, src->num_leaves, &d);
+    if (st) return st;
+    // Same layout: one copy of the whole block.
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = reinterpret_cast<char*>(d->masks + d->num_nodes()) - reinterpret_cast<char*>(d->block);
+    cudaError_t e = cudaMemcpyAsync(d->block, src->block, bytes, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        free_dag(d);
+        cudaGetLastError();
+        return set_error(ctx, cuda_status(e), std::string("copy: ") + cudaGetErrorString(e));
     }
     *out = d;
     return DAGC_OK;

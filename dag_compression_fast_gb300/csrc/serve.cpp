@@ -1,0 +1,282 @@
+// Serving loop over the dagc C ABI (include/dagc.h): compression requests are
+// admitted by their device-memory footprint into a fixed number of worker
+// slots and run concurrently, each slot on its own context (scratch arena,
+// DAG pool, recorded CUDA graphs) and its own stream, so that requests that
+// arrive while others run start as soon as a slot and memory are free and
+// their kernels overlap on the GPU. The reference has no counterpart (its
+// app compresses its subvolumes one after another,
+// src/DAG_Compression_Fast.cpp:283-302).
+//
+// Requests that name a chunk (its Morton index in a grid of chunks) keep their
+// intermediate DAG on the device after finishing; dagc_server_shared_dag
+// merges every such chunk into one device DAG (the growing shared DAG).
+
+#include "../../include/dagc.h"
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t ticket = 0;
+    const uint64_t* h_fragments = nullptr;  // caller-owned until the request is done
+    uint64_t n = 0;
+    int depth = 0;
+    int64_t chunk = -1;      // Morton index of the chunk, or -1
+    uint64_t footprint = 0;  // admission estimate, bytes
+    Clock::time_point submitted, started, finished;
+    int status = DAGC_OK;
+    std::string error;
+    std::vector<uint32_t> words;
+    bool done = false;
+};
+
+}  // namespace
+
+struct dagc_server_t {
+    int device = 0;
+    uint64_t budget = 0, in_use = 0, peak_in_use = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::map<uint64_t, std::shared_ptr<Request>> requests;
+    std::vector<std::thread> workers;
+    std::vector<dagc_context> contexts;
+    std::map<int64_t, dagc_dag> chunk_dags;  // kept on the device, by chunk Morton index
+    int chunk_depth = -1;
+    dagc_context merge_ctx = nullptr;
+    uint64_t next_ticket = 1;
+    uint64_t completed = 0, fragments_done = 0, running = 0, max_running = 0;
+    bool stop = false;
+};
+
+namespace {
+
+void worker_loop(dagc_server_t* sv, int slot) {
+    cudaSetDevice(sv->device);
+    dagc_context ctx = sv->contexts[slot];
+    cudaStream_t stream = nullptr;
+    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    // Staging buffer for the fragments, kept across requests: a cudaFree per
+    // request would synchronise the whole device and serialise the slots.
+    void* stage = nullptr;
+    uint64_t stage_cap = 0;
+    for (;;) {
+        std::shared_ptr<Request> r;
+        {
+            std::unique_lock<std::mutex> lock(sv->mu);
+            // FIFO admission: the head of the queue starts when a slot (this
+            // thread) is free and its footprint fits in the budget.
+            sv->cv_work.wait(lock, [&] {
+                return sv->stop ||
+                       (!sv->queue.empty() &&
+                        (sv->in_use + sv->queue.front()->footprint <= sv->budget || sv->in_use == 0));
+            });
+            if (sv->stop && sv->queue.empty()) break;
+            r = sv->queue.front();
+            sv->queue.pop_front();
+            sv->in_use += r->footprint;
+            sv->peak_in_use = std::max(sv->peak_in_use, sv->in_use);
+            ++sv->running;
+            sv->max_running = std::max(sv->max_running, sv->running);
+            r->started = Clock::now();
+        }
+        int st = DAGC_OK;
+        std::string err;
+        std::vector<uint32_t> words;
+        dagc_dag keep = nullptr;
+        {
+            // Host fragments in, host words out, on this slot's stream.
+            if (r->n > stage_cap) {
+                if (stage) cudaFree(stage);
+                stage = nullptr;
+                stage_cap = 0;
+                if (cudaMalloc(&stage, r->n * 8) != cudaSuccess) { cudaGetLastError(); st = DAGC_ERR_OUT_OF_MEMORY; }
+                else stage_cap = r->n;
+            }
+            if (!st && r->n && cudaMemcpyAsync(stage, r->h_fragments, r->n * 8, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+                cudaGetLastError();
+                st = DAGC_ERR_CUDA;
+            }
+            dagc_dag dag = nullptr;
+            if (!st) st = dagc_create(ctx, static_cast<const uint64_t*>(stage), r->n, r->depth, stream, &dag);
+            if (!st && r->chunk >= 0) {
+                // Keep a device copy of the chunk's DAG for the shared DAG.
+                std::lock_guard<std::mutex> lock(sv->mu);
+                st = dagc_dag_copy(sv->merge_ctx, dag, stream, &keep);
+            }
+            uint32_t* d_words = nullptr;
+            uint64_t nw = 0;
+            if (!st) st = dagc_final(ctx, dag, stream, &d_words, &nw);
+            else if (dag) dagc_dag_free(dag);
+            if (!st) {
+                words.resize(nw);
+                st = dagc_words_download(ctx, d_words, nw, words.data());
+                dagc_free_words(ctx, d_words, stream);
+            }
+            if (st) err = dagc_last_error(ctx);
+        }
+        {
+            std::lock_guard<std::mutex> lock(sv->mu);
+            r->status = st;
+            r->error = err;
+            r->words.swap(words);
+            r->finished = Clock::now();
+            r->done = true;
+            sv->in_use -= r->footprint;
+            --sv->running;
+            ++sv->completed;
+            sv->fragments_done += r->n;
+            if (keep) {
+                auto it = sv->chunk_dags.find(r->chunk);
+                if (it != sv->chunk_dags.end()) dagc_dag_free(it->second);
+                sv->chunk_dags[r->chunk] = keep;
+            }
+        }
+        sv->cv_done.notify_all();
+        sv->cv_work.notify_all();
+    }
+    if (stage) cudaFree(stage);
+    cudaStreamDestroy(stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int dagc_server_create(int device, int slots, uint64_t hbm_budget_bytes, dagc_server* out) {
+    if (!out || slots < 1 || slots > 64) return DAGC_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::unique_ptr<dagc_server_t> sv(new dagc_server_t);
+    sv->device = device;
+    sv->budget = hbm_budget_bytes;
+    for (int i = 0; i <= slots; ++i) {
+        dagc_context c = nullptr;
+        const int st = dagc_context_create(device, &c);
+        if (st) {
+            for (dagc_context x : sv->contexts) dagc_context_destroy(x);
+            if (sv->merge_ctx) dagc_context_destroy(sv->merge_ctx);
+            return st;
+        }
+        if (i < slots) sv->contexts.push_back(c);
+        else sv->merge_ctx = c;
+    }
+    for (int i = 0; i < slots; ++i) sv->workers.emplace_back(worker_loop, sv.get(), i);
+    *out = sv.release();
+    return DAGC_OK;
+}
+
+int dagc_server_submit(dagc_server sv, const uint64_t* h_fragments, uint64_t n, int depth, int64_t chunk_morton,
+                       uint64_t* ticket) {
+    if (!sv || !ticket || (n && !h_fragments) || depth < 2 || depth > 21) return DAGC_ERR_INVALID_ARGUMENT;
+    auto r = std::make_shared<Request>();
+    r->h_fragments = h_fragments;
+    r->n = n;
+    r->depth = depth;
+    r->chunk = chunk_morton;
+    // Scratch of the call + staged fragments + the DAG and its words (bounded
+    // by 16 bytes per fragment).
+    r->footprint = dagc_create_footprint(n, depth) + 8 * n + 16 * n;
+    r->submitted = Clock::now();
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        if (chunk_morton >= 0) {
+            if (sv->chunk_depth >= 0 && sv->chunk_depth != depth) return DAGC_ERR_INVALID_ARGUMENT;
+            sv->chunk_depth = depth;
+        }
+        r->ticket = sv->next_ticket++;
+        sv->requests[r->ticket] = r;
+        sv->queue.push_back(r);
+        *ticket = r->ticket;
+    }
+    sv->cv_work.notify_all();
+    return DAGC_OK;
+}
+
+int dagc_server_wait(dagc_server sv, uint64_t ticket, uint32_t* h_words, uint64_t capacity, uint64_t* n_words,
+                     double* latency_ms) {
+    if (!sv || !n_words) return DAGC_ERR_INVALID_ARGUMENT;
+    std::shared_ptr<Request> r;
+    {
+        std::unique_lock<std::mutex> lock(sv->mu);
+        auto it = sv->requests.find(ticket);
+        if (it == sv->requests.end()) return DAGC_ERR_INVALID_ARGUMENT;
+        r = it->second;
+        sv->cv_done.wait(lock, [&] { return r->done; });
+    }
+    *n_words = r->words.size();
+    if (latency_ms)
+        *latency_ms = std::chrono::duration<double, std::milli>(r->finished - r->submitted).count();
+    if (r->status) return r->status;
+    if (h_words) {
+        if (capacity < r->words.size()) return DAGC_ERR_INVALID_ARGUMENT;
+        if (!r->words.empty()) std::memcpy(h_words, r->words.data(), r->words.size() * 4);
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->requests.erase(ticket);  // the result has been collected
+    }
+    return DAGC_OK;
+}
+
+int dagc_server_stats(dagc_server sv, uint64_t* completed, uint64_t* fragments, uint64_t* max_concurrent,
+                      uint64_t* peak_footprint) {
+    if (!sv) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    if (completed) *completed = sv->completed;
+    if (fragments) *fragments = sv->fragments_done;
+    if (max_concurrent) *max_concurrent = sv->max_running;
+    if (peak_footprint) *peak_footprint = sv->peak_in_use;
+    return DAGC_OK;
+}
+
+int dagc_server_shared_dag(dagc_server sv, int top_levels, dagc_context* ctx_out, dagc_dag* out) {
+    if (!sv || !out || !ctx_out || top_levels < 0 || top_levels > 6) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    if (sv->chunk_depth < 0 || sv->chunk_depth + top_levels > 21) return DAGC_ERR_INVALID_ARGUMENT;
+    const uint64_t slots = 1ull << (3 * top_levels);
+    std::vector<dagc_dag> inputs(slots, nullptr);
+    int st = DAGC_OK;
+    // Copies of the kept chunk DAGs (dagc_merge consumes its inputs) and empty
+    // DAGs for the slots without a chunk.
+    for (uint64_t i = 0; i < slots && !st; ++i) {
+        auto it = sv->chunk_dags.find((int64_t)i);
+        if (it == sv->chunk_dags.end()) {
+            st = dagc_create(sv->merge_ctx, nullptr, 0, sv->chunk_depth, nullptr, &inputs[i]);
+            continue;
+        }
+        st = dagc_dag_copy(sv->merge_ctx, it->second, nullptr, &inputs[i]);  // dagc_merge consumes
+    }
+    if (!st) st = dagc_merge(sv->merge_ctx, inputs.data(), slots, nullptr, out);
+    for (dagc_dag d : inputs) if (d) dagc_dag_free(d);
+    *ctx_out = sv->merge_ctx;
+    return st;
+}
+
+void dagc_server_destroy(dagc_server sv) {
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    for (auto& t : sv->workers) t.join();
+    for (auto& kv : sv->chunk_dags) dagc_dag_free(kv.second);
+    for (dagc_context c : sv->contexts) dagc_context_destroy(c);
+    if (sv->merge_ctx) dagc_context_destroy(sv->merge_ctx);
+    delete sv;
+}
+
+}  // extern "C"

@@ -93,7 +93,12 @@ int dagc_dag_upload(dagc_context ctx, int num_levels, const uint64_t* level_size
                     const uint8_t* const* h_masks, const uint32_t* const* h_children,
                     const uint64_t* const* h_hashes, const uint64_t* h_leaves,
                     uint64_t num_leaves, void* stream, dagc_dag* out);
+/* Device copy of a DAG into (possibly another) context on the same device. */
+int dagc_dag_copy(dagc_context ctx, dagc_dag src, void* stream, dagc_dag* out);
 void dagc_dag_free(dagc_dag dag);
+/* Bytes of device scratch one dagc_create call of n fragments at this depth
+ * lays out (its arena; the DAG itself comes on top). 0 for n == 0. */
+uint64_t dagc_create_footprint(uint64_t n, int depth);
 
 /* ------------------------------------------------------------ MergeDAGs ---- */
 /* Replaces DAGCompression::MergeDAGs (src/DAGCompression.h:46,
@@ -187,6 +192,34 @@ int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint
 int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out,
                     const uint32_t* d_vals_in, uint32_t* d_vals_out, uint64_t n, int lo_bit,
                     int hi_bit, void* stream);
+
+/* -------------------------------------------------------------- serving ---- */
+/* A request loop: compression jobs are admitted in arrival order as soon as
+ * one of `slots` worker slots is free and their device-memory footprint fits
+ * in hbm_budget_bytes (a job larger than the budget runs alone); admitted jobs
+ * run concurrently, each slot with its own context and stream, so their work
+ * overlaps on the GPU. Each job: host fragments in, final words out. The
+ * reference has no counterpart (it compresses one subvolume after another). */
+typedef struct dagc_server_t* dagc_server;
+int dagc_server_create(int device, int slots, uint64_t hbm_budget_bytes, dagc_server* out);
+/* Queues a job; h_fragments must stay valid until dagc_server_wait returns for
+ * it. chunk_morton >= 0 marks the job as a chunk of a larger volume (all
+ * chunks of a server share one depth): its DAG is kept on the device for
+ * dagc_server_shared_dag. */
+int dagc_server_submit(dagc_server server, const uint64_t* h_fragments, uint64_t n, int depth,
+                       int64_t chunk_morton, uint64_t* ticket);
+/* Blocks until the job is done. With h_words == NULL only *n_words (and the
+ * latency from submission to completion) is returned; otherwise the words are
+ * copied out (capacity >= *n_words) and the job is forgotten. */
+int dagc_server_wait(dagc_server server, uint64_t ticket, uint32_t* h_words, uint64_t capacity,
+                     uint64_t* n_words, double* latency_ms);
+int dagc_server_stats(dagc_server server, uint64_t* completed, uint64_t* fragments,
+                      uint64_t* max_concurrent, uint64_t* peak_footprint);
+/* Merges every chunk job kept so far into one device DAG over a grid of
+ * 2^top_levels chunks per side (missing chunks empty), like dagc_merge; the
+ * DAG belongs to *ctx_out (the server's merge context). */
+int dagc_server_shared_dag(dagc_server server, int top_levels, dagc_context* ctx_out, dagc_dag* out);
+void dagc_server_destroy(dagc_server server);
 
 /* No counterpart in the reference. The key sort of dagc_sort_keys without any
  * allocation, for callers that must not allocate device memory once running:
