@@ -44,13 +44,14 @@ ERR_TOO_LARGE = 7
 # Every symbol of include/dagc.h, in declaration order.
 DAGC_SYMBOLS = [
     "dagc_context_create", "dagc_context_destroy", "dagc_last_error", "dagc_status_string",
-    "dagc_version", "dagc_create", "dagc_create_batched", "dagc_dag_num_levels", "dagc_dag_level_size",
+    "dagc_version", "dagc_hash_children", "dagc_create", "dagc_create_batched", "dagc_dag_num_levels", "dagc_dag_level_size",
     "dagc_dag_num_leaves", "dagc_dag_level_device", "dagc_dag_leaves_device",
     "dagc_dag_download_level", "dagc_dag_download_leaves", "dagc_dag_upload", "dagc_dag_copy",
     "dagc_dag_free", "dagc_create_footprint",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
-    "dagc_compress", "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
+    "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
@@ -96,6 +97,8 @@ def lib() -> ctypes.CDLL:
         L.dagc_last_error.restype = ctypes.c_char_p
         L.dagc_status_string.argtypes = [i32]
         L.dagc_status_string.restype = ctypes.c_char_p
+        L.dagc_hash_children.argtypes = [vp]
+        L.dagc_hash_children.restype = u64
         L.dagc_create.argtypes = [vp, vp, u64, i32, vp, pvp]
         L.dagc_create_batched.argtypes = [vp, vp, vp, vp, u64, i32, i32, vp, pvp]
         L.dagc_dag_num_levels.argtypes = [vp, ctypes.POINTER(i32)]
@@ -126,6 +129,9 @@ def lib() -> ctypes.CDLL:
         L.dagc_compress_host.argtypes = [vp, vp, u64, i32, vp, vp, u64, pu64]
         L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
+        L.dagc_file_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, vp, u64]
+        L.dagc_file_read.argtypes = [ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_uint32), vp, u64, pu64]
+        L.dagc_memory_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
         L.dagc_set_option.argtypes = [vp, i32, i32]
         L.dagc_profile_enable.argtypes = [vp, i32]
         L.dagc_profile_reset.argtypes = [vp]
@@ -438,6 +444,12 @@ class Context:
         self._check(lib().dagc_kernel_launches(self.handle, ctypes.byref(n)))
         return n.value
 
+    def memory_stats(self):
+        """Device memory of this context (dagc_memory_stats)."""
+        v = [ctypes.c_uint64(0) for _ in range(4)]
+        self._check(lib().dagc_memory_stats(self.handle, *[ctypes.byref(x) for x in v]))
+        return dict(zip(["in_use", "peak", "cached", "arena"], [x.value for x in v]))
+
     def last_counts(self):
         buf = (ctypes.c_uint64 * 64)()
         k = lib().dagc_last_counts(self.handle, buf, 64)
@@ -543,6 +555,38 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def write_dag_file(path: str, words: np.ndarray, depth: int, aabb=(0, 0, 0, 1, 1, 1)) -> None:
+    """Writes a final DAG as a .dag.bin file (the reference's format)."""
+    w = np.ascontiguousarray(words, np.uint32)
+    box = np.ascontiguousarray(np.asarray(aabb, np.float64))
+    st = lib().dagc_file_write(os.fsencode(path), box.ctypes.data, depth, _np_ptr(w), w.size)
+    if st:
+        raise DagcError(st, f"cannot write {path}")
+
+
+def read_dag_file(path: str):
+    """(words, depth, aabb) of a .dag.bin file."""
+    box = np.zeros(6, np.float64)
+    d = ctypes.c_uint32(0)
+    n = ctypes.c_uint64(0)
+    st = lib().dagc_file_read(os.fsencode(path), box.ctypes.data, ctypes.byref(d), None, 0, ctypes.byref(n))
+    if st:
+        raise DagcError(st, f"cannot read {path}")
+    w = np.zeros(n.value, np.uint32)
+    st = lib().dagc_file_read(os.fsencode(path), None, None, _np_ptr(w), w.size, ctypes.byref(n))
+    if st:
+        raise DagcError(st, f"cannot read {path}")
+    return w, d.value, tuple(box)
+
+
+def hash_children(h8) -> int:
+    """The node hash of 8 child hashes (dagc_hash_children)."""
+    a = np.ascontiguousarray(np.asarray(h8, dtype=np.uint64))
+    if a.size != 8:
+        raise DagcError(ERR_INVALID_ARGUMENT, "need 8 child hashes")
+    return int(lib().dagc_hash_children(a.ctypes.data))
 
 
 def create_footprint(n: int, depth: int) -> int:

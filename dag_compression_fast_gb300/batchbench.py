@@ -1,0 +1,106 @@
+"""Batched form against the plain per-chunk form (the batched workload).
+
+Workload: 256 chunks of 1024^3 (chunk depth 10) on a 16 x 16 footprint of a
+16384^2 fBm terrain with level-5 Menger sponges in some chunks; per-chunk
+fragment counts log-uniform in [10k, 8M] (about 306M in all); chunks in Morton
+order on a 16^3 grid of chunks (4 levels above them, depth 14 in all).
+
+  plain:   dagc_create per chunk (256 calls), then dagc_merge of the 4096
+           chunk slots (empty ones included), then dagc_final;
+  batched: dagc_create_batched once, then dagc_final.
+
+Both final DAGs must be identical. Prints one JSON line: chunks/s and voxels/s
+of each form, their ratio, and per-chunk latency (p50/p99) of the plain form.
+
+  python -m dag_compression_fast_gb300.batchbench [--scale 0.1] [--reps 3]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+
+def main(argv=None) -> int:
+    p = argparse.ArgumentParser()
+    p.add_argument("--scale", type=float, default=1.0, help="multiplies the per-chunk fragment targets")
+    p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--seed", type=int, default=0xDA6C0DE + 3)
+    a = p.parse_args(argv)
+    import torch
+
+    import dag_compression_fast_gb300 as D
+    t0 = time.perf_counter()
+    codes, counts, morton = D.gen_batched(chunk_depth=10, grid_xz=16, chunk_row=7, seed=a.seed,
+                                          min_fragments=1e4 * a.scale, max_fragments=8e6 * a.scale)
+    gen_s = time.perf_counter() - t0
+    n = int(codes.size)
+    k = int(counts.size)
+    offsets = np.zeros(k + 1, np.int64)
+    offsets[1:] = np.cumsum(counts.astype(np.int64))
+    ctx = D.Context(0)
+    d_codes = torch.from_numpy(codes.view(np.int64)).cuda()
+    s = torch.cuda.current_stream()
+
+    def batched():
+        dag = ctx.create_dag_batched(d_codes, counts, morton, 10, 4)
+        return ctx.create_final_dag(dag)
+
+    def plain(chunk_ms):
+        by_slot = {}
+        for i in range(k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            by_slot[int(morton[i])] = ctx.create_dag(d_codes[offsets[i]:offsets[i + 1]], 10)
+            e1.record(s)
+            e1.synchronize()
+            chunk_ms.append(e0.elapsed_time(e1))
+        dags = [by_slot.get(j) or ctx.create_dag(np.zeros(0, np.uint64), 10) for j in range(8 ** 4)]
+        return ctx.create_final_dag(ctx.merge_dags(dags))
+
+    def timed(fn, *args):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        w = fn(*args)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, w
+
+    ref = None
+    bt, pt, chunk_ms = [], [], []
+    for r in range(a.reps + 1):  # the first repetition warms up (graphs, arenas)
+        sec, w = timed(batched)
+        words_b = w.to_numpy()
+        w.free()
+        ms = []
+        sec_p, w = timed(plain, ms)
+        words_p = w.to_numpy()
+        w.free()
+        if ref is None:
+            ref = words_b
+        if not (np.array_equal(words_b, ref) and np.array_equal(words_p, ref)):
+            print(json.dumps({"error": "batched and per-chunk results differ"}))
+            return 1
+        if r:
+            bt.append(sec)
+            pt.append(sec_p)
+            chunk_ms += ms
+    b, pl = float(np.median(bt)), float(np.median(pt))
+    out = {
+        "workload": "batched_terrain_sponges_256x1024^3", "chunks": k, "fragments": n, "words": int(ref.size),
+        "generation_s": round(gen_s, 1), "bit_exact": True,
+        "batched": {"s": b, "chunks_per_s": k / b, "voxels_per_s": n / b, "ms_per_chunk": 1e3 * b / k},
+        "plain": {"s": pl, "chunks_per_s": k / pl, "voxels_per_s": n / pl,
+                  "chunk_ms_p50": float(np.percentile(chunk_ms, 50)),
+                  "chunk_ms_p99": float(np.percentile(chunk_ms, 99))},
+        "speedup_chunks_per_s": pl / b,
+    }
+    print(json.dumps(out), flush=True)
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -32,7 +32,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wextra", "-ffp
              f"-I{CUDA_HOME}/include", f"-I{INCLUDE}"]
 
 CU_SOURCES = ["sort.cu", "dag_kernels.cu", "sort_noalloc.cu"]
-CPP_SOURCES = ["dagc.cpp", "serve.cpp"]
+CPP_SOURCES = ["dagc.cpp", "serve.cpp", "io.cpp"]
 GEN_SOURCES = ["generators.cpp"]
 
 LIBDAGC = os.path.join(LIB, "libdagc.so")

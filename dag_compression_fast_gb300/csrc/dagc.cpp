@@ -100,6 +100,7 @@ public:
     }
     size_t in_use() const { return in_use_; }
     size_t peak() const { return peak_; }
+    size_t cached() const { return cached_; }
 
 private:
     std::multimap<size_t, void*> free_;
@@ -1171,6 +1172,8 @@ extern "C" {
 
 int dagc_version(void) { return 1; }
 
+uint64_t dagc_hash_children(const uint64_t* h8) { return h8 ? hash_children(h8) : 0; }
+
 const char* dagc_status_string(int status) {
     switch (status) {
         case DAGC_OK: return "ok";
@@ -1586,6 +1589,16 @@ int dagc_profile_read(dagc_context ctx, int stage, double* ms, uint64_t* launche
     if (ms) *ms = st.ms;
     if (launches) *launches = st.launches;
     if (bytes) *bytes = st.bytes;
+    return DAGC_OK;
+}
+
+int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64_t* cached, uint64_t* arena) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (in_use) *in_use = ctx->pool.in_use();
+    if (peak) *peak = ctx->pool.peak();
+    if (cached) *cached = ctx->pool.cached();
+    if (arena) *arena = ctx->arena.cap;
     return DAGC_OK;
 }
 

@@ -44,6 +44,10 @@ void dagc_context_destroy(dagc_context ctx);
 const char* dagc_last_error(dagc_context ctx);
 const char* dagc_status_string(int status);
 int dagc_version(void);
+/* The node hash: MurmurHash128xN of the 8 child hashes (0 = empty child) as
+ * 4 x 128-bit blocks, seed 0, low 64 bits, 0 mapped to 1 (HashChildrenHashes,
+ * src/DAGCompression.cu:758-763; src/Utils.h:119-154). Host function. */
+uint64_t dagc_hash_children(const uint64_t* h8);
 
 /* ------------------------------------------------------------ CreateDAG ---- */
 /* Replaces DAGCompression::CreateDAG (src/DAGCompression.h:45,
@@ -192,6 +196,24 @@ int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint
 int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out,
                     const uint32_t* d_vals_in, uint32_t* d_vals_out, uint64_t n, int lo_bit,
                     int hi_bit, void* stream);
+
+/* ------------------------------------------------------------ .dag.bin ---- */
+/* The reference's final-DAG file (src/Serializer.h:10-100, used at
+ * src/DAG_Compression_Fast.cpp:361-379): six doubles (AABB min x,y,z, max
+ * x,y,z), uint32 depth, uint64 word count, then the uint32 words. Host only. */
+int dagc_file_write(const char* path, const double* aabb6, uint32_t depth, const uint32_t* h_words,
+                    uint64_t n_words);
+/* Reads the header (aabb6, depth may be NULL) and, when h_words is not NULL
+ * and capacity >= *n_words, the words. */
+int dagc_file_read(const char* path, double* aabb6, uint32_t* depth, uint32_t* h_words,
+                   uint64_t capacity, uint64_t* n_words);
+
+/* --------------------------------------------------------- memory stats ---- */
+/* Device memory of a context (the reference's FMemory statistics,
+ * src/Memory.cpp:222-262): bytes held by live DAGs and word arrays, their
+ * peak, bytes cached for reuse, and the scratch arena's size. */
+int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64_t* cached,
+                      uint64_t* arena);
 
 /* -------------------------------------------------------------- serving ---- */
 /* A request loop: compression jobs are admitted in arrival order as soon as

@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 import dag_compression_fast_gb300 as D
@@ -49,3 +50,26 @@ def test_no_third_party_sort_libraries_in_sources():
         code = re.sub(r"//[^\n]*|/\*.*?\*/", "", text, flags=re.S)  # comments may cite the reference
         for banned in ("<cub/", "<thrust/", "moderngpu", "cub::", "thrust::", "mgpu::"):
             assert banned not in code, (f, banned)
+
+
+def test_dag_file_round_trip(tmp_path):
+    from oracle import oracle as O
+    from tests.inputs import random_codes
+    codes = random_codes(7, 3000, 4, cluster=True)
+    words = O.final_dag(O.create_dag(codes, 7))
+    path = str(tmp_path / "scene.dag.bin")
+    D.write_dag_file(path, words, 7, (-1.0, -2.0, -3.0, 4.0, 5.0, 6.0))
+    raw = open(path, "rb").read()
+    assert len(raw) == 6 * 8 + 4 + 8 + 4 * words.size  # the reference's layout, no padding
+    w, depth, box = D.read_dag_file(path)
+    assert depth == 7 and box == (-1.0, -2.0, -3.0, 4.0, 5.0, 6.0)
+    assert np.array_equal(w, words)
+
+
+def test_hash_children_matches_oracle():
+    import numpy as np
+    from oracle import oracle as O
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        h = rng.integers(0, 2**64 - 1, 8, dtype=np.uint64)
+        assert D.hash_children(h) == O.hash_children(h)
