@@ -39,13 +39,17 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* counter, uint32_t* s_slo
 // ---------------------------------------------------------------------------
 // Fused unique + leaf build.
 // ---------------------------------------------------------------------------
+// Tiles of kLeafTile sorted keys; thread t holds keys [16t, 16t + 16) of the
+// tile in registers (one 128-byte line, eight 16-byte loads), so shared memory
+// carries only one word per thread.
+constexpr int kLeafItems = 16;
+static_assert(kLeafTile == kT * kLeafItems, "leaf tile = 256 threads x 16 keys");
+
 struct LeafSmem {
-    uint64_t keys[kPadded];
-    uint64_t run_or[kTile];
-    uint16_t run_head[kTile];  // tile-local index of each run's first key
+    uint64_t lead[kT];   // OR of the thread's keys before its first run head (all keys if none)
+    uint8_t has_head[kT];
     uint32_t scan[34];
     uint32_t slot;
-    uint64_t lead_or;
     uint64_t p_base;
 };
 
@@ -56,101 +60,108 @@ __device__ __forceinline__ uint64_t global_code(const LeafBuildArgs& a, uint64_t
     return (__ldg(a.seg_code + (key >> a.seg_shift)) << a.seg_shift) | local;
 }
 
-// Fused unique + leaf build. Each tile emits the runs that START in it (one
-// (parent, mask) pair per distinct code >> 6); keys before the tile's first
-// head continue a run owned by an earlier tile: their OR goes to lead_or[tile]
-// and leaf_fixup folds it into that run's mask after this kernel.
+// Fused unique + leaf build. A run is a maximal range of keys with equal
+// key >> 6 (composite keys of the batched form have the same runs as their
+// global codes, since seg_shift >= 6); each tile emits the runs that START in
+// it as (parent, mask) pairs. A run is written by the thread holding its
+// head, which ORs in the leading keys of the following threads (shared
+// memory) up to the next head. Keys before the tile's first head continue a
+// run of an earlier tile: their OR goes to lead_or[tile] and leaf_fixup folds
+// it in after this kernel.
 __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LeafSmem& S = *reinterpret_cast<LeafSmem*>(smem_raw);
+    __shared__ LeafSmem S;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = load_count(a.d_n, a.n_bound);
-    const uint32_t ntiles = scan_tiles(n);
+    const uint32_t ntiles = leaf_tiles(n);
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
-        const uint64_t base = (uint64_t)tile * kTile;
-        const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
-        for (int i = tid; i < kTile; i += kT) {
-            if (i < (int)tile_n) S.keys[pad8(i)] = global_code(a, a.sorted[base + i]);
-            S.run_or[i] = 0;
-        }
-        if (tid == 0) S.lead_or = 0;
-        __syncthreads();
-
-        // Head flags of this thread's kI consecutive keys.
-        const int i0 = tid * kI;
-        bool hp;
-        uint64_t pv;
-        if (i0 == 0) { hp = base > 0; pv = hp ? (global_code(a, a.sorted[base - 1]) >> 6) : 0; }
-        else { hp = true; pv = i0 - 1 < (int)tile_n ? (S.keys[pad8(i0 - 1)] >> 6) : 0; }
-        const bool hp0 = hp;
-        const uint64_t pv0 = pv;
-        uint32_t heads = 0;
+        const uint64_t base = (uint64_t)tile * kLeafTile;
+        const uint64_t i0 = base + (uint64_t)tid * kLeafItems;
+        // Valid keys of this thread: the first nv.
+        const uint32_t nv = i0 >= n ? 0u : (uint32_t)(n - i0 < (uint64_t)kLeafItems ? n - i0 : kLeafItems);
+        uint64_t k[kLeafItems];
+        if (nv == kLeafItems) {
+            const ulonglong2* src = reinterpret_cast<const ulonglong2*>(a.sorted + i0);
 #pragma unroll
-        for (int j = 0; j < kI; ++j) {
-            const int i = i0 + j;
-            if (i < (int)tile_n) {
-                const uint64_t par = S.keys[pad8(i)] >> 6;
-                if (!hp || par != pv) ++heads;
-                pv = par;
-                hp = true;
+            for (int j = 0; j < kLeafItems / 2; ++j) {
+                const ulonglong2 v = __ldg(src + j);
+                k[2 * j] = v.x;
+                k[2 * j + 1] = v.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < kLeafItems; ++j) k[j] = (uint32_t)j < nv ? __ldg(a.sorted + i0 + j) : 0;
+        }
+        // Previous key's parent: the previous thread's last key (lane 0 reads it).
+        uint64_t prev = __shfl_up_sync(0xFFFFFFFFu, k[kLeafItems - 1], 1);
+        if (lane == 0 && i0 > 0 && nv > 0) prev = __ldg(a.sorted + i0 - 1);
+        const bool has_prev = i0 > 0;
+        uint32_t heads = 0;
+        uint64_t lead = 0;
+        {
+            uint64_t pv = prev >> 6;
+#pragma unroll
+            for (int j = 0; j < kLeafItems; ++j) {
+                if ((uint32_t)j < nv) {
+                    const uint64_t par = k[j] >> 6;
+                    if ((j == 0 && !has_prev) || par != pv) heads |= 1u << j;
+                    if (!heads) lead |= 1ull << (k[j] & 63);
+                    pv = par;
+                }
             }
         }
+        S.lead[tid] = lead;
+        S.has_head[tid] = heads != 0;
         uint32_t total_heads;
-        const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
-
-        // Warp 0 looks back first, so that the wait overlaps the other warps'
-        // run accumulation; it accumulates its own runs afterwards.
+        const uint32_t excl = block_exclusive_sum<uint32_t>((uint32_t)__popc(heads), S.scan, &total_heads);
         if (warp == 0) {
             const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
             if (lane == 0) S.p_base = pb;
         }
-        // Accumulate run ORs; run -1 = keys before the tile's first head.
-        {
-            int run = (int)excl - 1;
-            uint64_t acc = 0;
-            hp = hp0;
-            pv = pv0;
-#pragma unroll
-            for (int j = 0; j < kI; ++j) {
-                const int i = i0 + j;
-                if (i < (int)tile_n) {
-                    const uint64_t key = S.keys[pad8(i)];
-                    const uint64_t par = key >> 6;
-                    if (!hp || par != pv) {
-                        if (acc) atomicOr((unsigned long long*)(run >= 0 ? &S.run_or[run] : &S.lead_or),
-                                          (unsigned long long)acc);
-                        ++run;
-                        acc = 0;
-                        S.run_head[run] = (uint16_t)i;
-                    }
-                    acc |= 1ull << (key & 63);
-                    pv = par;
-                    hp = true;
-                }
-            }
-            if (acc) atomicOr((unsigned long long*)(run >= 0 ? &S.run_or[run] : &S.lead_or), (unsigned long long)acc);
-        }
         __syncthreads();
         const uint64_t p_base = S.p_base;
         bool overflow = false;
-        for (uint32_t r = tid; r < total_heads; r += kT) {
-            if (p_base + r < a.out_capacity) {
-                a.parents[p_base + r] = S.keys[pad8(S.run_head[r])] >> 6;
-                a.leaves[p_base + r] = S.run_or[r];
-            } else {
-                overflow = true;
+        if (heads) {
+            // Runs starting here: each ends at the next head of this thread or
+            // continues through the following threads' leading keys.
+            uint64_t r = p_base + excl;
+            uint64_t acc = 0, parent = 0;
+            bool open = false;
+#pragma unroll
+            for (int j = 0; j < kLeafItems; ++j) {
+                if ((uint32_t)j < nv) {
+                    if ((heads >> j) & 1u) {
+                        if (open) {
+                            if (r < a.out_capacity) { a.parents[r] = parent; a.leaves[r] = acc; } else overflow = true;
+                            ++r;
+                        }
+                        open = true;
+                        acc = 0;
+                        parent = global_code(a, k[j]) >> 6;
+                    }
+                    acc |= open ? 1ull << (k[j] & 63) : 0ull;
+                }
             }
+            for (uint32_t t = tid + 1; t < (uint32_t)kT; ++t) {
+                acc |= S.lead[t];
+                if (S.has_head[t]) break;
+            }
+            if (r < a.out_capacity) { a.parents[r] = parent; a.leaves[r] = acc; } else overflow = true;
         }
         if (overflow) atomicOr(a.err, kErrCapacity);
         if (tid == 0) {
             // Keys continuing the previous run: folded in by leaf_fixup. Tile 0
             // starts with a head, so it never has any.
-            a.lead_or[tile] = S.lead_or;
+            uint64_t lo = 0;
+            for (uint32_t t = 0; t < (uint32_t)kT; ++t) {
+                lo |= S.lead[t];
+                if (S.has_head[t]) break;
+            }
+            a.lead_or[tile] = lo;
             a.lead_run[tile] = p_base - 1;
-            if (base + tile_n == n) {
+            if (base + kLeafTile >= n) {
                 const uint64_t cnt = p_base + total_heads;
                 *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
             }
@@ -163,7 +174,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
 // earlier tile of leaf_build, one launch before, with a plain store).
 __global__ void leaf_fixup(LeafBuildArgs a) {
     const uint64_t n = load_count(a.d_n, a.n_bound);
-    const uint32_t ntiles = scan_tiles(n);
+    const uint32_t ntiles = leaf_tiles(n);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
         if (t == 0) continue;
         const uint64_t m = a.lead_or[t];
@@ -656,7 +667,7 @@ int occupancy_kernel(int which) {
     int occ = 0;
     switch (which) {
         case kKernelLeafBuild:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_build, kT, sizeof(LeafSmem));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_build, kT, 0);
             break;
         case kKernelExtract:
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, extract_level, kT, sizeof(ExtractSmem));
@@ -672,8 +683,8 @@ int occupancy_kernel(int which) {
 }
 
 void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s) {
-    leaf_build<<<a.grid, kT, sizeof(LeafSmem), s>>>(a);
-    const uint64_t tiles = scan_tiles(a.n_bound);
+    leaf_build<<<a.grid, kT, 0, s>>>(a);
+    const uint64_t tiles = leaf_tiles(a.n_bound);
     const int grid = (int)std::min<uint64_t>((tiles + 255) / 256, (uint64_t)g_blocks_small);
     leaf_fixup<<<grid > 0 ? grid : 1, 256, 0, s>>>(a);
 }

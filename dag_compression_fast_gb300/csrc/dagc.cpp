@@ -644,7 +644,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             a.status = cs.sv(n);
             a.tile_counter = cs.counter();
             a.err = err;
-            a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, scan_tiles(n));
+            a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, leaf_tiles(n));
             launch_leaf_build(a, s);
             ctx->launches += 2;
             DAGC_LAUNCHED(ctx);
