@@ -30,6 +30,8 @@ LIBGEN_PATH = os.path.join(LIB_DIR, "libdagc_gen.so")
 OPT_SORT_SHAPE_KEYS = 1
 OPT_SORT_SHAPE_PAIRS = 2
 OPT_GRAPHS = 3
+OPT_DEDUP = 4
+OPT_DEDUP_UNIQUE_LIMIT = 5
 NUM_SORT_SHAPES = 8
 
 OK = 0
@@ -51,7 +53,7 @@ DAGC_SYMBOLS = [
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
     "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
-    "dagc_last_counts", "dagc_set_option", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
@@ -129,6 +131,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_compress_host.argtypes = [vp, vp, u64, i32, vp, vp, u64, pu64]
         L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
+        L.dagc_dedup_fallbacks.argtypes = [vp, pu64]
         L.dagc_file_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, vp, u64]
         L.dagc_file_read.argtypes = [ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_uint32), vp, u64, pu64]
         L.dagc_memory_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
@@ -316,6 +319,12 @@ class Context:
             lib().dagc_context_destroy(self.handle)
             self.handle = None
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def __del__(self):
         try:
             self.close()
@@ -449,6 +458,12 @@ class Context:
         v = [ctypes.c_uint64(0) for _ in range(4)]
         self._check(lib().dagc_memory_stats(self.handle, *[ctypes.byref(x) for x in v]))
         return dict(zip(["in_use", "peak", "cached", "arena"], [x.value for x in v]))
+
+    def dedup_fallbacks(self) -> int:
+        """Calls rerun in the radix form because the hash-set dedup could not hold them."""
+        v = ctypes.c_uint64(0)
+        self._check(lib().dagc_dedup_fallbacks(self.handle, ctypes.byref(v)))
+        return v.value
 
     def last_counts(self):
         buf = (ctypes.c_uint64 * 64)()

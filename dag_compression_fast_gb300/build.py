@@ -31,7 +31,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wextra", "-ffp-contract=off",
              f"-I{CUDA_HOME}/include", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["sort.cu", "dag_kernels.cu", "sort_noalloc.cu"]
+CU_SOURCES = ["sort.cu", "dag_kernels.cu", "dedup.cu", "sort_noalloc.cu"]
 CPP_SOURCES = ["dagc.cpp", "serve.cpp", "io.cpp"]
 GEN_SOURCES = ["generators.cpp"]
 

@@ -49,6 +49,7 @@ struct CallHeader {
     uint64_t counts[64];
     uint32_t tile_counters[kMaxTileCounters];
     uint32_t hist[kMaxSorts][kMaxPasses * 256];
+    DedupState dedup[kMaxDepth + 1];  // leaves + one per level
 };
 static_assert(kCntSlots <= 64, "count slots");
 
@@ -173,8 +174,11 @@ struct GraphKey {
     int depth;
     void* arena;
     uint32_t chunks;  // batched calls: number of chunks (0 otherwise)
+    bool dedup;       // hash-set dedup (else radix sort + unique) for the leaves and levels
+    void* table;      // the dedup table block
     bool operator==(const GraphKey& o) const {
-        return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks;
+        return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks &&
+               dedup == o.dedup && table == o.table;
     }
 };
 struct GraphEntry {
@@ -201,6 +205,14 @@ struct dagc_context_t {
     int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
     DevicePool pool;
     Arena arena;
+    // Dedup table: keys (0 = empty) then aux words. Every level leaves its
+    // slots empty again; after a call that stopped early it is cleared.
+    bool use_dedup = true;
+    uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
+    void* table = nullptr;
+    uint64_t table_cap = 0;  // slots, a power of two
+    bool table_dirty = true;
+    uint64_t fallbacks = 0;  // calls rerun with the radix form
     std::string last_error;
     std::vector<uint64_t> last_counts;
     uint64_t* h_stage = nullptr;  // pinned: counts + error word read back
@@ -323,12 +335,13 @@ int device_error_status(uint32_t err, std::string& msg) {
 // for its tile bound; the regions are carved in launch order.
 struct CallSlots {
     CallHeader* h;
-    int next_counter = 0, next_hist = 0;
+    int next_counter = 0, next_hist = 0, next_dedup = 0;
     uint64_t* sv_next = nullptr;
     uint64_t* sv_end = nullptr;
     uint32_t* counter() { return &h->tile_counters[next_counter++]; }
     uint32_t* counters(int k) { uint32_t* p = &h->tile_counters[next_counter]; next_counter += k; return p; }
     uint32_t* hist() { return h->hist[next_hist++]; }
+    DedupState* dedup() { return &h->dedup[next_dedup++]; }
     uint64_t* sv(uint64_t n_bound) {
         uint64_t* p = sv_next;
         sv_next += scan_tiles(n_bound) + 1;
@@ -538,7 +551,11 @@ struct CreateLayout {
     size_t o_hdr, o_sv, o_ss0, o_ss1, o_A, o_B, o_P, o_LM, o_SK, o_SKa, o_V, o_Va, o_M0, o_M1;
     size_t o_NC0, o_NC1, o_NM, o_NCH, o_NH, o_PL, o_lead_or, o_lead_run, o_seg_off, o_seg_code;
     std::vector<size_t> o_ph, o_pc, o_pm;
-    CreateLayout(uint64_t n, int depth, uint32_t k_batch) {
+    // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
+    bool dedup = false;
+    uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
+    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bpos = 0;
+    CreateLayout(uint64_t n, int depth, uint32_t k_batch, bool use_dedup, uint64_t unique_limit = kDedupMaxUnique) {
         const int nl = depth - 2;
         cap.resize(nl);
         for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
@@ -555,10 +572,27 @@ struct CreateLayout {
         o_B = L.take<uint64_t>(n);
         o_P = L.take<uint64_t>(p0cap);
         o_LM = L.take<uint64_t>(p0cap);
-        o_SK = L.take<uint64_t>(p0cap);
-        o_SKa = L.take<uint64_t>(p0cap);
-        o_V = L.take<uint32_t>(p0cap);
-        o_Va = L.take<uint32_t>(p0cap);
+        dedup = use_dedup;
+        const uint64_t sort_cap = dedup ? 0 : p0cap;  // hash sorts of the radix form only
+        o_SK = L.take<uint64_t>(sort_cap);
+        o_SKa = L.take<uint64_t>(sort_cap);
+        o_V = L.take<uint32_t>(sort_cap);
+        o_Va = L.take<uint32_t>(sort_cap);
+        if (dedup) {
+            // Items per level are at most p0cap (leaves) or cap[l] <= p0cap.
+            item_cap = std::min<uint64_t>(p0cap, kDedupMaxItems);
+            uniq_cap = std::min<uint64_t>(p0cap, std::min<uint64_t>(unique_limit, kDedupMaxUnique));
+            bucket_area = dedup_bucket_area(uniq_cap);
+            table_slots = 1024;
+            while (table_slots < 2 * item_cap) table_slots <<= 1;
+            o_islot = L.take<uint32_t>(item_cap);
+            o_ukey = L.take<uint64_t>(uniq_cap);
+            o_uslot = L.take<uint32_t>(uniq_cap);
+            o_spl = L.take<uint64_t>(kDedupMaxSampledBuckets);
+            o_bcnt = L.take<uint32_t>(kDedupMaxBuckets);
+            o_bkey = L.take<uint64_t>(bucket_area);
+            o_bpos = L.take<uint32_t>(bucket_area);
+        }
         o_M0 = L.take<uint32_t>(p0cap);
         o_M1 = L.take<uint32_t>(p0cap);
         o_NC0 = L.take<uint64_t>(capmax);
@@ -581,16 +615,42 @@ struct CreateLayout {
     }
 };
 
+// Grows the context's dedup table to `slots` (zeroed); clears it after a call
+// that may have stopped between an insert and its map.
+int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
+    if (slots > ctx->table_cap) {
+        if (ctx->table) cudaFree(ctx->table);
+        ctx->table = nullptr;
+        ctx->table_cap = 0;
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 16));
+        ctx->table_cap = slots;
+        ctx->table_dirty = true;
+    }
+    if (ctx->table_dirty) {
+        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 8, s));
+        ctx->table_dirty = false;
+    }
+    return DAGC_OK;
+}
+
+// Internal status: the hash-set dedup could not hold this input; the caller
+// reruns the call with the radix form.
+constexpr int kStatusFallback = -1000;
+
 int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
-                    CreatePools& out, const BatchSpec* batch = nullptr) {
+                    CreatePools& out, const BatchSpec* batch, bool use_dedup) {
     const int nl = depth - 2;
     const int bits = 3 * depth;
-    const CreateLayout Lo(n, depth, batch ? batch->k : 0u);
+    const CreateLayout Lo(n, depth, batch ? batch->k : 0u, use_dedup, ctx->dedup_unique_limit);
     const std::vector<uint64_t>& cap = Lo.cap;
     const uint64_t capmax = Lo.capmax, p0cap = Lo.p0cap, sv_total = Lo.sv_total;
     const size_t zero_bytes = Lo.zero_bytes;
     (void)capmax;
     DAGC_CUDA(ctx, ctx->arena.reserve(Lo.total));
+    if (use_dedup) {
+        const int st = reserve_table(ctx, Lo.table_slots, s);
+        if (st) return st;
+    }
     char* b = static_cast<char*>(ctx->arena.base);
     auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
     auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
@@ -652,6 +712,45 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         }
         // 3. Leaf dedup: SortLevel on the leaf masks (the mask is its own hash).
         StageTimer t_dedup(ctx, DAGC_STAGE_LEAF_DEDUP, s);
+        // Hash-set dedup arguments shared by the leaves and every level.
+        auto dedup_args = [&](const uint64_t* keys, uint64_t* d_n, const uint8_t* masks, const uint32_t* children,
+                              uint64_t* out_keys, uint8_t* out_masks, uint32_t* out_children, uint64_t out_cap,
+                              uint64_t* d_out_n, uint32_t* map) {
+            DedupArgs d{};
+            d.keys = keys;
+            d.d_n = d_n;
+            d.masks = masks;
+            d.children = children;
+            d.sampled = masks == nullptr;  // leaf masks are not uniformly distributed; node hashes are
+            d.item_cap = Lo.item_cap;
+            d.table_key = static_cast<uint64_t*>(ctx->table);
+            d.table_aux = static_cast<uint64_t*>(ctx->table) + ctx->table_cap;
+            d.table_cap = ctx->table_cap;
+            d.item_slot = P32(Lo.o_islot);
+            d.uniq_key = P64(Lo.o_ukey);
+            d.uniq_slot = P32(Lo.o_uslot);
+            d.uniq_cap = Lo.uniq_cap;
+            d.splitters = P64(Lo.o_spl);
+            d.bucket_count = P32(Lo.o_bcnt);
+            d.bucket_key = P64(Lo.o_bkey);
+            d.bucket_pos = P32(Lo.o_bpos);
+            d.bucket_area = Lo.bucket_area;
+            d.state = cs.dedup();
+            d.out_keys = out_keys;
+            d.out_masks = out_masks;
+            d.out_children = out_children;
+            d.out_capacity = out_cap;
+            d.d_out_n = d_out_n;
+            d.map = map;
+            d.err = err;
+            return d;
+        };
+        if (use_dedup) {
+            ctx->launches += launch_dedup(dedup_args(P64(Lo.o_LM), cs.count(kCntBricks), nullptr, nullptr, P64(Lo.o_PL),
+                                                     nullptr, nullptr, p0cap, cs.count(kCntLeaves), P32(Lo.o_M0)),
+                                          s);
+            DAGC_LAUNCHED(ctx);
+        } else {
         st = run_sort(ctx, cs, sb, P64(Lo.o_LM), P64(Lo.o_SK), P64(Lo.o_SKa), nullptr, P32(Lo.o_V), P32(Lo.o_Va), true, p0cap,
                       cs.count(kCntBricks), 0, 64, 0, s);
         if (st) return st;
@@ -672,6 +771,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             launch_unique(a, s);
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
+        }
         }
         t_dedup.stop();
         // 4. Level loop, bottom-up.
@@ -710,6 +810,20 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
 
+            if (use_dedup) {
+                ctx->launches += launch_dedup(dedup_args(P64(Lo.o_NH), cs.count(kCntNodes + l), P8(Lo.o_NM),
+                                                         P32(Lo.o_NCH), P64(Lo.o_ph[l]), P8(Lo.o_pm[l]),
+                                                         P32(Lo.o_pc[l]), cap[l], cs.count(kCntUnique + l),
+                                                         maps[it & 1]),
+                                              s);
+                DAGC_LAUNCHED(ctx);
+                child_codes = node_codes[it & 1];
+                child_map = maps[it & 1];
+                child_hashes = P64(Lo.o_ph[l]);
+                d_child_n = cs.count(kCntNodes + l);
+                child_bound = cap[l];
+                continue;
+            }
             st = run_sort(ctx, cs, sb, P64(Lo.o_NH), P64(Lo.o_SK), P64(Lo.o_SKa), nullptr, P32(Lo.o_V), P32(Lo.o_Va), true,
                           cap[l], cs.count(kCntNodes + l), 0, 64, 0, s);
             if (st) return st;
@@ -767,8 +881,10 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
     return DAGC_OK;
     };
-    int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u}, s, enqueue);
-    if (st) return st;
+    int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u, use_dedup,
+                                       use_dedup ? ctx->table : nullptr},
+                         s, enqueue);
+    if (st) { ctx->table_dirty = true; return st; }
     CallHeader* hdr = reinterpret_cast<CallHeader*>(b + Lo.o_hdr);
     // 5. One read-back of every count and the error word.
     static_assert(sizeof(CallHeader) >= 8 * 65, "header");
@@ -794,6 +910,8 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         set_pending_bytes(ctx, DAGC_STAGE_LEVELS, lb);
         settle_profile(ctx);
     }
+    if (e32) ctx->table_dirty = true;  // a level may have stopped before clearing its slots
+    if ((e32 & kErrFallback) && !(e32 & (kErrBadInput | kErrTimeout))) return kStatusFallback;
     std::string msg;
     st = device_error_status(e32, msg);
     if (st) return set_error(ctx, st, msg);
@@ -1205,6 +1323,7 @@ int dagc_context_create(int device, dagc_context* out) {
         c->capture_stream = nullptr;  // graphs off; calls launch directly
     }
     if (const char* g = std::getenv("DAGC_GRAPHS")) c->use_graphs = std::atoi(g) != 0;
+    if (const char* d = std::getenv("DAGC_DEDUP")) c->use_dedup = std::atoi(d) != 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumSortShapes; ++sh) {
         c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
@@ -1228,6 +1347,7 @@ int dagc_context_create(int device, dagc_context* out) {
     c->grid_unique = std::max(1, occupancy_kernel(2)) * c->sms;
     c->grid_scan = std::max(1, occupancy_kernel(3)) * c->sms;
     c->grid_write = 8 * c->sms;
+    dedup_configure(c->sms);
     *out = c.release();
     return DAGC_OK;
 }
@@ -1241,6 +1361,7 @@ void dagc_context_destroy(dagc_context ctx) {
     drop_graphs(ctx);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     ctx->arena.release();
+    if (ctx->table) cudaFree(ctx->table);
     ctx->pool.trim();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     delete ctx;
@@ -1264,7 +1385,11 @@ int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int d
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     CreatePools p;
-    int st = create_pipeline(ctx, d_fragments, n, depth, s, p);
+    int st = create_pipeline(ctx, d_fragments, n, depth, s, p, nullptr, ctx->use_dedup);
+    if (st == kStatusFallback) {
+        ++ctx->fallbacks;
+        st = create_pipeline(ctx, d_fragments, n, depth, s, p, nullptr, false);
+    }
     if (st) return st;
     return materialise(ctx, p, nl, s, out);
 }
@@ -1300,14 +1425,19 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const BatchSpec batch{h_chunk_offsets, h_chunk_morton, (uint32_t)k, chunk_depth};
     CreatePools p;
-    int st = create_pipeline(ctx, d_fragments, n, depth, s, p, &batch);
+    int st = create_pipeline(ctx, d_fragments, n, depth, s, p, &batch, ctx->use_dedup);
+    if (st == kStatusFallback) {
+        ++ctx->fallbacks;
+        st = create_pipeline(ctx, d_fragments, n, depth, s, p, &batch, false);
+    }
     if (st) return st;
     return materialise(ctx, p, nl, s, out);
 }
 
 uint64_t dagc_create_footprint(uint64_t n, int depth) {
     if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
-    return CreateLayout(n, depth, 0).total;
+    const CreateLayout L(n, depth, 0, true);
+    return L.total + L.table_slots * 16;
 }
 
 int dagc_dag_num_levels(dagc_dag d, int* num_levels) {
@@ -1498,6 +1628,10 @@ int dagc_free_all(dagc_context ctx) {
     DAGC_CUDA(ctx, cudaDeviceSynchronize());
     drop_graphs(ctx);
     ctx->arena.release();
+    if (ctx->table) cudaFree(ctx->table);
+    ctx->table = nullptr;
+    ctx->table_cap = 0;
+    ctx->table_dirty = true;
     ctx->pool.trim();
     return DAGC_OK;
 }
@@ -1563,6 +1697,14 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
             ctx->use_graphs = value != 0;
             if (!ctx->use_graphs) drop_graphs(ctx);
             return DAGC_OK;
+        case DAGC_OPT_DEDUP:
+            ctx->use_dedup = value != 0;
+            return DAGC_OK;
+        case DAGC_OPT_DEDUP_UNIQUE_LIMIT:
+            if (value < 1) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "limit must be positive");
+            ctx->dedup_unique_limit = (uint64_t)value;
+            drop_graphs(ctx);
+            return DAGC_OK;
         default:
             return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "unknown option");
     }
@@ -1599,6 +1741,13 @@ int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64
     if (peak) *peak = ctx->pool.peak();
     if (cached) *cached = ctx->pool.cached();
     if (arena) *arena = ctx->arena.cap;
+    return DAGC_OK;
+}
+
+int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count) {
+    if (!valid_ctx(ctx) || !count) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *count = ctx->fallbacks;
     return DAGC_OK;
 }
 

@@ -19,6 +19,7 @@ enum : uint32_t {
     kErrCapacity = 8u,      // an upper bound on a buffer was exceeded
     kErrNotRooted = 16u,    // level 0 does not hold exactly one node
     kErrMergeRoot = 32u,    // a sub-DAG root hash missing from the merged level
+    kErrFallback = 64u,     // the hash-set dedup could not hold a level: rerun with the radix form
 };
 
 constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;
@@ -141,6 +142,43 @@ struct ExtractArgs {
     uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
 };
 void launch_extract(const ExtractArgs& a, cudaStream_t s);
+
+// Level dedup by hash set + bucket sort (dedup.cu): same outputs as sort
+// pairs + unique_runs on (key, item) for one level.
+constexpr uint32_t kDedupPerBucket = 256;            // expected distinct keys per bucket
+constexpr uint32_t kDedupTopBitCap = 1024;           // bucket room, top-bit form (128-256 expected)
+constexpr uint32_t kDedupSampledCap = 2048;          // bucket room, sampled form (256 expected)
+constexpr uint32_t kDedupMaxBuckets = 16384;         // top-bit form
+constexpr uint32_t kDedupMaxSampledBuckets = 4096;   // sampled form
+constexpr uint32_t kDedupSamplesPerBucket = 4;
+constexpr uint32_t kDedupMaxSample = kDedupSamplesPerBucket * kDedupMaxSampledBuckets;
+constexpr uint64_t kDedupMaxItems = 1ull << 24;
+constexpr uint64_t kDedupMaxUnique = (uint64_t)kDedupMaxBuckets * kDedupPerBucket;
+DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) { return 8 * uniq_cap + kDedupSampledCap; }
+struct DedupState {
+    unsigned long long u;  // distinct keys found (zero before the level)
+    uint32_t nbuckets, pad;
+};
+struct DedupArgs {
+    const uint64_t* keys; const uint64_t* d_n;       // items: key per item
+    const uint8_t* masks; const uint32_t* children;  // item payloads (null for leaves)
+    bool sampled;                                    // leaf masks: splitters from a sample; else top bits
+    uint64_t item_cap;
+    // Table of table_cap slots (a power of two): keys, 0 = empty (all 0 on
+    // entry and exit); aux = representative item | unique id << 32.
+    uint64_t* table_key; uint64_t* table_aux; uint64_t table_cap;
+    uint32_t* item_slot;
+    uint64_t* uniq_key; uint32_t* uniq_slot; uint64_t uniq_cap;
+    uint64_t* splitters; uint32_t* bucket_count;     // kDedupMaxSampledBuckets, kDedupMaxBuckets
+    uint64_t* bucket_key; uint32_t* bucket_pos; uint64_t bucket_area;
+    DedupState* state;
+    uint64_t* out_keys; uint8_t* out_masks; uint32_t* out_children; uint64_t out_capacity;
+    uint64_t* d_out_n;
+    uint32_t* map;  // item -> unique id
+    uint32_t* err;
+};
+void dedup_configure(int sms);
+int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (4 or 5)
 
 // The top levels in one single-CTA launch: every level l <= first_level has at
 // most kTailCap nodes, so extract + hash + sort + unique run in shared memory.

@@ -1,0 +1,327 @@
+// Level deduplication by hash set + bucket sort, for sm_103a. Replaces, for
+// one level (or the leaves), the reference's SortLevel
+// (src/DAGCompression.cu:864-914): sort (hash, index) pairs, flag runs, scan,
+// scatter to unique ids. Same result: the distinct keys in ascending order,
+// their payloads, and a map item -> unique id. Instead of eight 8-bit radix
+// passes over every item, the distinct keys are found first and only those
+// are sorted:
+//
+//   dedup_insert   every item inserts its key into an open-addressing table
+//                  (linear probing, atomicCAS on the key); the first inserter
+//                  of a key appends (key, slot) to the unique list and records
+//                  itself as the slot's representative;
+//   dedup_split    (leaf masks only) one CTA sorts a strided sample of 4 keys
+//                  per bucket and picks the bucket splitters: the keys are
+//                  distinct, so bucket sizes depend only on ranks, whatever
+//                  the key distribution. Node hashes are MurmurHash outputs:
+//                  their top bits are the bucket, no sample needed;
+//   dedup_scatter  unique keys go to fixed-capacity buckets (4x to 8x the
+//                  expected keys);
+//   dedup_sort     each bucket is ranked in shared memory (rank = number of
+//                  smaller keys) and written at its global ranks, with the
+//                  representative's payload; the unique id goes to the slot;
+//   dedup_map      every item reads its unique id and representative through
+//                  its slot, duplicates are compared in full with their
+//                  representative (collision check), the slots are cleared.
+//
+// What the fixed sizes cannot hold (table, unique list, a bucket) sets
+// kErrFallback, and the caller reruns the call with the radix-sort form.
+
+#include "dagc_device.cuh"
+#include "dagc_kernels.h"
+
+namespace dagc {
+namespace {
+
+__device__ __forceinline__ uint64_t table_size_for(uint64_t n) {
+    const uint64_t want = n < 512 ? 1024 : 2 * n;
+    return 1ull << (64 - __clzll(want - 1));
+}
+
+__device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
+    // Finaliser of MurmurHash3 (published constants): spreads leaf masks,
+    // whose bits are far from uniform, over the table.
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+__device__ __forceinline__ uint64_t unique_count(const DedupArgs& a) {
+    const uint64_t u = a.state->u;
+    return u < a.uniq_cap ? u : a.uniq_cap;
+}
+
+// Buckets of the top-bit form: a power of two with ~kDedupPerBucket keys each.
+__device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
+    uint32_t nb = 1;
+    int lg = 0;
+    while ((uint64_t)nb * kDedupPerBucket < u && nb < kDedupMaxBuckets) { nb <<= 1; ++lg; }
+    *shift = 64 - lg;
+    return nb;
+}
+
+__global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
+    const uint64_t n = *a.d_n;
+    const uint64_t S = table_size_for(n);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = gtid; b < kDedupMaxBuckets; b += gsize) a.bucket_count[b] = 0;
+    if (S > a.table_cap || n > a.item_cap) {
+        if (gtid == 0) atomicOr(a.err, kErrFallback);
+        return;
+    }
+    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);  // [2s] representative, [2s+1] unique id
+    const uint64_t warps = gsize / 32;
+    const uint64_t warp = gtid / 32;
+    bool bad = false, full = false;
+    for (uint64_t base = warp * 32; base < n; base += warps * 32) {
+        const uint64_t i = base + lane;
+        bool won = false;
+        uint64_t s = 0, h = 0;
+        if (i < n) {
+            h = a.keys[i];
+            uint32_t slot_out = 0xFFFFFFFFu;  // no slot: map gives 0, the error bits reject the call
+            if (h == 0) {
+                bad = true;  // 0 marks an empty slot; hashes and leaf masks are never 0
+            } else {
+                s = slot_hash(h) & (S - 1);
+                bool found = false;
+                for (uint64_t probe = 0; probe < S; ++probe) {
+                    uint64_t cur = ld_relaxed(a.table_key + s);
+                    if (cur == 0) {
+                        cur = atomicCAS((unsigned long long*)(a.table_key + s), 0ull, (unsigned long long)h);
+                        if (cur == 0) { won = true; break; }
+                    }
+                    if (cur == h) { found = true; break; }
+                    s = (s + 1) & (S - 1);
+                }
+                if (won || found) slot_out = (uint32_t)s;
+                else full = true;  // cannot happen below half load; rerun rather than guess
+            }
+            a.item_slot[i] = slot_out;
+        }
+        // Winners append to the unique list (one atomic per warp). Every lane
+        // takes part in the ballot and the shuffle.
+        const uint32_t wm = __ballot_sync(0xFFFFFFFFu, won);
+        uint64_t pos0 = 0;
+        if (lane == 0 && wm) pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)__popc(wm));
+        pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+        if (won) {
+            const uint64_t pos = pos0 + __popc(wm & lanemask_lt());
+            aux[2 * s] = (uint32_t)i;
+            if (pos < a.uniq_cap) {
+                a.uniq_key[pos] = h;
+                a.uniq_slot[pos] = (uint32_t)s;
+            } else {
+                full = true;
+            }
+        }
+    }
+    if (bad) atomicOr(a.err, kErrBadInput);
+    if (full) atomicOr(a.err, kErrFallback);
+}
+
+// Leaf masks: bucket count and splitters from a sorted sample (one CTA).
+constexpr int kSplitThreads = 1024;
+
+__global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* sample = reinterpret_cast<uint64_t*>(smem_raw);  // kDedupMaxSample
+    const uint32_t tid = threadIdx.x;
+    const uint64_t u = unique_count(a);
+    const uint64_t nb64 = (u + kDedupPerBucket - 1) / kDedupPerBucket;
+    const uint32_t nb = nb64 < 1 ? 1u : (uint32_t)(nb64 < kDedupMaxSampledBuckets ? nb64 : kDedupMaxSampledBuckets);
+    if (nb64 > kDedupMaxSampledBuckets || (uint64_t)nb * kDedupSampledCap > a.bucket_area) {
+        if (tid == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
+        return;
+    }
+    if (tid == 0) a.state->nbuckets = nb;
+    if (nb == 1) return;
+    const uint32_t ns = (uint32_t)(kDedupSamplesPerBucket * nb < u ? kDedupSamplesPerBucket * nb : u);
+    uint32_t p2 = 1;
+    while (p2 < ns) p2 <<= 1;
+    for (uint32_t j = tid; j < p2; j += kSplitThreads)
+        sample[j] = j < ns ? a.uniq_key[(uint64_t)j * u / ns] : ~0ull;
+    __syncthreads();
+    for (uint32_t k = 2; k <= p2; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = tid; i < p2; i += kSplitThreads) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const uint64_t x = sample[i], y = sample[ixj];
+                    if ((x > y) == ((i & k) == 0)) { sample[i] = y; sample[ixj] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // Bucket b holds keys in [splitter b-1, splitter b); splitter b is the
+    // sample of rank (b + 1) * ns / nb.
+    for (uint32_t b = tid; b + 1 < nb; b += kSplitThreads) a.splitters[b] = sample[(uint64_t)(b + 1) * ns / nb];
+}
+
+__global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // sampled form: kDedupMaxSampledBuckets
+    const uint64_t u = unique_count(a);
+    const uint32_t cap = a.sampled ? kDedupSampledCap : kDedupTopBitCap;
+    uint32_t nb;
+    int shift = 64;
+    if (a.sampled) {
+        nb = a.state->nbuckets;
+        if (nb == 0) return;
+        for (uint32_t b = threadIdx.x; b + 1 < nb; b += blockDim.x) spl[b] = a.splitters[b];
+        __syncthreads();
+    } else {
+        nb = topbit_buckets(u, &shift);
+        if ((uint64_t)nb * kDedupPerBucket < u || (uint64_t)nb * cap > a.bucket_area) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
+            return;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.state->nbuckets = nb;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = u;
+    bool over = false;
+    for (uint64_t pos = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < u;
+         pos += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = a.uniq_key[pos];
+        uint32_t b;
+        if (a.sampled) {
+            uint32_t lo = 0, hi = nb - 1;  // number of splitters <= key
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (spl[mid] <= key) lo = mid + 1; else hi = mid;
+            }
+            b = lo;
+        } else {
+            b = shift >= 64 ? 0u : (uint32_t)(key >> shift);
+        }
+        const uint32_t slot = atomicAdd(a.bucket_count + b, 1u);
+        if (slot < cap) {
+            a.bucket_key[(uint64_t)b * cap + slot] = key;
+            a.bucket_pos[(uint64_t)b * cap + slot] = (uint32_t)pos;
+        } else {
+            over = true;
+        }
+    }
+    if (over) atomicOr(a.err, kErrFallback);
+}
+
+// Each CTA takes a contiguous range of buckets; a bucket's keys are distinct,
+// so a key's rank is the number of smaller keys in its bucket.
+constexpr int kBucketThreads = 256;
+
+__global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
+    __shared__ uint64_t key[kDedupSampledCap];
+    __shared__ uint32_t red[kBucketThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t nb = a.state->nbuckets;
+    if (nb == 0) return;
+    const uint32_t cap = a.sampled ? kDedupSampledCap : kDedupTopBitCap;
+    const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
+    const uint32_t b1 = (uint32_t)((uint64_t)nb * (blockIdx.x + 1) / gridDim.x);
+    if (b0 >= b1) return;
+    // Keys in the buckets before this range.
+    uint32_t part = 0;
+    for (uint32_t x = tid; x < b0; x += kBucketThreads) part += min(a.bucket_count[x], cap);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    uint64_t start = 0;
+    for (int w = 0; w < kBucketThreads / 32; ++w) start += red[w];
+    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t cnt = min(a.bucket_count[b], cap);
+        const uint64_t src = (uint64_t)b * cap;
+        __syncthreads();  // the previous bucket's keys are no longer read
+        for (uint32_t j = tid; j < cnt; j += kBucketThreads) key[j] = a.bucket_key[src + j];
+        __syncthreads();
+        for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
+            const uint64_t k = key[j];
+            uint32_t r = 0;
+            for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
+            const uint64_t uid = start + r;
+            const uint32_t p = a.bucket_pos[src + j];
+            const uint32_t s = p < a.uniq_cap ? a.uniq_slot[p] : 0xFFFFFFFFu;
+            if (uid < a.out_capacity && s < a.table_cap) {
+                a.out_keys[uid] = k;
+                aux[2 * (uint64_t)s + 1] = (uint32_t)uid;
+                if (a.out_masks) {
+                    const uint32_t rep = aux[2 * (uint64_t)s];
+                    a.out_masks[uid] = a.masks[rep];
+                    const uint4* s4 = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                    uint4* d4 = reinterpret_cast<uint4*>(a.out_children + uid * 8);
+                    d4[0] = s4[0];
+                    d4[1] = s4[1];
+                }
+            } else {
+                atomicOr(a.err, kErrCapacity);
+            }
+        }
+        start += cnt;
+    }
+}
+
+__global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
+    const uint64_t n = *a.d_n;
+    if (table_size_for(n) > a.table_cap || n > a.item_cap) return;  // insert did nothing
+    const uint32_t last = a.out_capacity ? (uint32_t)(a.out_capacity - 1) : 0u;
+    bool collision = false;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = a.item_slot[i];
+        uint32_t uid = 0;
+        if (s < a.table_cap) {
+            const uint64_t aux = a.table_aux[s];
+            const uint32_t rep = (uint32_t)aux;
+            uid = (uint32_t)(aux >> 32);
+            if (a.masks && rep != (uint32_t)i && rep < n) {
+                const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
+                const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
+                collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
+                             x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
+            }
+            a.table_key[s] = 0;  // leave the table empty for the next level
+        }
+        // Ids stay inside the next level's arrays even when a fallback or an
+        // error discards this call.
+        a.map[i] = uid <= last ? uid : last;
+    }
+    if (collision) atomicOr(a.err, kErrCollision);
+}
+
+int g_sms = 152;
+
+}  // namespace
+
+void dedup_configure(int sms) {
+    cudaFuncSetAttribute(dedup_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupMaxSample * 8));
+    cudaFuncSetAttribute(dedup_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kDedupMaxSampledBuckets * 8));
+    g_sms = sms > 0 ? sms : 152;
+}
+
+int launch_dedup(const DedupArgs& a, cudaStream_t s) {
+    const uint64_t want = (a.item_cap + 255) / 256;
+    const int g = 4 * g_sms;
+    const int gi = (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
+    dedup_insert<<<gi, 256, 0, s>>>(a);
+    int launches = 1;
+    if (a.sampled) {
+        dedup_split<<<1, kSplitThreads, kDedupMaxSample * 8, s>>>(a);
+        ++launches;
+    }
+    dedup_scatter<<<gi, 256, a.sampled ? kDedupMaxSampledBuckets * 8 : 0, s>>>(a);
+    const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
+    const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
+    dedup_sort<<<gs, kBucketThreads, 0, s>>>(a);
+    dedup_map<<<gi, 256, 0, s>>>(a);
+    return launches + 3;
+}
+
+}  // namespace dagc

@@ -160,7 +160,17 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * replay it for later calls with the same input pointer, size and depth;
  * 0: launch every kernel directly. Profiling always launches directly. */
 #define DAGC_OPT_GRAPHS 3
+/* 1 (default): deduplicate the leaves and each level with a hash set and sort
+ * only the distinct hashes (bucket sort); 0: sort every (hash, index) pair with
+ * the radix sort, as the reference's SortLevel does. Results are identical.
+ * An input the hash-set form cannot hold is rerun in the radix form. */
+#define DAGC_OPT_DEDUP 4
+/* Testing: caps the hash-set form's unique list at `value` keys per level, so
+ * that larger levels take the rerun. */
+#define DAGC_OPT_DEDUP_UNIQUE_LIMIT 5
 int dagc_set_option(dagc_context ctx, int option, int value);
+/* Calls of this context rerun in the radix form so far. */
+int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
 
 /* ---------------------------------------------------- instrumentation ---- */
 /* Off by default. When enabled, each stage of a call is bracketed by CUDA

@@ -78,6 +78,62 @@ def test_create_dag_bit_exact(ctx, case):
     assert np.array_equal(decode_final(w, depth), np.unique(codes))
 
 
+@pytest.mark.parametrize("case", ["sphere_d7", "clustered_d10", "all_duplicates", "sparse_d21", "depth2"])
+def test_radix_form_bit_exact(case):
+    """The radix-sort form of the level dedup (option off) gives the same DAG."""
+    codes, depth = CASES[case]()
+    with D.Context(0) as c:
+        c.set_option(D.OPT_DEDUP, 0)
+        dag = c.create_dag(codes, depth)
+        assert_dag_equal(dag.to_host(), O.create_dag(codes, depth))
+        assert c.dedup_fallbacks() == 0
+
+
+def test_dedup_rerun_when_unique_list_is_full():
+    """A level with more distinct hashes than the hash-set form holds is rerun
+    in the radix form: same result, one rerun counted."""
+    codes, depth = CASES["sparse_d21"]()  # ~20k distinct nodes on most levels
+    ref = O.create_dag(codes, depth)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_DEDUP_UNIQUE_LIMIT, 100)
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 1
+        # The aborted levels left the table empty: the next call, with room
+        # again, runs the hash-set form and agrees.
+        c.set_option(D.OPT_DEDUP_UNIQUE_LIMIT, 1 << 30)
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 1
+
+
+def test_dedup_form_is_the_one_that_runs():
+    """Four or five launches per deduplicated level instead of a radix sort's
+    ten or more: the launch counter tells the two forms apart."""
+    codes, depth = CASES["clustered_d10"]()
+    launches = {}
+    for form in (0, 1):
+        with D.Context(0) as c:
+            c.set_option(D.OPT_GRAPHS, 0)
+            c.set_option(D.OPT_DEDUP, form)
+            before = c.kernel_launches()
+            c.create_dag(codes, depth)
+            launches[form] = c.kernel_launches() - before
+    assert launches[1] < launches[0]
+
+
+def test_dedup_many_buckets_and_skewed_leaves():
+    """Leaf masks confined to their low 16 bits (a skewed key distribution) and
+    levels with hundreds of thousands of distinct hashes (hundreds of buckets)."""
+    rng = np.random.default_rng(9)
+    depth = 9
+    bricks = rng.choice(8 ** (depth - 2), size=400_000, replace=False).astype(np.uint64)
+    low = rng.integers(0, 16, size=(bricks.size, 3)).astype(np.uint64)
+    codes = np.concatenate([(bricks << np.uint64(6)) | low[:, k] for k in range(3)])
+    ref = O.create_dag(codes, depth)
+    with D.Context(0) as c:
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 0
+
+
 def test_counts_reported(ctx):
     codes, depth = CASES["sphere_d7"]()
     ctx.create_dag(codes, depth).free()
