@@ -53,7 +53,7 @@ DAGC_SYMBOLS = [
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
     "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
-    "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
@@ -132,6 +132,9 @@ def lib() -> ctypes.CDLL:
         L.dagc_compress.argtypes = [vp, vp, u64, i32, vp, pvp, pu64]
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
         L.dagc_dedup_fallbacks.argtypes = [vp, pu64]
+        L.dagc_trace.argtypes = [vp, vp, u64, i32, vp, vp, vp, vp]
+        L.dagc_trace_camera.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32, vp, vp,
+                                        i32, ctypes.c_uint32, vp]
         L.dagc_file_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, vp, u64]
         L.dagc_file_read.argtypes = [ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_uint32), vp, u64, pu64]
         L.dagc_memory_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
@@ -282,6 +285,30 @@ class Words:
             self.free()
         except Exception:
             pass
+
+
+class TraceParams(ctypes.Structure):
+    """dagc_trace_params: the reference's FDAGTracer::TracePathsParams
+    (src/DAGTracer.h:15-25) in voxel units of the 2^depth grid."""
+    _fields_ = [("debug_level", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32), ("camera", ctypes.c_double * 3), ("ray_min", ctypes.c_double * 3),
+                ("ray_ddx", ctypes.c_double * 3), ("ray_ddy", ctypes.c_double * 3)]
+
+
+TRACE_POSITION_COLORS = 0xFFFFFFFF
+
+
+def trace_camera(position, right, up, forward, fov_degrees: float, width: int, height: int, aabb_min, aabb_max,
+                 depth: int, debug_level: int = TRACE_POSITION_COLORS) -> TraceParams:
+    """FDAGTracer::GetTraceParams (src/DAGTracer.h:26-79): a camera in scene
+    units mapped onto the 2^depth voxel grid of the box [aabb_min, aabb_max]."""
+    vecs = [np.ascontiguousarray(v, np.float64) for v in (position, right, up, forward, aabb_min, aabb_max)]
+    p = TraceParams()
+    st = lib().dagc_trace_camera(*[v.ctypes.data for v in vecs[:4]], float(fov_degrees), width, height,
+                                 vecs[4].ctypes.data, vecs[5].ctypes.data, depth, debug_level, ctypes.byref(p))
+    if st:
+        raise DagcError(st, "bad camera")
+    return p
 
 
 def _device_u64(fragments, device: int):
@@ -458,6 +485,29 @@ class Context:
         v = [ctypes.c_uint64(0) for _ in range(4)]
         self._check(lib().dagc_memory_stats(self.handle, *[ctypes.byref(x) for x in v]))
         return dict(zip(["in_use", "peak", "cached", "arena"], [x.value for x in v]))
+
+    def trace(self, words, depth: int, params: TraceParams, hits: bool = True, stream=None):
+        """Headless FDAGTracer::ResolvePaths: traces the final DAG (a Words
+        object, or a uint32 array / tensor of its words) and returns
+        (colours uint32[h, w], hits uint64[h, w] or None) on the host."""
+        import torch
+        if isinstance(words, Words):
+            ptr, n, keep = words.ptr, words.n, None
+        else:
+            t = words if isinstance(words, torch.Tensor) else torch.from_numpy(
+                np.ascontiguousarray(words, np.uint32).view(np.int32))
+            keep = t.to(f"cuda:{self.device}").contiguous()
+            ptr, n = keep.data_ptr(), keep.numel()
+        dev = f"cuda:{self.device}"
+        colors = torch.empty((params.height, params.width), dtype=torch.int32, device=dev)
+        hit_t = torch.empty((params.height, params.width), dtype=torch.int64, device=dev) if hits else None
+        st = lib().dagc_trace(self.handle, ptr, n, depth, ctypes.byref(params), colors.data_ptr(),
+                              hit_t.data_ptr() if hits else None, _stream_handle(stream))
+        del keep
+        self._check(st)
+        c = colors.cpu().numpy().view(np.uint32)
+        h = hit_t.cpu().numpy().view(np.uint64) if hits else None
+        return c, h
 
     def dedup_fallbacks(self) -> int:
         """Calls rerun in the radix form because the hash-set dedup could not hold them."""

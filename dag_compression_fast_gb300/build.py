@@ -31,7 +31,10 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wextra", "-ffp-contract=off",
              f"-I{CUDA_HOME}/include", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["sort.cu", "dag_kernels.cu", "dedup.cu", "sort_noalloc.cu"]
+CU_SOURCES = ["sort.cu", "dag_kernels.cu", "dedup.cu", "trace.cu", "sort_noalloc.cu"]
+# The tracer's float arithmetic must round once per operation (no FMA
+# contraction) so that its results are reproducible on the CPU.
+CU_EXTRA = {"trace.cu": ["--fmad=false"]}
 CPP_SOURCES = ["dagc.cpp", "serve.cpp", "io.cpp"]
 GEN_SOURCES = ["generators.cpp"]
 
@@ -71,7 +74,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
         objs.append(o)
         if force or not _newer(o, [s] + headers):
             extra = ["-Xptxas", "-v"] if ptxas_verbose else []
-            jobs.append([NVCC] + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+            jobs.append([NVCC] + NVCC_FLAGS + CU_EXTRA.get(src, []) + extra + ["-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")

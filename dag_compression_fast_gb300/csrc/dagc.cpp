@@ -15,6 +15,7 @@
 #include "dagc_kernels.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -213,6 +214,7 @@ struct dagc_context_t {
     uint64_t table_cap = 0;  // slots, a power of two
     bool table_dirty = true;
     uint64_t fallbacks = 0;  // calls rerun with the radix form
+    uint32_t* trace_err = nullptr;  // tracer error word
     std::string last_error;
     std::vector<uint64_t> last_counts;
     uint64_t* h_stage = nullptr;  // pinned: counts + error word read back
@@ -1362,6 +1364,7 @@ void dagc_context_destroy(dagc_context ctx) {
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     ctx->arena.release();
     if (ctx->table) cudaFree(ctx->table);
+    if (ctx->trace_err) cudaFree(ctx->trace_err);
     ctx->pool.trim();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     delete ctx;
@@ -1741,6 +1744,82 @@ int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64
     if (peak) *peak = ctx->pool.peak();
     if (cached) *cached = ctx->pool.cached();
     if (arena) *arena = ctx->arena.cap;
+    return DAGC_OK;
+}
+
+int dagc_trace_camera(const double position[3], const double right[3], const double up[3], const double forward[3],
+                      double fov_degrees, uint32_t width, uint32_t height, const double aabb_min[3],
+                      const double aabb_max[3], int depth, uint32_t debug_level, dagc_trace_params* out) {
+    if (!position || !right || !up || !forward || !aabb_min || !aabb_max || !out || !width || !height ||
+        depth < 3 || depth > kMaxDepth)
+        return DAGC_ERR_INVALID_ARGUMENT;
+    const double fov = fov_degrees / 2.0 * (3.14159265358979323846 / 180.);
+    const double aspect = double(width) / double(height);
+    const double sf = std::sin(fov), cf = std::cos(fov);
+    double bl[3], br[3], tl[3], cam[3];
+    for (int i = 0; i < 3; ++i) {
+        const double x = right[i] * sf * aspect, y = up[i] * sf, z = forward[i] * cf;
+        bl[i] = position[i] + z - y - x;
+        br[i] = position[i] + z - y + x;
+        tl[i] = position[i] + z + y - x;
+        const double scale = double(1u << depth) / (aabb_max[i] - aabb_min[i]);
+        const double t = -aabb_min[i];
+        cam[i] = (position[i] + t) * scale;
+        bl[i] = (bl[i] + t) * scale;
+        br[i] = (br[i] + t) * scale;
+        tl[i] = (tl[i] + t) * scale;
+    }
+    dagc_trace_params p{};
+    p.debug_level = debug_level;
+    p.width = width;
+    p.height = height;
+    for (int i = 0; i < 3; ++i) {
+        p.camera[i] = cam[i];
+        p.ray_min[i] = bl[i];
+        p.ray_ddx[i] = (br[i] - bl[i]) * (1.0 / width);
+        p.ray_ddy[i] = (tl[i] - bl[i]) * (1.0 / height);
+    }
+    *out = p;
+    return DAGC_OK;
+}
+
+int dagc_trace(dagc_context ctx, const uint32_t* d_words, uint64_t n_words, int depth,
+               const dagc_trace_params* params, uint32_t* d_colors, uint64_t* d_hits, void* stream) {
+    if (!valid_ctx(ctx) || !params) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (depth < 3 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [3, 21]");
+    const uint64_t pixels = (uint64_t)params->width * params->height;
+    if (pixels == 0) return DAGC_OK;
+    if (!d_colors || !d_words || n_words == 0) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null buffers");
+    if (params->width > 65535u * 8u || params->height > 65535u * 16u)
+        return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "image too large");
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!ctx->trace_err) DAGC_CUDA(ctx, cudaMalloc(&ctx->trace_err, 256));
+    DAGC_CUDA(ctx, cudaMemsetAsync(ctx->trace_err, 0, 4, s));
+    TraceArgs a{};
+    a.words = d_words;
+    a.n_words = n_words;
+    a.depth = depth;
+    a.debug_level = params->debug_level;
+    a.width = params->width;
+    a.height = params->height;
+    for (int i = 0; i < 3; ++i) {
+        a.camera[i] = params->camera[i];
+        a.ray_min[i] = params->ray_min[i];
+        a.ray_ddx[i] = params->ray_ddx[i];
+        a.ray_ddy[i] = params->ray_ddy[i];
+    }
+    a.colors = d_colors;
+    a.hits = d_hits;
+    a.err = ctx->trace_err;
+    launch_trace(a, s);
+    ++ctx->launches;
+    DAGC_LAUNCHED(ctx);
+    uint32_t err = 0;
+    DAGC_CUDA(ctx, cudaMemcpyAsync(&err, ctx->trace_err, 4, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    if (err) return set_error(ctx, DAGC_ERR_BAD_INPUT, "the word array is not a valid final DAG of this depth");
     return DAGC_OK;
 }
 

@@ -180,6 +180,18 @@ struct DedupArgs {
 void dedup_configure(int sms);
 int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (4 or 5)
 
+// Headless tracer (trace.cu): one primary ray per pixel through the final
+// word layout of a depth-`depth` DAG (depth >= 3).
+struct TraceArgs {
+    const uint32_t* words; uint64_t n_words; int depth;
+    uint32_t debug_level, width, height;
+    double camera[3], ray_min[3], ray_ddx[3], ray_ddy[3];
+    uint32_t* colors;  // width * height, row-major
+    uint64_t* hits;    // optional: Morton code of the voxel hit, ~0 for a miss
+    uint32_t* err;
+};
+void launch_trace(const TraceArgs& a, cudaStream_t s);
+
 // The top levels in one single-CTA launch: every level l <= first_level has at
 // most kTailCap nodes, so extract + hash + sort + unique run in shared memory.
 constexpr int kTailThreads = 1024;

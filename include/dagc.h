@@ -225,6 +225,35 @@ int dagc_file_read(const char* path, double* aabb6, uint32_t* depth, uint32_t* h
 int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64_t* cached,
                       uint64_t* arena);
 
+/* ------------------------------------------------------------- tracer ---- */
+/* Headless counterpart of the reference's FDAGTracer (src/DAGTracer.h:8-93,
+ * src/DAGTracer.cu:297-443): one primary ray per pixel through a final DAG
+ * (the words dagc_final returns), written to device buffers instead of an
+ * OpenGL surface. Ray parameters are in voxel units of the 2^depth grid, as in
+ * the reference's TracePathsParams. */
+typedef struct dagc_trace_params {
+    uint32_t debug_level; /* 0xFFFFFFFF: colour = hit position (low 8 bits per axis);
+                             else colour = MurmurHash32 of the node word index at
+                             level depth - 2 - debug_level on the ray's path */
+    uint32_t width, height, pad;
+    double camera[3];  /* ray origin */
+    double ray_min[3]; /* point seen by pixel (0, 0) */
+    double ray_ddx[3]; /* step per pixel in x */
+    double ray_ddy[3]; /* step per pixel in y */
+} dagc_trace_params;
+/* The reference's FDAGTracer::GetTraceParams (src/DAGTracer.h:26-79): camera
+ * position and basis (right, up, forward), vertical field of view in degrees,
+ * scene box; maps the box onto the 2^depth grid. */
+int dagc_trace_camera(const double position[3], const double right[3], const double up[3], const double forward[3],
+                      double fov_degrees, uint32_t width, uint32_t height, const double aabb_min[3],
+                      const double aabb_max[3], int depth, uint32_t debug_level, dagc_trace_params* out);
+/* Traces width x height rays (pixel (x, y) at y * width + x). d_colors:
+ * RGBA8 words; d_hits (may be NULL): Morton code of the voxel hit, ~0 for a
+ * miss. Needs depth in [3, 21]. A word array that is not a valid final DAG
+ * gives DAGC_ERR_BAD_INPUT (reads stay inside n_words). Synchronous. */
+int dagc_trace(dagc_context ctx, const uint32_t* d_words, uint64_t n_words, int depth,
+               const dagc_trace_params* params, uint32_t* d_colors, uint64_t* d_hits, void* stream);
+
 /* -------------------------------------------------------------- serving ---- */
 /* A request loop: compression jobs are admitted in arrival order as soon as
  * one of `slots` worker slots is free and their device-memory footprint fits

@@ -60,6 +60,8 @@ def lib():
         L.oracle_final.argtypes = [vp, vp, u64, ctypes.POINTER(u64)]
         L.oracle_final.restype = i32
         L.oracle_radix_sort_keys.argtypes = [vp, u64, i32, i32, i32]
+        L.oracle_trace.argtypes = [vp, u64, i32, vp, vp, vp, i32]
+        L.oracle_trace.restype = u64
         _lib = L
     return _lib
 
@@ -175,6 +177,18 @@ def merge_dags(dags) -> Dag:
     finally:
         for x in handles:
             L.oracle_free(x)
+
+
+def trace(words: np.ndarray, depth: int, params, threads: int = 4):
+    """The reference's trace_paths (src/DAGTracer.cu:297-427) restated on the
+    CPU: (colours uint32[h, w], hits uint64[h, w], pixels that read outside the
+    word array). `params` is a dagc_trace_params (ctypes structure)."""
+    w = np.ascontiguousarray(words, np.uint32)
+    colors = np.zeros((params.height, params.width), np.uint32)
+    hits = np.zeros((params.height, params.width), np.uint64)
+    bad = lib().oracle_trace(w.ctypes.data, w.size, depth, ctypes.addressof(params), colors.ctypes.data,
+                             hits.ctypes.data, threads)
+    return colors, hits, int(bad)
 
 
 def final_dag(d: Dag) -> np.ndarray:
