@@ -32,6 +32,8 @@ OPT_SORT_SHAPE_PAIRS = 2
 OPT_GRAPHS = 3
 OPT_DEDUP = 4
 OPT_DEDUP_UNIQUE_LIMIT = 5
+VOXELIZE_GL = 0
+VOXELIZE_SAT = 1
 NUM_SORT_SHAPES = 8
 
 OK = 0
@@ -53,7 +55,7 @@ DAGC_SYMBOLS = [
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
     "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
-    "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_profile_enable", "dagc_profile_reset",
+    "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_voxelize", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
@@ -62,7 +64,7 @@ DAGC_SYMBOLS = [
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
           "final", "merge"]
 GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
-               "dagc_gen_triangle_soup", "dagc_gen_batched"]
+               "dagc_gen_triangle_soup", "dagc_gen_soup_triangles", "dagc_gen_batched"]
 
 
 class DagcError(RuntimeError):
@@ -133,6 +135,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_last_counts.argtypes = [vp, pu64, i32]
         L.dagc_dedup_fallbacks.argtypes = [vp, pu64]
         L.dagc_trace.argtypes = [vp, vp, u64, i32, vp, vp, vp, vp]
+        L.dagc_voxelize.argtypes = [vp, vp, u64, vp, i32, i32, vp, u64, pu64, vp]
         L.dagc_trace_camera.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32, vp, vp,
                                         i32, ctypes.c_uint32, vp]
         L.dagc_file_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, vp, u64]
@@ -161,6 +164,7 @@ def gen_lib() -> ctypes.CDLL:
         G.dagc_gen_sphere_shell.argtypes = [i32, u64, dbl, vp, vp]
         G.dagc_gen_terrain.argtypes = [i32, u64, dbl, vp, vp]
         G.dagc_gen_triangle_soup.argtypes = [i32, u64, u64, i32, vp, vp]
+        G.dagc_gen_soup_triangles.argtypes = [i32, u64, u64, vp]
         G.dagc_gen_batched.argtypes = [i32, i32, i32, u64, dbl, dbl, i32, vp, vp, vp, vp, vp]
         _gen = G
     return _gen
@@ -509,6 +513,33 @@ class Context:
         h = hit_t.cpu().numpy().view(np.uint64) if hits else None
         return c, h
 
+    def voxelize(self, vertices, aabb, depth: int, mode: int = 0, capacity: int = None, stream=None):
+        """FVoxelizer::GenerateFragments on the GPU: triangles (n x 9 or n x 3 x 3
+        doubles, scene units; host array or device tensor) in the box aabb =
+        (min xyz, max xyz) -> device tensor of Morton codes (int64 view of the
+        uint64 codes), in a fixed order. mode: VOXELIZE_GL (the reference's
+        rule) or VOXELIZE_SAT. Without a capacity, a counting call sizes the buffer."""
+        import torch
+        dev = f"cuda:{self.device}"
+        if isinstance(vertices, torch.Tensor):
+            v = vertices.to(device=dev, dtype=torch.float64).contiguous()
+        else:
+            v = torch.from_numpy(np.ascontiguousarray(vertices, np.float64)).to(dev)
+        n_tri = v.numel() // 9
+        box = np.ascontiguousarray(aabb, np.float64)
+        n = ctypes.c_uint64(0)
+        if capacity is None:
+            st = lib().dagc_voxelize(self.handle, v.data_ptr(), n_tri, box.ctypes.data, depth, mode, None, 0,
+                                     ctypes.byref(n), _stream_handle(stream))
+            if st not in (OK, ERR_TOO_LARGE):
+                self._check(st)
+            capacity = n.value
+        out = torch.empty(max(capacity, 1), dtype=torch.int64, device=dev)
+        st = lib().dagc_voxelize(self.handle, v.data_ptr(), n_tri, box.ctypes.data, depth, mode, out.data_ptr(),
+                                 capacity, ctypes.byref(n), _stream_handle(stream))
+        self._check(st)
+        return out[: n.value]
+
     def dedup_fallbacks(self) -> int:
         """Calls rerun in the radix form because the hash-set dedup could not hold them."""
         v = ctypes.c_uint64(0)
@@ -678,6 +709,14 @@ def gen_sphere_shell(depth: int = 7, seed: int = 0xDA6C0DE, target_fragments: fl
 
 def gen_terrain(depth: int = 11, seed: int = 0xDA6C0DE + 1, column_fraction: float = 1.0) -> np.ndarray:
     return _gen_call(gen_lib().dagc_gen_terrain, depth, seed, float(column_fraction))
+
+
+def gen_soup_triangles(depth: int = 13, seed: int = 0xDA6C0DE + 2, num_triangles: int = 2_000_000) -> np.ndarray:
+    """The triangles of gen_triangle_soup (same arguments), grid units, shape (n, 3, 3)."""
+    out = np.zeros((num_triangles, 3, 3), np.float64)
+    if gen_lib().dagc_gen_soup_triangles(depth, seed, num_triangles, out.ctypes.data if num_triangles else None):
+        raise ValueError("bad generator arguments")
+    return out
 
 
 def gen_triangle_soup(depth: int = 13, seed: int = 0xDA6C0DE + 2, num_triangles: int = 2_000_000,

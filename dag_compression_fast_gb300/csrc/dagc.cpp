@@ -215,6 +215,8 @@ struct dagc_context_t {
     bool table_dirty = true;
     uint64_t fallbacks = 0;  // calls rerun with the radix form
     uint32_t* trace_err = nullptr;  // tracer error word
+    void* vox_scratch = nullptr;    // voxelizer counters and look-back status
+    size_t vox_scratch_bytes = 0;
     std::string last_error;
     std::vector<uint64_t> last_counts;
     uint64_t* h_stage = nullptr;  // pinned: counts + error word read back
@@ -1365,6 +1367,7 @@ void dagc_context_destroy(dagc_context ctx) {
     ctx->arena.release();
     if (ctx->table) cudaFree(ctx->table);
     if (ctx->trace_err) cudaFree(ctx->trace_err);
+    if (ctx->vox_scratch) cudaFree(ctx->vox_scratch);
     ctx->pool.trim();
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     delete ctx;
@@ -1820,6 +1823,58 @@ int dagc_trace(dagc_context ctx, const uint32_t* d_words, uint64_t n_words, int 
     DAGC_CUDA(ctx, cudaMemcpyAsync(&err, ctx->trace_err, 4, cudaMemcpyDeviceToHost, s));
     DAGC_CUDA(ctx, cudaStreamSynchronize(s));
     if (err) return set_error(ctx, DAGC_ERR_BAD_INPUT, "the word array is not a valid final DAG of this depth");
+    return DAGC_OK;
+}
+
+int dagc_voxelize(dagc_context ctx, const double* d_vertices, uint64_t n_triangles, const double aabb[6], int depth,
+                  int mode, uint64_t* d_codes, uint64_t capacity, uint64_t* n_codes, void* stream) {
+    if (!valid_ctx(ctx) || !aabb || !n_codes) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *n_codes = 0;
+    if (depth < 1 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [1, 21]");
+    if (mode != DAGC_VOXELIZE_GL && mode != DAGC_VOXELIZE_SAT)
+        return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "unknown voxelization mode");
+    for (int a = 0; a < 3; ++a)
+        if (!(aabb[3 + a] > aabb[a])) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "empty box");
+    if (n_triangles == 0) return DAGC_OK;
+    if (!d_vertices || (capacity && !d_codes)) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null buffers");
+    if (n_triangles > (1ull << 36)) return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many triangles");
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Scratch: total, tile counter, error word, look-back status per tile.
+    const uint64_t tiles = voxelize_tiles(n_triangles);
+    const size_t bytes = 64 + (tiles + 1) * 8;
+    if (bytes > ctx->vox_scratch_bytes) {
+        if (ctx->vox_scratch) cudaFree(ctx->vox_scratch);
+        ctx->vox_scratch = nullptr;
+        ctx->vox_scratch_bytes = 0;
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->vox_scratch, bytes));
+        ctx->vox_scratch_bytes = bytes;
+    }
+    char* b = static_cast<char*>(ctx->vox_scratch);
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, bytes, s));
+    VoxArgs a{};
+    a.vertices = d_vertices;
+    a.n_tri = n_triangles;
+    for (int i = 0; i < 6; ++i) a.aabb[i] = aabb[i];
+    a.depth = depth;
+    a.mode = mode;
+    a.codes = d_codes;
+    a.capacity = capacity;
+    a.d_total = reinterpret_cast<uint64_t*>(b);
+    a.tile_counter = reinterpret_cast<uint32_t*>(b + 8);
+    a.err = reinterpret_cast<uint32_t*>(b + 16);
+    a.status = reinterpret_cast<uint64_t*>(b + 64);
+    const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)ctx->sms * 8);
+    launch_voxelize(a, grid, s);
+    ++ctx->launches;
+    DAGC_LAUNCHED(ctx);
+    uint64_t h[3] = {0, 0, 0};
+    DAGC_CUDA(ctx, cudaMemcpyAsync(h, b, 24, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    if ((uint32_t)h[2]) return set_error(ctx, DAGC_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out");
+    *n_codes = h[0];
+    if (h[0] > capacity) return set_error(ctx, DAGC_ERR_TOO_LARGE, "fragment buffer too small (see n_codes)");
     return DAGC_OK;
 }
 

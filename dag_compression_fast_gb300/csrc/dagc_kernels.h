@@ -192,6 +192,20 @@ struct TraceArgs {
 };
 void launch_trace(const TraceArgs& a, cudaStream_t s);
 
+// Triangle voxelizer (voxelize.cu).
+constexpr int kVoxGL = 0;   // the reference's GL rule: one voxel per covered pixel of the dominant view
+constexpr int kVoxSAT = 1;  // every voxel the triangle touches (separating axis test)
+struct VoxArgs {
+    const double* vertices; uint64_t n_tri;  // 9 doubles per triangle
+    double aabb[6];                          // box mapped onto the grid: min xyz, max xyz
+    int depth, mode;
+    uint64_t* codes; uint64_t capacity;
+    uint64_t* d_total;                       // fragments produced (may exceed capacity)
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err;  // status: voxelize_tiles + 1 words, zero
+};
+void launch_voxelize(const VoxArgs& a, int grid, cudaStream_t s);
+uint64_t voxelize_tiles(uint64_t n_tri);
+
 // The top levels in one single-CTA launch: every level l <= first_level has at
 // most kTailCap nodes, so extract + hash + sort + unique run in shared memory.
 constexpr int kTailThreads = 1024;

@@ -277,24 +277,35 @@ V3 random_direction(Xoshiro& rng) {
     }
 }
 
-void soup_triangles(int depth, uint64_t seed, uint64_t t_lo, uint64_t t_hi, std::vector<uint64_t>& out) {
+// Triangle t of the soup: v0 uniform in the grid, two edges of log-uniform
+// length in [1, 16] along uniform directions, clamped into the grid.
+void soup_triangle(int depth, uint64_t seed, uint64_t t, V3 v[3]) {
     const double G = (double)((int64_t)1 << depth);
+    Xoshiro rng(mix3(seed, t, 0x7A1, 0));
+    const V3 v0{rng.uniform() * G, rng.uniform() * G, rng.uniform() * G};
+    const double l1 = exp2_det(4.0 * rng.uniform());  // log-uniform in [1, 16]
+    const double l2 = exp2_det(4.0 * rng.uniform());
+    const V3 d1 = random_direction(rng), d2 = random_direction(rng);
+    V3 v1{v0.x + l1 * d1.x, v0.y + l1 * d1.y, v0.z + l1 * d1.z};
+    V3 v2{v0.x + l2 * d2.x, v0.y + l2 * d2.y, v0.z + l2 * d2.z};
+    auto clampv = [&](V3& q) {
+        q.x = std::min(std::max(q.x, 0.0), G - 1e-9);
+        q.y = std::min(std::max(q.y, 0.0), G - 1e-9);
+        q.z = std::min(std::max(q.z, 0.0), G - 1e-9);
+    };
+    clampv(v1);
+    clampv(v2);
+    v[0] = v0;
+    v[1] = v1;
+    v[2] = v2;
+}
+
+void soup_triangles(int depth, uint64_t seed, uint64_t t_lo, uint64_t t_hi, std::vector<uint64_t>& out) {
     const int64_t Gi = (int64_t)1 << depth;
     for (uint64_t t = t_lo; t < t_hi; ++t) {
-        Xoshiro rng(mix3(seed, t, 0x7A1, 0));
-        const V3 v0{rng.uniform() * G, rng.uniform() * G, rng.uniform() * G};
-        const double l1 = exp2_det(4.0 * rng.uniform());  // log-uniform in [1, 16]
-        const double l2 = exp2_det(4.0 * rng.uniform());
-        const V3 d1 = random_direction(rng), d2 = random_direction(rng);
-        V3 v1{v0.x + l1 * d1.x, v0.y + l1 * d1.y, v0.z + l1 * d1.z};
-        V3 v2{v0.x + l2 * d2.x, v0.y + l2 * d2.y, v0.z + l2 * d2.z};
-        auto clampv = [&](V3& v) {
-            v.x = std::min(std::max(v.x, 0.0), G - 1e-9);
-            v.y = std::min(std::max(v.y, 0.0), G - 1e-9);
-            v.z = std::min(std::max(v.z, 0.0), G - 1e-9);
-        };
-        clampv(v1);
-        clampv(v2);
+        V3 v[3];
+        soup_triangle(depth, seed, t, v);
+        const V3 v0 = v[0], v1 = v[1], v2 = v[2];
         const int64_t bx0 = (int64_t)std::floor(std::min(v0.x, std::min(v1.x, v2.x)));
         const int64_t by0 = (int64_t)std::floor(std::min(v0.y, std::min(v1.y, v2.y)));
         const int64_t bz0 = (int64_t)std::floor(std::min(v0.z, std::min(v1.z, v2.z)));
@@ -345,6 +356,20 @@ int dagc_gen_terrain(int depth, uint64_t seed, double column_fraction, uint64_t*
     std::vector<uint64_t> vox;
     terrain_columns(depth, seed, column_fraction, 0, G, 0, G, (double)G / 4.0, G / 4, G / 2, 0, depth, vox);
     return emit(duplicate_and_shuffle(vox, seed, 4), out, n);
+}
+
+int dagc_gen_soup_triangles(int depth, uint64_t seed, uint64_t num_triangles, double* vertices) {
+    if (depth < 2 || depth > 21 || (num_triangles && !vertices)) return 1;
+    for (uint64_t t = 0; t < num_triangles; ++t) {
+        V3 v[3];
+        soup_triangle(depth, seed, t, v);
+        for (int k = 0; k < 3; ++k) {
+            vertices[9 * t + 3 * k + 0] = v[k].x;
+            vertices[9 * t + 3 * k + 1] = v[k].y;
+            vertices[9 * t + 3 * k + 2] = v[k].z;
+        }
+    }
+    return 0;
 }
 
 int dagc_gen_triangle_soup(int depth, uint64_t seed, uint64_t num_triangles, int threads,

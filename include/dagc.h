@@ -254,6 +254,24 @@ int dagc_trace_camera(const double position[3], const double right[3], const dou
 int dagc_trace(dagc_context ctx, const uint32_t* d_words, uint64_t n_words, int depth,
                const dagc_trace_params* params, uint32_t* d_colors, uint64_t* d_hits, void* stream);
 
+/* ---------------------------------------------------------- voxelizer ---- */
+/* The fragment producer: CUDA counterpart of the reference's OpenGL
+ * voxelization pass (FVoxelizer::GenerateFragments, src/Voxelizer.cpp:254-369,
+ * with its shaders). Triangles: 9 doubles each (v0, v1, v2) in DEVICE memory,
+ * in scene units; aabb (host): min xyz, max xyz, mapped onto the 2^depth grid.
+ * Writes up to `capacity` Morton codes to d_codes (triangles in input order,
+ * each triangle's fragments in a fixed order) and the total produced to
+ * *n_codes; a total above capacity gives DAGC_ERR_TOO_LARGE (the buffer then
+ * holds the first `capacity` codes), as the reference's fragment buffer check
+ * (src/Voxelizer.cpp:312). Synchronous. */
+#define DAGC_VOXELIZE_GL 0  /* the reference's rule: each triangle projected on
+                               its dominant axis, one voxel per covered pixel at
+                               the smallest depth over the pixel (float32) */
+#define DAGC_VOXELIZE_SAT 1 /* every voxel the triangle touches (separating
+                               axis test, float64) */
+int dagc_voxelize(dagc_context ctx, const double* d_vertices, uint64_t n_triangles, const double aabb[6], int depth,
+                  int mode, uint64_t* d_codes, uint64_t capacity, uint64_t* n_codes, void* stream);
+
 /* -------------------------------------------------------------- serving ---- */
 /* A request loop: compression jobs are admitted in arrival order as soon as
  * one of `slots` worker slots is free and their device-memory footprint fits

@@ -31,6 +31,10 @@ int dagc_gen_sphere_shell(int depth, uint64_t seed, double target_fragments, uin
  * column_fraction of the columns, each emitted U{1..4} times. */
 int dagc_gen_terrain(int depth, uint64_t seed, double column_fraction, uint64_t** out, uint64_t* n);
 
+/* The triangles of dagc_gen_triangle_soup (same depth, seed and count), in
+ * grid units: 9 doubles per triangle (v0, v1, v2). */
+int dagc_gen_soup_triangles(int depth, uint64_t seed, uint64_t num_triangles, double* vertices);
+
 /* Random triangle soup in a 2^depth grid: vertex v0 uniform, two edges of
  * log-uniform length in [1, 16] voxels and uniform direction, conservatively
  * surface-voxelized by a triangle/box separating-axis test. */

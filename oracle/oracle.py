@@ -61,6 +61,8 @@ def lib():
         L.oracle_final.restype = i32
         L.oracle_radix_sort_keys.argtypes = [vp, u64, i32, i32, i32]
         L.oracle_trace.argtypes = [vp, u64, i32, vp, vp, vp, i32]
+        L.oracle_voxelize_gl.argtypes = [vp, u64, vp, i32, vp, u64]
+        L.oracle_voxelize_gl.restype = u64
         L.oracle_trace.restype = u64
         _lib = L
     return _lib
@@ -189,6 +191,18 @@ def trace(words: np.ndarray, depth: int, params, threads: int = 4):
     bad = lib().oracle_trace(w.ctypes.data, w.size, depth, ctypes.addressof(params), colors.ctypes.data,
                              hits.ctypes.data, threads)
     return colors, hits, int(bad)
+
+
+def voxelize_gl(vertices: np.ndarray, aabb, depth: int) -> np.ndarray:
+    """The reference's GL voxelization (Shaders/*.glsl, src/Voxelizer.cpp)
+    restated on the CPU: Morton codes in triangle order."""
+    v = np.ascontiguousarray(vertices, np.float64).reshape(-1, 9)
+    box = np.ascontiguousarray(aabb, np.float64)
+    n = lib().oracle_voxelize_gl(v.ctypes.data, v.shape[0], box.ctypes.data, depth, None, 0)
+    out = np.zeros(n, np.uint64)
+    if n:
+        lib().oracle_voxelize_gl(v.ctypes.data, v.shape[0], box.ctypes.data, depth, out.ctypes.data, n)
+    return out
 
 
 def final_dag(d: Dag) -> np.ndarray:
