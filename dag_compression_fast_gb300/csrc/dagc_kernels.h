@@ -147,17 +147,18 @@ void launch_extract(const ExtractArgs& a, cudaStream_t s);
 // pairs + unique_runs on (key, item) for one level.
 constexpr uint32_t kDedupPerBucket = 256;            // expected distinct keys per bucket
 constexpr uint32_t kDedupTopBitCap = 1024;           // bucket room, top-bit form (128-256 expected)
-constexpr uint32_t kDedupSampledCap = 2048;          // bucket room, sampled form (256 expected)
+constexpr uint32_t kDedupSampledCap = 2048;          // least bucket room, sampled form (8x expected)
+constexpr uint32_t kDedupSampledCapMax = 8192;       // most (4M distinct keys over 4096 buckets)
 constexpr uint32_t kDedupMaxBuckets = 16384;         // top-bit form
 constexpr uint32_t kDedupMaxSampledBuckets = 4096;   // sampled form
 constexpr uint32_t kDedupSamplesPerBucket = 4;
 constexpr uint32_t kDedupMaxSample = kDedupSamplesPerBucket * kDedupMaxSampledBuckets;
 constexpr uint64_t kDedupMaxItems = 1ull << 24;
 constexpr uint64_t kDedupMaxUnique = (uint64_t)kDedupMaxBuckets * kDedupPerBucket;
-DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) { return 8 * uniq_cap + kDedupSampledCap; }
+DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) { return 8 * uniq_cap + 8 * kDedupSampledCapMax; }
 struct DedupState {
     unsigned long long u;  // distinct keys found (zero before the level)
-    uint32_t nbuckets, pad;
+    uint32_t nbuckets, bucket_cap;
 };
 struct DedupArgs {
     const uint64_t* keys; const uint64_t* d_n;       // items: key per item

@@ -16,7 +16,8 @@
 //                  the key distribution. Node hashes are MurmurHash outputs:
 //                  their top bits are the bucket, no sample needed;
 //   dedup_scatter  unique keys go to fixed-capacity buckets (4x to 8x the
-//                  expected keys);
+//                  expected keys; sampled buckets grow past 256 expected keys
+//                  once there are 4096 of them);
 //   dedup_sort     each bucket is ranked in shared memory (rank = number of
 //                  smaller keys) and written at its global ranks, with the
 //                  representative's payload; the unique id goes to the slot;
@@ -135,11 +136,13 @@ __global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
     const uint64_t u = unique_count(a);
     const uint64_t nb64 = (u + kDedupPerBucket - 1) / kDedupPerBucket;
     const uint32_t nb = nb64 < 1 ? 1u : (uint32_t)(nb64 < kDedupMaxSampledBuckets ? nb64 : kDedupMaxSampledBuckets);
-    if (nb64 > kDedupMaxSampledBuckets || (uint64_t)nb * kDedupSampledCap > a.bucket_area) {
+    const uint64_t per = (u + nb - 1) / nb;  // expected keys per bucket
+    const uint64_t cap = per * 8 > kDedupSampledCap ? per * 8 : kDedupSampledCap;
+    if (cap > kDedupSampledCapMax || (uint64_t)nb * cap > a.bucket_area) {
         if (tid == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
         return;
     }
-    if (tid == 0) a.state->nbuckets = nb;
+    if (tid == 0) { a.state->nbuckets = nb; a.state->bucket_cap = (uint32_t)cap; }
     if (nb == 1) return;
     const uint32_t ns = (uint32_t)(kDedupSamplesPerBucket * nb < u ? kDedupSamplesPerBucket * nb : u);
     uint32_t p2 = 1;
@@ -168,7 +171,7 @@ __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // sampled form: kDedupMaxSampledBuckets
     const uint64_t u = unique_count(a);
-    const uint32_t cap = a.sampled ? kDedupSampledCap : kDedupTopBitCap;
+    const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
     uint32_t nb;
     int shift = 64;
     if (a.sampled) {
@@ -216,12 +219,13 @@ __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
 constexpr int kBucketThreads = 256;
 
 __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
-    __shared__ uint64_t key[kDedupSampledCap];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t* key = reinterpret_cast<uint64_t*>(smem_raw);  // bucket room: kDedupSampledCapMax or kDedupTopBitCap
     __shared__ uint32_t red[kBucketThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nb = a.state->nbuckets;
     if (nb == 0) return;
-    const uint32_t cap = a.sampled ? kDedupSampledCap : kDedupTopBitCap;
+    const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
     const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
     const uint32_t b1 = (uint32_t)((uint64_t)nb * (blockIdx.x + 1) / gridDim.x);
     if (b0 >= b1) return;
@@ -303,6 +307,7 @@ void dedup_configure(int sms) {
     cudaFuncSetAttribute(dedup_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupMaxSample * 8));
     cudaFuncSetAttribute(dedup_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kDedupMaxSampledBuckets * 8));
+    cudaFuncSetAttribute(dedup_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupSampledCapMax * 8));
     g_sms = sms > 0 ? sms : 152;
 }
 
@@ -319,7 +324,7 @@ int launch_dedup(const DedupArgs& a, cudaStream_t s) {
     dedup_scatter<<<gi, 256, a.sampled ? kDedupMaxSampledBuckets * 8 : 0, s>>>(a);
     const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
     const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
-    dedup_sort<<<gs, kBucketThreads, 0, s>>>(a);
+    dedup_sort<<<gs, kBucketThreads, (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s>>>(a);
     dedup_map<<<gi, 256, 0, s>>>(a);
     return launches + 3;
 }

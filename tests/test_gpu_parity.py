@@ -120,6 +120,21 @@ def test_dedup_form_is_the_one_that_runs():
     assert launches[1] < launches[0]
 
 
+def test_dedup_over_a_million_distinct_leaves():
+    """More distinct leaf masks than 4096 sampled buckets of 256: the buckets
+    grow instead of the call being rerun."""
+    rng = np.random.default_rng(12)
+    depth = 11
+    bricks = rng.choice(8 ** (depth - 2), size=1_500_000, replace=False).astype(np.uint64)
+    low = rng.integers(0, 64, size=(bricks.size, 5)).astype(np.uint64)
+    codes = np.concatenate([(bricks << np.uint64(6)) | low[:, k] for k in range(5)])
+    ref = O.create_dag(codes, depth, threads=8)
+    assert ref.leaves.size > 1_050_000
+    with D.Context(0) as c:
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 0
+
+
 def test_dedup_many_buckets_and_skewed_leaves():
     """Leaf masks confined to their low 16 bits (a skewed key distribution) and
     levels with hundreds of thousands of distinct hashes (hundreds of buckets)."""
