@@ -558,7 +558,7 @@ struct CreateLayout {
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
-    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bpos = 0;
+    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bslot = 0, o_brep = 0;
     CreateLayout(uint64_t n, int depth, uint32_t k_batch, bool use_dedup, uint64_t unique_limit = kDedupMaxUnique) {
         const int nl = depth - 2;
         cap.resize(nl);
@@ -592,10 +592,12 @@ struct CreateLayout {
             o_islot = L.take<uint32_t>(item_cap);
             o_ukey = L.take<uint64_t>(uniq_cap);
             o_uslot = L.take<uint32_t>(uniq_cap);
+            o_uitem = L.take<uint32_t>(uniq_cap);
             o_spl = L.take<uint64_t>(kDedupMaxSampledBuckets);
             o_bcnt = L.take<uint32_t>(kDedupMaxBuckets);
             o_bkey = L.take<uint64_t>(bucket_area);
-            o_bpos = L.take<uint32_t>(bucket_area);
+            o_bslot = L.take<uint32_t>(bucket_area);
+            o_brep = L.take<uint32_t>(bucket_area);
         }
         o_M0 = L.take<uint32_t>(p0cap);
         o_M1 = L.take<uint32_t>(p0cap);
@@ -733,11 +735,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.item_slot = P32(Lo.o_islot);
             d.uniq_key = P64(Lo.o_ukey);
             d.uniq_slot = P32(Lo.o_uslot);
+            d.uniq_item = P32(Lo.o_uitem);
             d.uniq_cap = Lo.uniq_cap;
             d.splitters = P64(Lo.o_spl);
             d.bucket_count = P32(Lo.o_bcnt);
             d.bucket_key = P64(Lo.o_bkey);
-            d.bucket_pos = P32(Lo.o_bpos);
+            d.bucket_slot = P32(Lo.o_bslot);
+            d.bucket_rep = P32(Lo.o_brep);
             d.bucket_area = Lo.bucket_area;
             d.state = cs.dedup();
             d.out_keys = out_keys;

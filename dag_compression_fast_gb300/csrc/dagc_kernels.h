@@ -169,9 +169,9 @@ struct DedupArgs {
     // entry and exit); aux = representative item | unique id << 32.
     uint64_t* table_key; uint64_t* table_aux; uint64_t table_cap;
     uint32_t* item_slot;
-    uint64_t* uniq_key; uint32_t* uniq_slot; uint64_t uniq_cap;
+    uint64_t* uniq_key; uint32_t* uniq_slot; uint32_t* uniq_item; uint64_t uniq_cap;
     uint64_t* splitters; uint32_t* bucket_count;     // kDedupMaxSampledBuckets, kDedupMaxBuckets
-    uint64_t* bucket_key; uint32_t* bucket_pos; uint64_t bucket_area;
+    uint64_t* bucket_key; uint32_t* bucket_slot; uint32_t* bucket_rep; uint64_t bucket_area;
     DedupState* state;
     uint64_t* out_keys; uint8_t* out_masks; uint32_t* out_children; uint64_t out_capacity;
     uint64_t* d_out_n;

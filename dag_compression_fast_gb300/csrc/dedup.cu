@@ -8,14 +8,15 @@
 //
 //   dedup_insert   every item inserts its key into an open-addressing table
 //                  (linear probing, atomicCAS on the key); the first inserter
-//                  of a key appends (key, slot) to the unique list and records
-//                  itself as the slot's representative;
+//                  of a key appends (key, slot, itself) to the unique list and
+//                  records itself as the slot's representative;
 //   dedup_split    (leaf masks only) one CTA sorts a strided sample of 4 keys
 //                  per bucket and picks the bucket splitters: the keys are
 //                  distinct, so bucket sizes depend only on ranks, whatever
 //                  the key distribution. Node hashes are MurmurHash outputs:
 //                  their top bits are the bucket, no sample needed;
-//   dedup_scatter  unique keys go to fixed-capacity buckets (4x to 8x the
+//   dedup_scatter  unique keys, with their slot and representative, go to
+//                  fixed-capacity buckets (4x to 8x the
 //                  expected keys; sampled buckets grow past 256 expected keys
 //                  once there are 4096 of them);
 //   dedup_sort     each bucket is ranked in shared memory (rank = number of
@@ -64,6 +65,9 @@ __device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
     return nb;
 }
 
+// Items per lane in flight at once (independent probe chains).
+constexpr int kIlp = 4;
+
 __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     const uint64_t n = *a.d_n;
     const uint64_t S = table_size_for(n);
@@ -79,46 +83,68 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     const uint64_t warps = gsize / 32;
     const uint64_t warp = gtid / 32;
     bool bad = false, full = false;
-    for (uint64_t base = warp * 32; base < n; base += warps * 32) {
-        const uint64_t i = base + lane;
-        bool won = false;
-        uint64_t s = 0, h = 0;
-        if (i < n) {
-            h = a.keys[i];
-            uint32_t slot_out = 0xFFFFFFFFu;  // no slot: map gives 0, the error bits reject the call
-            if (h == 0) {
-                bad = true;  // 0 marks an empty slot; hashes and leaf masks are never 0
-            } else {
-                s = slot_hash(h) & (S - 1);
-                bool found = false;
-                for (uint64_t probe = 0; probe < S; ++probe) {
-                    uint64_t cur = ld_relaxed(a.table_key + s);
-                    if (cur == 0) {
-                        cur = atomicCAS((unsigned long long*)(a.table_key + s), 0ull, (unsigned long long)h);
-                        if (cur == 0) { won = true; break; }
-                    }
-                    if (cur == h) { found = true; break; }
-                    s = (s + 1) & (S - 1);
-                }
-                if (won || found) slot_out = (uint32_t)s;
-                else full = true;  // cannot happen below half load; rerun rather than guess
-            }
-            a.item_slot[i] = slot_out;
+    // Each lane takes kIlp items (32 apart) per round and runs their probe
+    // chains side by side. A probe reads the slot first and only an empty
+    // slot takes an atomicCAS: duplicated keys (common leaf masks) would
+    // otherwise serialise on their slot's atomics.
+    for (uint64_t base = warp * 32 * kIlp; base < n; base += warps * 32 * kIlp) {
+        uint64_t h[kIlp], s[kIlp];
+        bool live[kIlp], won[kIlp];
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint64_t i = base + k * 32 + lane;
+            won[k] = false;
+            live[k] = i < n;
+            h[k] = live[k] ? a.keys[i] : 0;
+            if (live[k] && h[k] == 0) { bad = true; live[k] = false; }  // 0 marks an empty slot
+            s[k] = slot_hash(h[k]) & (S - 1);
         }
-        // Winners append to the unique list (one atomic per warp). Every lane
-        // takes part in the ballot and the shuffle.
-        const uint32_t wm = __ballot_sync(0xFFFFFFFFu, won);
-        uint64_t pos0 = 0;
-        if (lane == 0 && wm) pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)__popc(wm));
-        pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
-        if (won) {
-            const uint64_t pos = pos0 + __popc(wm & lanemask_lt());
-            aux[2 * s] = (uint32_t)i;
-            if (pos < a.uniq_cap) {
-                a.uniq_key[pos] = h;
-                a.uniq_slot[pos] = (uint32_t)s;
-            } else {
-                full = true;
+        bool found[kIlp];
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) found[k] = false;
+        for (uint64_t probe = 0; probe < S; ++probe) {
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k) {
+                if (!live[k] || won[k] || found[k]) continue;
+                uint64_t cur = ld_relaxed(a.table_key + s[k]);
+                if (cur == 0)
+                    cur = atomicCAS((unsigned long long*)(a.table_key + s[k]), 0ull, (unsigned long long)h[k]);
+                if (cur == 0) won[k] = true;
+                else if (cur == h[k]) found[k] = true;
+                else { s[k] = (s[k] + 1) & (S - 1); any = true; }
+            }
+            if (!any) break;
+        }
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint64_t i = base + k * 32 + lane;
+            if (i < n) {
+                const bool placed = live[k] && (won[k] || found[k]);
+                if (live[k] && !placed) full = true;  // cannot happen below half load; rerun rather than guess
+                a.item_slot[i] = placed ? (uint32_t)s[k] : 0xFFFFFFFFu;
+            }
+        }
+        // Winners append to the unique list (one atomic per warp and item
+        // row). Every lane takes part in the ballots and shuffles.
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint32_t wm = __ballot_sync(0xFFFFFFFFu, won[k]);
+            uint64_t pos0 = 0;
+            if (lane == 0 && wm)
+                pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)__popc(wm));
+            pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+            if (won[k]) {
+                const uint64_t i = base + k * 32 + lane;
+                const uint64_t pos = pos0 + __popc(wm & lanemask_lt());
+                aux[2 * s[k]] = (uint32_t)i;
+                if (pos < a.uniq_cap) {
+                    a.uniq_key[pos] = h[k];
+                    a.uniq_slot[pos] = (uint32_t)s[k];
+                    a.uniq_item[pos] = (uint32_t)i;
+                } else {
+                    full = true;
+                }
             }
         }
     }
@@ -205,8 +231,10 @@ __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
         }
         const uint32_t slot = atomicAdd(a.bucket_count + b, 1u);
         if (slot < cap) {
-            a.bucket_key[(uint64_t)b * cap + slot] = key;
-            a.bucket_pos[(uint64_t)b * cap + slot] = (uint32_t)pos;
+            const uint64_t e = (uint64_t)b * cap + slot;
+            a.bucket_key[e] = key;
+            a.bucket_slot[e] = a.uniq_slot[pos];
+            a.bucket_rep[e] = a.uniq_item[pos];
         } else {
             over = true;
         }
@@ -229,9 +257,19 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
     const uint32_t b1 = (uint32_t)((uint64_t)nb * (blockIdx.x + 1) / gridDim.x);
     if (b0 >= b1) return;
-    // Keys in the buckets before this range.
+    // Keys in the buckets before this range (8 independent loads per thread
+    // in flight).
     uint32_t part = 0;
-    for (uint32_t x = tid; x < b0; x += kBucketThreads) part += min(a.bucket_count[x], cap);
+    for (uint32_t x0 = 0; x0 < b0; x0 += 8 * kBucketThreads) {
+        uint32_t c[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const uint32_t x = x0 + u * kBucketThreads + tid;
+            c[u] = x < b0 ? a.bucket_count[x] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) part += min(c[u], cap);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
     if (lane == 0) red[warp] = part;
@@ -246,22 +284,31 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) key[j] = a.bucket_key[src + j];
         __syncthreads();
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
+            // Slot and representative come with the key; their loads (and the
+            // payload's) are in flight while the rank is counted.
+            const uint32_t s = a.bucket_slot[src + j];
+            const uint32_t rep = a.bucket_rep[src + j];
+            uint8_t m = 0;
+            uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
+            if (a.out_masks) {
+                m = a.masks[rep];
+                const uint4* s4 = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                c0 = s4[0];
+                c1 = s4[1];
+            }
             const uint64_t k = key[j];
             uint32_t r = 0;
+#pragma unroll 8
             for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
             const uint64_t uid = start + r;
-            const uint32_t p = a.bucket_pos[src + j];
-            const uint32_t s = p < a.uniq_cap ? a.uniq_slot[p] : 0xFFFFFFFFu;
             if (uid < a.out_capacity && s < a.table_cap) {
                 a.out_keys[uid] = k;
                 aux[2 * (uint64_t)s + 1] = (uint32_t)uid;
                 if (a.out_masks) {
-                    const uint32_t rep = aux[2 * (uint64_t)s];
-                    a.out_masks[uid] = a.masks[rep];
-                    const uint4* s4 = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                    a.out_masks[uid] = m;
                     uint4* d4 = reinterpret_cast<uint4*>(a.out_children + uid * 8);
-                    d4[0] = s4[0];
-                    d4[1] = s4[1];
+                    d4[0] = c0;
+                    d4[1] = c1;
                 }
             } else {
                 atomicOr(a.err, kErrCapacity);
@@ -275,26 +322,40 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
     const uint64_t n = *a.d_n;
     if (table_size_for(n) > a.table_cap || n > a.item_cap) return;  // insert did nothing
     const uint32_t last = a.out_capacity ? (uint32_t)(a.out_capacity - 1) : 0u;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     bool collision = false;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = a.item_slot[i];
-        uint32_t uid = 0;
-        if (s < a.table_cap) {
-            const uint64_t aux = a.table_aux[s];
-            const uint32_t rep = (uint32_t)aux;
-            uid = (uint32_t)(aux >> 32);
-            if (a.masks && rep != (uint32_t)i && rep < n) {
-                const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
-                const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
-                const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
-                collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
-                             x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
-            }
-            a.table_key[s] = 0;  // leave the table empty for the next level
+    // kIlp items per thread per round, their slot reads in flight together.
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += stride * kIlp) {
+        uint32_t s[kIlp];
+        uint64_t aux[kIlp];
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint64_t i = i0 + k * stride;
+            s[k] = i < n ? a.item_slot[i] : 0xFFFFFFFFu;
         }
-        // Ids stay inside the next level's arrays even when a fallback or an
-        // error discards this call.
-        a.map[i] = uid <= last ? uid : last;
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) aux[k] = s[k] < a.table_cap ? a.table_aux[s[k]] : 0;
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint64_t i = i0 + k * stride;
+            if (i >= n) continue;
+            uint32_t uid = 0;
+            if (s[k] < a.table_cap) {
+                const uint32_t rep = (uint32_t)aux[k];
+                uid = (uint32_t)(aux[k] >> 32);
+                if (a.masks && rep != (uint32_t)i && rep < n) {
+                    const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
+                    const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                    const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
+                    collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
+                                 x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
+                }
+                a.table_key[s[k]] = 0;  // leave the table empty for the next level
+            }
+            // Ids stay inside the next level's arrays even when a fallback or
+            // an error discards this call.
+            a.map[i] = uid <= last ? uid : last;
+        }
     }
     if (collision) atomicOr(a.err, kErrCollision);
 }
@@ -313,7 +374,7 @@ void dedup_configure(int sms) {
 
 int launch_dedup(const DedupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.item_cap + 255) / 256;
-    const int g = 4 * g_sms;
+    const int g = 8 * g_sms;  // full occupancy: 8 CTAs of 256 threads per SM
     const int gi = (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
     dedup_insert<<<gi, 256, 0, s>>>(a);
     int launches = 1;
