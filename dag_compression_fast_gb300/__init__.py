@@ -32,6 +32,7 @@ OPT_SORT_SHAPE_PAIRS = 2
 OPT_GRAPHS = 3
 OPT_DEDUP = 4
 OPT_DEDUP_UNIQUE_LIMIT = 5
+OPT_GROUP = 6
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
 NUM_SORT_SHAPES = 8
@@ -62,7 +63,7 @@ DAGC_SYMBOLS = [
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
-          "final", "merge"]
+          "final", "merge", "group"]
 GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
                "dagc_gen_triangle_soup", "dagc_gen_soup_triangles", "dagc_gen_batched"]
 

@@ -71,6 +71,7 @@ __device__ __forceinline__ uint64_t global_code(const LeafBuildArgs& a, uint64_t
 __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
     __shared__ LeafSmem S;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (a.gate && *a.gate != a.gate_run) return;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = leaf_tiles(n);
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
@@ -173,6 +174,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
 // ORs every tile's leading keys into the run they continue (written by an
 // earlier tile of leaf_build, one launch before, with a plain store).
 __global__ void leaf_fixup(LeafBuildArgs a) {
+    if (a.gate && *a.gate != a.gate_run) return;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = leaf_tiles(n);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {

@@ -51,6 +51,8 @@ struct CallHeader {
     uint32_t tile_counters[kMaxTileCounters];
     uint32_t hist[kMaxSorts][kMaxPasses * 256];
     DedupState dedup[kMaxDepth + 1];  // leaves + one per level
+    uint32_t sketch[kGroupSketchRegs];  // distinct-brick sketch of the fragment grouping
+    uint32_t path[2];                   // 1: fragments grouped by hash, 0: sorted; log2 table slots
 };
 static_assert(kCntSlots <= 64, "count slots");
 
@@ -177,9 +179,10 @@ struct GraphKey {
     uint32_t chunks;  // batched calls: number of chunks (0 otherwise)
     bool dedup;       // hash-set dedup (else radix sort + unique) for the leaves and levels
     void* table;      // the dedup table block
+    int group;        // fragment grouping mode
     bool operator==(const GraphKey& o) const {
         return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks &&
-               dedup == o.dedup && table == o.table;
+               dedup == o.dedup && table == o.table && group == o.group;
     }
 };
 struct GraphEntry {
@@ -206,9 +209,12 @@ struct dagc_context_t {
     int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
     DevicePool pool;
     Arena arena;
-    // Dedup table: keys (0 = empty) then aux words. Every level leaves its
-    // slots empty again; after a call that stopped early it is cleared.
+    // Hash table shared by the fragment grouping and the dedup: keys (0 =
+    // empty), then the dedup's aux words, then the grouping's masks. Keys and
+    // masks are zero between uses (every level and the grouping clear the
+    // slots they used); after a call that stopped early it is cleared.
     bool use_dedup = true;
+    int group_mode = 1;  // DAGC_OPT_GROUP
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
     uint64_t table_cap = 0;  // slots, a power of two
@@ -371,7 +377,7 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
              uint64_t* keys_out, uint64_t* keys_alt, const uint32_t* vals_in, uint32_t* vals_out,
              uint32_t* vals_alt, bool with_values, uint64_t n_bound, const uint64_t* d_n, int lo, int hi,
              int validate_bits, cudaStream_t s, int hist_stage = -1, int pass_stage = -1,
-             const SegmentSpec* seg = nullptr) {
+             const SegmentSpec* seg = nullptr, const uint32_t* gate = nullptr, uint32_t gate_run = 0) {
     if (cs.next_hist >= kMaxSorts || cs.next_counter + kMaxPasses > kMaxTileCounters)
         return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many sorts in one call");
     SortArgs a{};
@@ -395,6 +401,8 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     const uint64_t tiles = sort_tiles(n_bound);
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
     a.shape = with_values ? ctx->shape_pairs : ctx->shape_keys;
+    a.gate = gate;
+    a.gate_run = gate_run;
     if (seg && seg->d_offsets) {
         a.seg_offsets = seg->d_offsets;
         a.seg_count = seg->count;
@@ -628,12 +636,13 @@ int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
         if (ctx->table) cudaFree(ctx->table);
         ctx->table = nullptr;
         ctx->table_cap = 0;
-        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 16));
+        // keys u64 | dedup aux u64 | grouping masks u64, per slot
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 24));
         ctx->table_cap = slots;
         ctx->table_dirty = true;
     }
     if (ctx->table_dirty) {
-        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 8, s));
+        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 24, s));
         ctx->table_dirty = false;
     }
     return DAGC_OK;
@@ -645,6 +654,7 @@ constexpr int kStatusFallback = -1000;
 
 int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
                     CreatePools& out, const BatchSpec* batch, bool use_dedup) {
+    const int group_mode = ctx->group_mode;
     const int nl = depth - 2;
     const int bits = 3 * depth;
     const CreateLayout Lo(n, depth, batch ? batch->k : 0u, use_dedup, ctx->dedup_unique_limit);
@@ -685,11 +695,57 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
         uint32_t* err = &cs.h->err;
 
-        // 1. Fragment sort on the brick key bits [6, 3*depth): only the order of
-        //    code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
+        int st = DAGC_OK;
+        // 1a. Fragment grouping by hash (group.cu): a sketch of the distinct
+        //     bricks picks, on the device, this path or the sort path 1b-2;
+        //     the kernels of the path not taken do nothing. Either path leaves
+        //     the sorted bricks in P, their leaf masks in LM and their count.
+        const uint32_t* gate = nullptr;
+        if (group_mode != 0 && use_dedup) {
+            StageTimer tg(ctx, DAGC_STAGE_GROUP, s);
+            GroupArgs g{};
+            g.frags = d_frag;
+            g.n = n;
+            g.seg_offsets = batch ? P64(Lo.o_seg_off) : nullptr;
+            g.seg_count = batch ? batch->k : 0u;
+            g.seg_shift = seg_shift;
+            g.seg_code = batch ? P64(Lo.o_seg_code) : nullptr;
+            g.validate_bits = validate;
+            g.mode = group_mode;
+            g.sketch = cs.h->sketch;
+            g.path = cs.h->path;
+            g.table_key = static_cast<uint64_t*>(ctx->table);
+            g.table_val = static_cast<uint64_t*>(ctx->table) + 2 * ctx->table_cap;
+            g.table_cap = ctx->table_cap;
+            g.bricks = P64(Lo.o_A);
+            g.slots = P32(Lo.o_M0);
+            g.cap = p0cap;
+            g.d_count = cs.count(kCntBricks);
+            g.sorted_bricks = P64(Lo.o_P);
+            g.sorted_slots = P32(Lo.o_M1);
+            g.parents = P64(Lo.o_P);
+            g.leaves = P64(Lo.o_LM);
+            g.err = err;
+            launch_group_front(g, s);
+            ctx->launches += 3;
+            DAGC_LAUNCHED(ctx);
+            // The bricks (B of them instead of N fragments), sorted with their slots.
+            st = run_sort(ctx, cs, sb, P64(Lo.o_A), P64(Lo.o_P), P64(Lo.o_B), P32(Lo.o_M0), P32(Lo.o_M1),
+                          P32(Lo.o_LM), true, p0cap, cs.count(kCntBricks), 0, sort_hi - 6, 0, s, -1, -1, nullptr,
+                          cs.h->path, 1u);
+            if (st) return st;
+            launch_group_gather(g, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
+            tg.stop();
+            gate = cs.h->path;
+        }
+
+        // 1b. Fragment sort on the brick key bits [6, 3*depth): only the order of
+        //     code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
         const SegmentSpec seg{batch ? P64(Lo.o_seg_off) : nullptr, batch ? batch->k : 0u, seg_shift};
-        int st = run_sort(ctx, cs, sb, d_frag, P64(Lo.o_A), P64(Lo.o_B), nullptr, nullptr, nullptr, false, n, nullptr,
-                          6, sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg);
+        st = run_sort(ctx, cs, sb, d_frag, P64(Lo.o_A), P64(Lo.o_B), nullptr, nullptr, nullptr, false, n, nullptr, 6,
+                      sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg, gate, 0u);
         if (st) return st;
 
         // 2. Fused unique + leaf build.
@@ -711,6 +767,8 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             a.tile_counter = cs.counter();
             a.err = err;
             a.grid = grid_for(ctx->grid_leaf / ctx->sms, ctx->sms, leaf_tiles(n));
+            a.gate = gate;
+            a.gate_run = 0u;
             launch_leaf_build(a, s);
             ctx->launches += 2;
             DAGC_LAUNCHED(ctx);
@@ -890,7 +948,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     return DAGC_OK;
     };
     int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u, use_dedup,
-                                       use_dedup ? ctx->table : nullptr},
+                                       use_dedup ? ctx->table : nullptr, use_dedup ? group_mode : 0},
                          s, enqueue);
     if (st) { ctx->table_dirty = true; return st; }
     CallHeader* hdr = reinterpret_cast<CallHeader*>(b + Lo.o_hdr);
@@ -909,6 +967,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // Algorithmic bytes: the minimum each stage must read and write.
         const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP, 16 * n + 16 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
         uint64_t lb = 0;
         for (int l = 0; l < nl; ++l) {
@@ -1332,6 +1391,7 @@ int dagc_context_create(int device, dagc_context* out) {
     }
     if (const char* g = std::getenv("DAGC_GRAPHS")) c->use_graphs = std::atoi(g) != 0;
     if (const char* d = std::getenv("DAGC_DEDUP")) c->use_dedup = std::atoi(d) != 0;
+    if (const char* gm = std::getenv("DAGC_GROUP")) c->group_mode = std::min(2, std::max(0, std::atoi(gm)));
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumSortShapes; ++sh) {
         c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
@@ -1356,6 +1416,7 @@ int dagc_context_create(int device, dagc_context* out) {
     c->grid_scan = std::max(1, occupancy_kernel(3)) * c->sms;
     c->grid_write = 8 * c->sms;
     dedup_configure(c->sms);
+    group_configure(c->sms);
     *out = c.release();
     return DAGC_OK;
 }
@@ -1447,7 +1508,7 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
 uint64_t dagc_create_footprint(uint64_t n, int depth) {
     if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
     const CreateLayout L(n, depth, 0, true);
-    return L.total + L.table_slots * 16;
+    return L.total + L.table_slots * 24;
 }
 
 int dagc_dag_num_levels(dagc_dag d, int* num_levels) {
@@ -1709,6 +1770,10 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
             return DAGC_OK;
         case DAGC_OPT_DEDUP:
             ctx->use_dedup = value != 0;
+            return DAGC_OK;
+        case DAGC_OPT_GROUP:
+            if (value < 0 || value > 2) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "group mode must be 0, 1 or 2");
+            ctx->group_mode = value;
             return DAGC_OK;
         case DAGC_OPT_DEDUP_UNIQUE_LIMIT:
             if (value < 1) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "limit must be positive");

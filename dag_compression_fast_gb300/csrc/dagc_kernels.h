@@ -56,6 +56,9 @@ struct SortArgs {
     uint32_t* err;
     int grid_hist, grid_pass; // persistent grid sizes
     int shape;                // digit-pass kernel shape, see sort_shape_*
+    // Gate: when non-null, every kernel of the sort does nothing unless
+    // *gate == gate_run (a path chosen on the device, see GroupArgs).
+    const uint32_t* gate; uint32_t gate_run;
     // Segmented input (batched chunks): when seg_offsets is non-null, the key at
     // position i of keys_in belongs to segment s with seg_offsets[s] <= i <
     // seg_offsets[s+1] (seg_count + 1 ascending entries) and is sorted as the
@@ -108,8 +111,33 @@ struct LeafBuildArgs {
     uint64_t* parents; uint64_t* leaves; uint64_t out_capacity; uint64_t* d_out_n;
     uint64_t* lead_or; uint64_t* lead_run;  // per tile: OR of keys continuing an earlier run, its run id
     uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
+    const uint32_t* gate; uint32_t gate_run;  // as in SortArgs
 };
 void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s);  // two launches (build + fix-up)
+
+// Fragment grouping by hash (group.cu): the same parents and leaf masks as
+// the fragment sort + leaf build, for inputs with many fragments per brick.
+constexpr double kGroupMinRedundancy = 8.0;  // fragments per distinct brick that make grouping pay
+constexpr int kGroupSketchRegs = 4096;
+constexpr uint64_t kGroupMaxSlots = 1ull << 22;  // keys + masks of 64 MB: the table stays in the L2
+struct GroupArgs {
+    const uint64_t* frags; uint64_t n;
+    const uint64_t* seg_offsets; uint32_t seg_count; int seg_shift;  // batched input (as in SortArgs)
+    const uint64_t* seg_code;                                         // chunk Morton index per segment
+    int validate_bits;
+    int mode;                  // 1: choose by the sketch, 2: always group (tests)
+    uint32_t* sketch;          // kGroupSketchRegs words, zero
+    uint32_t* path;            // written: [0] 1 grouping, 0 sort path; [1] log2 of the table slots used
+    uint64_t* table_key; uint64_t* table_val; uint64_t table_cap;  // both zero on entry, left zero
+    uint64_t* bricks; uint32_t* slots; uint64_t cap;               // brick list (unsorted)
+    uint64_t* d_count;         // bricks found
+    const uint64_t* sorted_bricks; const uint32_t* sorted_slots;   // after the brick sort
+    uint64_t* parents; uint64_t* leaves;
+    uint32_t* err;
+};
+void group_configure(int sms);
+void launch_group_front(const GroupArgs& a, cudaStream_t s);   // sketch, insert, collect: three launches
+void launch_group_gather(const GroupArgs& a, cudaStream_t s);  // one launch
 
 // Unique over (key, perm) sorted by key: uid = rank of the key among distinct
 // keys; map[perm[i]] = uid; for the first of each run, out_keys[uid] = key and

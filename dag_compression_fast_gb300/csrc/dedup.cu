@@ -24,7 +24,8 @@
 //                  representative's payload; the unique id goes to the slot;
 //   dedup_map      every item reads its unique id and representative through
 //                  its slot, duplicates are compared in full with their
-//                  representative (collision check), the slots are cleared.
+//                  representative (collision check), the slots' keys are
+//                  cleared (items sharing a slot still read its aux word).
 //
 // What the fixed sizes cannot hold (table, unique list, a bucket) sets
 // kErrFallback, and the caller reruns the call with the radix-sort form.

@@ -52,8 +52,10 @@ __device__ __forceinline__ uint32_t segment_from(const uint64_t* off, uint32_t c
 __global__ void __launch_bounds__(kSortThreads)
 radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t n_host, int lo_bit,
                 int hi_bit, int validate_bits, uint32_t* __restrict__ hist, uint32_t* status0,
-                uint32_t* err, const uint64_t* seg_offsets, uint32_t seg_count, int seg_shift) {
+                uint32_t* err, const uint64_t* seg_offsets, uint32_t seg_count, int seg_shift,
+                const uint32_t* gate, uint32_t gate_run) {
     __shared__ uint32_t s_hist[kMaxPasses][kRadix];
+    if (gate && *gate != gate_run) return;
     const uint64_t n = load_n(d_n, n_host);
     const int passes = sort_passes(lo_bit, hi_bit);
     for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
@@ -113,6 +115,8 @@ struct PassParams {
     const uint64_t* seg_offsets;  // first pass of a segmented sort only
     uint32_t seg_count;
     int seg_shift;
+    const uint32_t* gate;
+    uint32_t gate_run;
 };
 
 // Exclusive prefix of one digit over the tiles before `tile`: walks back over
@@ -195,6 +199,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (p.gate && *p.gate != p.gate_run) return;
     const uint64_t n64 = load_n(p.d_n, p.n_host);
     const uint32_t n = (uint32_t)n64;
     const uint32_t ntiles = (uint32_t)((n64 + kTile - 1) / kTile);
@@ -335,7 +340,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
 }
 
 __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin, uint32_t* vout,
-                          bool with_values, const uint64_t* d_n, uint64_t n_host) {
+                          bool with_values, const uint64_t* d_n, uint64_t n_host, const uint32_t* gate,
+                          uint32_t gate_run) {
+    if (gate && *gate != gate_run) return;
     const uint64_t n = load_n(d_n, n_host);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         out[i] = in[i];
@@ -412,6 +419,8 @@ static PassParams pass_params(const SortArgs& a, int i) {
     p.seg_offsets = i == 0 ? a.seg_offsets : nullptr;
     p.seg_count = a.seg_count;
     p.seg_shift = a.seg_shift;
+    p.gate = a.gate;
+    p.gate_run = a.gate_run;
     return p;
 }
 
@@ -420,10 +429,11 @@ void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
     // there is no digit to sort.
     radix_histogram<<<a.grid_hist, kSortThreads, 0, s>>>(a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
                                                          a.validate_bits, a.hist, a.status[0], a.err,
-                                                         a.seg_offsets, a.seg_count, a.seg_shift);
+                                                         a.seg_offsets, a.seg_count, a.seg_shift, a.gate,
+                                                         a.gate_run);
     if (sort_passes(a.lo_bit, a.hi_bit) == 0)
         copy_keys<<<a.grid_hist, 256, 0, s>>>(a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
-                                              a.d_n, a.n);
+                                              a.d_n, a.n, a.gate, a.gate_run);
 }
 
 void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {

@@ -168,6 +168,12 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
 /* Testing: caps the hash-set form's unique list at `value` keys per level, so
  * that larger levels take the rerun. */
 #define DAGC_OPT_DEDUP_UNIQUE_LIMIT 5
+/* How fragments are grouped into bricks (SortKeys + SelectUnique +
+ * ReduceByKey): 1 (default) choose on the device per call, from a sketch of
+ * the distinct bricks: a hash table when fragments hold >= 8 per brick on
+ * average, else the radix sort; 0 always the radix sort; 2 always the hash
+ * table. Results are identical. */
+#define DAGC_OPT_GROUP 6
 int dagc_set_option(dagc_context ctx, int option, int value);
 /* Calls of this context rerun in the radix form so far. */
 int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
@@ -186,7 +192,8 @@ int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
 #define DAGC_STAGE_MATERIALISE 5    /* copy of the level outputs into the DAG */
 #define DAGC_STAGE_FINAL 6          /* final word layout */
 #define DAGC_STAGE_MERGE 7          /* MergeDAGs */
-#define DAGC_NUM_STAGES 8
+#define DAGC_STAGE_GROUP 8          /* fragment grouping by hash: sketch, insert, brick sort, gather */
+#define DAGC_NUM_STAGES 9
 int dagc_profile_enable(dagc_context ctx, int enable);
 int dagc_profile_reset(dagc_context ctx);
 int dagc_profile_read(dagc_context ctx, int stage, double* device_ms, uint64_t* launches,

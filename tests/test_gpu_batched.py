@@ -48,6 +48,17 @@ def test_batched_equals_per_chunk_merge_and_whole_volume(ctx, chunk_depth, top_l
     assert_dag_equal(merged, whole)
 
 
+@pytest.mark.parametrize("mode", [0, 2])
+def test_batched_grouping_forms(mode):
+    chunks, morton = make_chunks(5, 2, 20, 6)
+    counts = np.array([c.size for c in chunks], np.uint64)
+    frag = np.concatenate(chunks)
+    whole = O.create_dag(global_codes(chunks, morton, 5), 7)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, mode)
+        assert_dag_equal(c.create_dag_batched(frag, counts, morton, 5, 2).to_host(), whole)
+
+
 def test_batched_generator_terrain_chunks(ctx):
     """A reduced config-4 layout: 4x4 terrain chunks of 256^3 with sponges."""
     codes, counts, morton = D.gen_batched(chunk_depth=8, grid_xz=4, chunk_row=1, seed=11,

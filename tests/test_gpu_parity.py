@@ -89,6 +89,29 @@ def test_radix_form_bit_exact(case):
         assert c.dedup_fallbacks() == 0
 
 
+@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("case", ["sphere_d7", "terrain_d8", "clustered_d10", "all_duplicates", "sparse_d21",
+                                  "depth2", "tiny_d3", "soup_d10"])
+def test_grouping_forms_bit_exact(mode, case):
+    """Fragments grouped by the radix sort (0) or by the hash table (2, forced
+    even where the sketch would not choose it) give the same DAG."""
+    codes, depth = CASES[case]()
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, mode)
+        dag = c.create_dag(codes, depth)
+        assert_dag_equal(dag.to_host(), O.create_dag(codes, depth))
+        w = c.create_final_dag(dag).to_numpy()
+        assert np.array_equal(decode_final(w, depth), np.unique(codes))
+
+
+def test_grouping_rejects_out_of_range_codes():
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, 2)
+        with pytest.raises(D.DagcError) as e:
+            c.create_dag(np.array([1, 2, 1 << 30], np.uint64), 9)  # 2^30 >= 8^9
+        assert e.value.status == D.ERR_BAD_INPUT
+
+
 def test_dedup_rerun_when_unique_list_is_full():
     """A level with more distinct hashes than the hash-set form holds is rerun
     in the radix form: same result, one rerun counted."""
