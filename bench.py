@@ -72,16 +72,27 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_pass_bytes(n_keys: int):
-    """DRAM bytes of one fragment-sort digit pass, from the committed ncu summary
-    (bytes per key, measured on a smaller case and scaled by the key count)."""
-    path = os.path.join(REPO, "profiles", "onesweep_pass_keys_20M_27bit.md")
+def profile_figure(name: str, key: str, scale: float):
+    """A per-item DRAM byte count from a committed ncu summary (measured on a
+    smaller case), scaled by the item count of this workload."""
+    path = os.path.join(REPO, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_key_per_pass:"):
-            return float(line.split(":")[1]) * n_keys
+        if line.startswith(key + ":"):
+            return float(line.split(":")[1]) * scale
     return None
+
+
+def stage_roofline(prof, stage, kernel, peak, peak_kind, traffic):
+    ms, launches, nbytes = prof[stage]
+    achieved = (nbytes / 1e9) / (ms / 1e3) if ms > 0 else 0.0
+    return {"kernel": kernel, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": nbytes // max(launches, 1),
+            "avg_launch_ms": ms / max(launches, 1), "launches": launches,
+            "timing": "CUDA events around each launch on the call's stream, over profiled steps run right "
+                      "after the timed region (same workload)"}
 
 
 class ClockSampler:
@@ -275,19 +286,33 @@ def main():
     e2e = {"value": n * args.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
            "d2h_bytes_per_step": 4 * int(nw.value)}
 
-    # ---- roofline of the dominant kernel: the fragment-sort digit pass ----
-    pass_ms, pass_launches, pass_bytes = prof["fragment_pass"]
+    # ---- roofline of the dominant kernel of the path the device chose ----
+    # Fragments with many per brick are grouped by a hash table (group_insert
+    # dominates); otherwise they are radix-sorted (the digit pass dominates).
     peak, peak_kind = measured_peaks()
-    achieved = (pass_bytes / 1e9) / (pass_ms / 1e3) if pass_ms > 0 else 0.0
-    per_launch_traffic = traffic_per_pass_bytes(n)
-    roofline = {"kernel": "onesweep_pass (fragment sort, 8-bit digit, keys only)", "bound": "hbm",
-                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": per_launch_traffic,
-                "algorithmic_bytes_per_launch": pass_bytes // max(pass_launches, 1),
-                "avg_launch_ms": pass_ms / max(pass_launches, 1), "launches": pass_launches,
-                "timing": "CUDA events around each launch on the call's stream, over --steps profiled "
-                          "steps run right after the timed region (same workload)"}
+    pass_traffic = profile_figure("onesweep_pass_keys_20M_27bit.md", "dram_bytes_per_key_per_pass", n)
+    if prof["group_insert"][0] > prof["fragment_pass"][0]:
+        roofline = stage_roofline(prof, "group_insert",
+                                  "group_insert (fragment grouping: table probe + atomicOr in the L2)", peak,
+                                  peak_kind, profile_figure("group_insert_terrain_d10.md",
+                                                            "dram_bytes_per_fragment", n))
+        # The radix-sort path's digit pass on the same fragments, for reference
+        # (it serves inputs with few fragments per brick).
+        ctx.set_option(D.OPT_GROUP, 0)
+        ctx.profile(True)
+        ctx.profile_reset()
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        ctx.profile(False)
+        ctx.set_option(D.OPT_GROUP, 1)
+        sort_prof = ctx.profile_read()
+        roofline_sort = stage_roofline(sort_prof, "fragment_pass", "onesweep_pass (fragment sort, 8-bit digit, "
+                                       "keys only; sort path forced)", peak, peak_kind, pass_traffic)
+    else:
+        roofline = stage_roofline(prof, "fragment_pass", "onesweep_pass (fragment sort, 8-bit digit, keys only)",
+                                  peak, peak_kind, pass_traffic)
+        roofline_sort = None
     stages = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
                   "gbs": round((v[2] / 1e9) / (v[0] / 1e3), 1) if v[0] > 0 and v[2] else None}
               for k, v in prof.items() if v[1]}
@@ -304,6 +329,8 @@ def main():
         "gpu_launches": int(launches),
         "stages": stages,
     }
+    if roofline_sort:
+        line["roofline_sort_pass"] = roofline_sort
     if clocks:
         line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

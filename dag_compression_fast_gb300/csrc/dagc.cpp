@@ -209,14 +209,14 @@ struct dagc_context_t {
     int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
     DevicePool pool;
     Arena arena;
-    // Hash table shared by the fragment grouping and the dedup: keys (0 =
-    // empty), then the dedup's aux words, then the grouping's masks. Keys and
-    // masks are zero between uses (every level and the grouping clear the
-    // slots they used); after a call that stopped early it is cleared.
+    // Dedup table: keys (0 = empty), then aux words; every level leaves its
+    // keys zero. Grouping table: kGroupMaxSlots keys then as many masks, left
+    // zero by the gather. After a call that stopped early both are cleared.
     bool use_dedup = true;
     int group_mode = 1;  // DAGC_OPT_GROUP
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
+    void* gtable = nullptr;  // fragment grouping table
     uint64_t table_cap = 0;  // slots, a power of two
     bool table_dirty = true;
     uint64_t fallbacks = 0;  // calls rerun with the radix form
@@ -636,14 +636,18 @@ int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
         if (ctx->table) cudaFree(ctx->table);
         ctx->table = nullptr;
         ctx->table_cap = 0;
-        // keys u64 | dedup aux u64 | grouping masks u64, per slot
-        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 24));
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 16));  // keys u64 | aux u64
         ctx->table_cap = slots;
         ctx->table_dirty = true;
     }
     if (ctx->table_dirty) {
-        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 24, s));
+        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 8, s));
+        if (ctx->gtable) DAGC_CUDA(ctx, cudaMemsetAsync(ctx->gtable, 0, kGroupMaxSlots * 16, s));
         ctx->table_dirty = false;
+    }
+    if (!ctx->gtable && ctx->group_mode != 0) {
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->gtable, kGroupMaxSlots * 16));
+        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->gtable, 0, kGroupMaxSlots * 16, s));
     }
     return DAGC_OK;
 }
@@ -701,8 +705,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         //     the kernels of the path not taken do nothing. Either path leaves
         //     the sorted bricks in P, their leaf masks in LM and their count.
         const uint32_t* gate = nullptr;
-        if (group_mode != 0 && use_dedup) {
-            StageTimer tg(ctx, DAGC_STAGE_GROUP, s);
+        if (group_mode != 0 && use_dedup && ctx->gtable) {
             GroupArgs g{};
             g.frags = d_frag;
             g.n = n;
@@ -714,9 +717,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.mode = group_mode;
             g.sketch = cs.h->sketch;
             g.path = cs.h->path;
-            g.table_key = static_cast<uint64_t*>(ctx->table);
-            g.table_val = static_cast<uint64_t*>(ctx->table) + 2 * ctx->table_cap;
-            g.table_cap = ctx->table_cap;
+            g.table = static_cast<uint64_t*>(ctx->gtable);
             g.bricks = P64(Lo.o_A);
             g.slots = P32(Lo.o_M0);
             g.cap = p0cap;
@@ -726,8 +727,19 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.parents = P64(Lo.o_P);
             g.leaves = P64(Lo.o_LM);
             g.err = err;
-            launch_group_front(g, s);
-            ctx->launches += 3;
+            {
+                StageTimer t1(ctx, DAGC_STAGE_GROUP_SKETCH, s);
+                launch_group_sketch(g, s);
+                ++ctx->launches;
+                t1.stop();
+                StageTimer t2(ctx, DAGC_STAGE_GROUP_INSERT, s);
+                launch_group_insert(g, s);
+                ++ctx->launches;
+                t2.stop();
+            }
+            StageTimer tg(ctx, DAGC_STAGE_GROUP, s);
+            launch_group_collect(g, s);
+            ++ctx->launches;
             DAGC_LAUNCHED(ctx);
             // The bricks (B of them instead of N fragments), sorted with their slots.
             st = run_sort(ctx, cs, sb, P64(Lo.o_A), P64(Lo.o_P), P64(Lo.o_B), P32(Lo.o_M0), P32(Lo.o_M1),
@@ -967,7 +979,12 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // Algorithmic bytes: the minimum each stage must read and write.
         const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
-        set_pending_bytes(ctx, DAGC_STAGE_GROUP, 16 * n + 16 * p0);
+        // Grouping: each pass over the fragments reads 8 bytes per fragment
+        // (the table stays in the L2); the brick list, its sort and the
+        // gather move ~60 bytes per brick.
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SKETCH, 8 * n);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_INSERT, 8 * n);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP, 60 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
         uint64_t lb = 0;
         for (int l = 0; l < nl; ++l) {
@@ -1431,6 +1448,7 @@ void dagc_context_destroy(dagc_context ctx) {
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     ctx->arena.release();
     if (ctx->table) cudaFree(ctx->table);
+    if (ctx->gtable) cudaFree(ctx->gtable);
     if (ctx->trace_err) cudaFree(ctx->trace_err);
     if (ctx->vox_scratch) cudaFree(ctx->vox_scratch);
     ctx->pool.trim();
@@ -1508,7 +1526,7 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
 uint64_t dagc_create_footprint(uint64_t n, int depth) {
     if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
     const CreateLayout L(n, depth, 0, true);
-    return L.total + L.table_slots * 24;
+    return L.total + L.table_slots * 16 + kGroupMaxSlots * 16;
 }
 
 int dagc_dag_num_levels(dagc_dag d, int* num_levels) {
@@ -1700,7 +1718,9 @@ int dagc_free_all(dagc_context ctx) {
     drop_graphs(ctx);
     ctx->arena.release();
     if (ctx->table) cudaFree(ctx->table);
+    if (ctx->gtable) cudaFree(ctx->gtable);
     ctx->table = nullptr;
+    ctx->gtable = nullptr;
     ctx->table_cap = 0;
     ctx->table_dirty = true;
     ctx->pool.trim();

@@ -128,7 +128,7 @@ struct GroupArgs {
     int mode;                  // 1: choose by the sketch, 2: always group (tests)
     uint32_t* sketch;          // kGroupSketchRegs words, zero
     uint32_t* path;            // written: [0] 1 grouping, 0 sort path; [1] log2 of the table slots used
-    uint64_t* table_key; uint64_t* table_val; uint64_t table_cap;  // both zero on entry, left zero
+    uint64_t* table;           // keys (brick + 1) then masks, kGroupMaxSlots each; zero on entry, left zero
     uint64_t* bricks; uint32_t* slots; uint64_t cap;               // brick list (unsorted)
     uint64_t* d_count;         // bricks found
     const uint64_t* sorted_bricks; const uint32_t* sorted_slots;   // after the brick sort
@@ -136,7 +136,9 @@ struct GroupArgs {
     uint32_t* err;
 };
 void group_configure(int sms);
-void launch_group_front(const GroupArgs& a, cudaStream_t s);   // sketch, insert, collect: three launches
+void launch_group_sketch(const GroupArgs& a, cudaStream_t s);
+void launch_group_insert(const GroupArgs& a, cudaStream_t s);   // also picks the path
+void launch_group_collect(const GroupArgs& a, cudaStream_t s);
 void launch_group_gather(const GroupArgs& a, cudaStream_t s);  // one launch
 
 // Unique over (key, perm) sorted by key: uid = rank of the key among distinct

@@ -19,9 +19,10 @@
 //   group_gather  leaf masks read from the slots in sorted brick order,
 //                 parents written, slots cleared.
 //
-// The table is the dedup table's key array (zero on entry and on exit) with a
-// mask array of its own beside it, zero on entry and left zero by the gather
-// (each slot once).
+// The table holds kGroupMaxSlots keys (brick + 1) and, beside them,
+// kGroupMaxSlots masks; zero on entry, and left zero by the gather (each used
+// slot once). (Reading key and mask together, to skip the OR of a bit already
+// set, measured slower: the reads, not the fire-and-forget ORs, bound it.)
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
@@ -86,6 +87,7 @@ __global__ void __launch_bounds__(256) group_sketch(GroupArgs a) {
 
 constexpr int kIlp = 4;
 
+
 // Distinct-brick estimate from the sketch (HyperLogLog with the linear
 // counting correction for small counts); the whole CTA takes part.
 __device__ double sketch_estimate(const uint32_t* sketch, double* red) {
@@ -120,19 +122,14 @@ __global__ void __launch_bounds__(256) group_insert(GroupArgs a) {
     // and ~2.5 slots per estimated brick fit the table and the L2 (random
     // atomics on a table in HBM are slower than the sort).
     uint64_t S = 1024;
-    while ((double)S < 2.5 * est + 1.0 && S < a.table_cap) S <<= 1;
+    while ((double)S < 2.5 * est + 1.0 && S < kGroupMaxSlots) S <<= 1;
     const bool group = a.mode == 2 ||
-                       (a.mode == 1 && est * kGroupMinRedundancy <= (double)a.n && (double)S >= 2.5 * est &&
-                        S <= a.table_cap && S <= kGroupMaxSlots);
+                       (a.mode == 1 && est * kGroupMinRedundancy <= (double)a.n && (double)S >= 2.5 * est);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.path[0] = group ? 1u : 0u;
         a.path[1] = (uint32_t)(63 - __clzll(S));
     }
     if (!group) return;
-    if (S > a.table_cap) {  // forced grouping that cannot fit: rerun
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrFallback);
-        return;
-    }
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t warps = gsize / 32, warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
@@ -159,11 +156,10 @@ __global__ void __launch_bounds__(256) group_insert(GroupArgs a) {
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
                 if (!live[k]) continue;
-                uint64_t cur = ld_relaxed(a.table_key + s[k]);
-                if (cur == 0)
-                    cur = atomicCAS((unsigned long long*)(a.table_key + s[k]), 0ull, (unsigned long long)key[k]);
+                uint64_t cur = ld_relaxed(a.table + s[k]);
+                if (cur == 0) cur = atomicCAS((unsigned long long*)(a.table + s[k]), 0ull, (unsigned long long)key[k]);
                 if (cur == 0 || cur == key[k]) {
-                    atomicOr((unsigned long long*)(a.table_val + s[k]), (unsigned long long)bit[k]);
+                    atomicOr((unsigned long long*)(a.table + kGroupMaxSlots + s[k]), (unsigned long long)bit[k]);
                     live[k] = false;
                 } else {
                     s[k] = (s[k] + 1) & (S - 1);
@@ -187,7 +183,7 @@ __global__ void __launch_bounds__(256) group_collect(GroupArgs a) {
     __shared__ uint64_t scan[34];
     __shared__ uint64_t base_s;
     if (a.path[0] != 1u) return;
-    const uint64_t S = (1ull << a.path[1]) < a.table_cap ? (1ull << a.path[1]) : a.table_cap;
+    const uint64_t S = (1ull << a.path[1]) < kGroupMaxSlots ? (1ull << a.path[1]) : kGroupMaxSlots;
     const uint64_t tile = 256ull * kCollectItems;
     for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < S; t0 += (uint64_t)gridDim.x * tile) {
         const uint64_t s0 = t0 + (uint64_t)threadIdx.x * kCollectItems;
@@ -195,7 +191,7 @@ __global__ void __launch_bounds__(256) group_collect(GroupArgs a) {
         uint64_t cnt = 0;
 #pragma unroll
         for (int j = 0; j < kCollectItems; ++j) {
-            key[j] = s0 + j < S ? a.table_key[s0 + j] : 0;
+            key[j] = s0 + j < S ? a.table[s0 + j] : 0;
             cnt += key[j] != 0;
         }
         uint64_t total;
@@ -234,7 +230,7 @@ __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
             b[k] = i < count ? a.sorted_bricks[i] : 0;
         }
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) m[k] = s[k] < a.table_cap ? a.table_val[s[k]] : 0;
+        for (int k = 0; k < kIlp; ++k) m[k] = s[k] < kGroupMaxSlots ? a.table[kGroupMaxSlots + s[k]] : 0;
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
             const uint64_t i = i0 + k * stride;
@@ -245,9 +241,9 @@ __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
             if (a.seg_code) parent = (__ldg(a.seg_code + (b[k] >> (a.seg_shift - 6))) << (a.seg_shift - 6)) | (b[k] & lmask);
             a.parents[i] = parent;
             a.leaves[i] = m[k];
-            if (s[k] < a.table_cap) {
-                a.table_key[s[k]] = 0;  // leave the table empty
-                a.table_val[s[k]] = 0;
+            if (s[k] < kGroupMaxSlots) {
+                a.table[s[k]] = 0;  // leave the table empty
+                a.table[kGroupMaxSlots + s[k]] = 0;
             }
         }
     }
@@ -259,13 +255,13 @@ int g_group_sms = 152;
 
 void group_configure(int sms) { g_group_sms = sms > 0 ? sms : 152; }
 
-void launch_group_front(const GroupArgs& a, cudaStream_t s) {
+static int front_grid(const GroupArgs& a) {
     const uint64_t want = (a.n + 1023) / 1024;
-    const int g = (int)(want < (uint64_t)(8 * g_group_sms) ? (want > 0 ? want : 1) : 8 * g_group_sms);
-    group_sketch<<<g, 256, 0, s>>>(a);
-    group_insert<<<g, 256, 0, s>>>(a);
-    group_collect<<<8 * g_group_sms, 256, 0, s>>>(a);
+    return (int)(want < (uint64_t)(8 * g_group_sms) ? (want > 0 ? want : 1) : 8 * g_group_sms);
 }
+void launch_group_sketch(const GroupArgs& a, cudaStream_t s) { group_sketch<<<front_grid(a), 256, 0, s>>>(a); }
+void launch_group_insert(const GroupArgs& a, cudaStream_t s) { group_insert<<<front_grid(a), 256, 0, s>>>(a); }
+void launch_group_collect(const GroupArgs& a, cudaStream_t s) { group_collect<<<8 * g_group_sms, 256, 0, s>>>(a); }
 
 void launch_group_gather(const GroupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.cap + 1023) / 1024;
