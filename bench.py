@@ -287,15 +287,24 @@ def main():
            "d2h_bytes_per_step": 4 * int(nw.value)}
 
     # ---- roofline of the dominant kernel of the path the device chose ----
-    # Fragments with many per brick are grouped by a hash table (group_insert
-    # dominates); otherwise they are radix-sorted (the digit pass dominates).
+    # Fragments with many per brick are grouped by hash (partition scatter +
+    # per-partition tables); otherwise they are radix-sorted (the digit pass
+    # dominates).
     peak, peak_kind = measured_peaks()
     pass_traffic = profile_figure("onesweep_pass_keys_20M_27bit.md", "dram_bytes_per_key_per_pass", n)
-    if prof["group_insert"][0] > prof["fragment_pass"][0]:
-        roofline = stage_roofline(prof, "group_insert",
-                                  "group_insert (fragment grouping: table probe + atomicOr in the L2)", peak,
-                                  peak_kind, profile_figure("group_insert_terrain_d10.md",
-                                                            "dram_bytes_per_fragment", n))
+    group_kernels = {
+        "group_sketch": ("group_sketch + group_plan (sketch and partition counts, one read)",
+                         "group_sketch_terrain_d11.md"),
+        "group_scatter": ("group_scatter (fragments by partition: one read, one write)",
+                          "group_scatter_terrain_d11.md"),
+        "group_aggregate": ("group_aggregate (per-partition tables in shared memory: one read)",
+                            "group_aggregate_terrain_d11.md"),
+    }
+    top = max(group_kernels, key=lambda k: prof[k][0])
+    if prof[top][0] > prof["fragment_pass"][0]:
+        label, prof_file = group_kernels[top]
+        roofline = stage_roofline(prof, top, label, peak, peak_kind,
+                                  profile_figure(prof_file, "dram_bytes_per_fragment", n))
         # The radix-sort path's digit pass on the same fragments, for reference
         # (it serves inputs with few fragments per brick).
         ctx.set_option(D.OPT_GROUP, 0)

@@ -63,7 +63,7 @@ DAGC_SYMBOLS = [
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
-          "final", "merge", "group", "group_sketch", "group_insert"]
+          "final", "merge", "group", "group_sketch", "group_aggregate", "group_scatter"]
 GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
                "dagc_gen_triangle_soup", "dagc_gen_soup_triangles", "dagc_gen_batched"]
 

@@ -52,7 +52,9 @@ struct CallHeader {
     uint32_t hist[kMaxSorts][kMaxPasses * 256];
     DedupState dedup[kMaxDepth + 1];  // leaves + one per level
     uint32_t sketch[kGroupSketchRegs];  // distinct-brick sketch of the fragment grouping
-    uint32_t path[2];                   // 1: fragments grouped by hash, 0: sorted; log2 table slots
+    uint64_t ghist[kGroupMaxParts];     // its fragment counts per fine partition
+    uint64_t gcursor[kGroupMaxParts];   // its partition starts, then ends
+    uint32_t path[4];                   // [0] 1: fragments grouped by hash, 0: sorted; [1], [2] its shape
 };
 static_assert(kCntSlots <= 64, "count slots");
 
@@ -210,13 +212,13 @@ struct dagc_context_t {
     DevicePool pool;
     Arena arena;
     // Dedup table: keys (0 = empty), then aux words; every level leaves its
-    // keys zero. Grouping table: kGroupMaxSlots keys then as many masks, left
-    // zero by the gather. After a call that stopped early both are cleared.
+    // keys zero; after a call that stopped early it is cleared. Grouping
+    // scratch (kGroupScratchBytes): the brick masks.
     bool use_dedup = true;
     int group_mode = 1;  // DAGC_OPT_GROUP
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
-    void* gtable = nullptr;  // fragment grouping table
+    void* gtable = nullptr;  // fragment grouping scratch
     uint64_t table_cap = 0;  // slots, a power of two
     bool table_dirty = true;
     uint64_t fallbacks = 0;  // calls rerun with the radix form
@@ -642,13 +644,9 @@ int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
     }
     if (ctx->table_dirty) {
         DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 8, s));
-        if (ctx->gtable) DAGC_CUDA(ctx, cudaMemsetAsync(ctx->gtable, 0, kGroupMaxSlots * 16, s));
         ctx->table_dirty = false;
     }
-    if (!ctx->gtable && ctx->group_mode != 0) {
-        DAGC_CUDA(ctx, cudaMalloc(&ctx->gtable, kGroupMaxSlots * 16));
-        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->gtable, 0, kGroupMaxSlots * 16, s));
-    }
+    if (!ctx->gtable && ctx->group_mode != 0) DAGC_CUDA(ctx, cudaMalloc(&ctx->gtable, kGroupScratchBytes));
     return DAGC_OK;
 }
 
@@ -715,35 +713,42 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.seg_code = batch ? P64(Lo.o_seg_code) : nullptr;
             g.validate_bits = validate;
             g.mode = group_mode;
+            g.chunks = group_chunks(n);
             g.sketch = cs.h->sketch;
+            g.hist = cs.h->ghist;
+            g.cursor = cs.h->gcursor;
             g.path = cs.h->path;
-            g.table = static_cast<uint64_t*>(ctx->gtable);
+            g.parts = P64(Lo.o_B);
             g.bricks = P64(Lo.o_A);
-            g.slots = P32(Lo.o_M0);
-            g.cap = p0cap;
+            g.idx = P32(Lo.o_M0);
+            g.masks = static_cast<uint64_t*>(ctx->gtable);
+            g.cap = std::min<uint64_t>(p0cap, kGroupMaxBricks);
             g.d_count = cs.count(kCntBricks);
             g.sorted_bricks = P64(Lo.o_P);
-            g.sorted_slots = P32(Lo.o_M1);
+            g.sorted_idx = P32(Lo.o_M1);
             g.parents = P64(Lo.o_P);
             g.leaves = P64(Lo.o_LM);
             g.err = err;
             {
                 StageTimer t1(ctx, DAGC_STAGE_GROUP_SKETCH, s);
                 launch_group_sketch(g, s);
-                ++ctx->launches;
+                launch_group_plan(g, s);
+                ctx->launches += 2;
                 t1.stop();
-                StageTimer t2(ctx, DAGC_STAGE_GROUP_INSERT, s);
-                launch_group_insert(g, s);
+                StageTimer t2(ctx, DAGC_STAGE_GROUP_SCATTER, s);
+                launch_group_scatter(g, s);
                 ++ctx->launches;
                 t2.stop();
+                StageTimer t3(ctx, DAGC_STAGE_GROUP_AGGREGATE, s);
+                launch_group_aggregate(g, s);
+                ++ctx->launches;
+                t3.stop();
             }
-            StageTimer tg(ctx, DAGC_STAGE_GROUP, s);
-            launch_group_collect(g, s);
-            ++ctx->launches;
             DAGC_LAUNCHED(ctx);
-            // The bricks (B of them instead of N fragments), sorted with their slots.
+            StageTimer tg(ctx, DAGC_STAGE_GROUP, s);
+            // The bricks (B of them instead of N fragments), sorted with their indices.
             st = run_sort(ctx, cs, sb, P64(Lo.o_A), P64(Lo.o_P), P64(Lo.o_B), P32(Lo.o_M0), P32(Lo.o_M1),
-                          P32(Lo.o_LM), true, p0cap, cs.count(kCntBricks), 0, sort_hi - 6, 0, s, -1, -1, nullptr,
+                          P32(Lo.o_LM), true, g.cap, cs.count(kCntBricks), 0, sort_hi - 6, 0, s, -1, -1, nullptr,
                           cs.h->path, 1u);
             if (st) return st;
             launch_group_gather(g, s);
@@ -979,11 +984,12 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // Algorithmic bytes: the minimum each stage must read and write.
         const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
-        // Grouping: each pass over the fragments reads 8 bytes per fragment
-        // (the table stays in the L2); the brick list, its sort and the
-        // gather move ~60 bytes per brick.
+        // Grouping: the sketch and the aggregation read 8 bytes per fragment,
+        // the scatter reads and writes 8; the brick sort and the gather move
+        // ~60 bytes per brick.
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_SKETCH, 8 * n);
-        set_pending_bytes(ctx, DAGC_STAGE_GROUP_INSERT, 8 * n);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, 16 * n);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, 8 * n + 20 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP, 60 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
         uint64_t lb = 0;
@@ -1526,7 +1532,7 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
 uint64_t dagc_create_footprint(uint64_t n, int depth) {
     if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
     const CreateLayout L(n, depth, 0, true);
-    return L.total + L.table_slots * 16 + kGroupMaxSlots * 16;
+    return L.total + L.table_slots * 16 + kGroupScratchBytes;
 }
 
 int dagc_dag_num_levels(dagc_dag d, int* num_levels) {

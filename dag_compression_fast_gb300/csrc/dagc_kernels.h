@@ -119,27 +119,41 @@ void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s);  // two launches
 // the fragment sort + leaf build, for inputs with many fragments per brick.
 constexpr double kGroupMinRedundancy = 8.0;  // fragments per distinct brick that make grouping pay
 constexpr int kGroupSketchRegs = 4096;
-constexpr uint64_t kGroupMaxSlots = 1ull << 22;  // keys + masks of 64 MB: the table stays in the L2
+constexpr int kGroupPartLog = 11;                        // fine partitions counted by the sketch pass
+constexpr int kGroupMaxParts = 1 << kGroupPartLog;
+constexpr int kGroupPartSlotsLog = 12;                   // shared-memory table of one partition
+constexpr int kGroupPartSlots = 1 << kGroupPartSlotsLog;
+constexpr double kGroupBricksPerPart = 384.0;            // partition count target: estimate / this
+constexpr double kGroupMaxBricksPerPart = 0.45 * kGroupPartSlots;  // beyond this, the sort path
+constexpr uint64_t kGroupMaxPartFrags = 1ull << 18;      // one CTA reads one partition
+constexpr uint64_t kGroupMaxBricks = (uint64_t)kGroupMaxParts * kGroupPartSlots;
+constexpr int kGroupMaxChunks = 512;                     // CTAs of the sketch and scatter passes
+constexpr uint64_t kGroupScratchBytes = kGroupMaxBricks * 8;  // the brick masks
 struct GroupArgs {
     const uint64_t* frags; uint64_t n;
     const uint64_t* seg_offsets; uint32_t seg_count; int seg_shift;  // batched input (as in SortArgs)
     const uint64_t* seg_code;                                         // chunk Morton index per segment
     int validate_bits;
     int mode;                  // 1: choose by the sketch, 2: always group (tests)
+    int chunks;                // CTAs of the scatter: chunk c = [c*L, (c+1)*L), L = ceil(n / chunks)
     uint32_t* sketch;          // kGroupSketchRegs words, zero
-    uint32_t* path;            // written: [0] 1 grouping, 0 sort path; [1] log2 of the table slots used
-    uint64_t* table;           // keys (brick + 1) then masks, kGroupMaxSlots each; zero on entry, left zero
-    uint64_t* bricks; uint32_t* slots; uint64_t cap;               // brick list (unsorted)
+    uint64_t* hist;            // kGroupMaxParts fragment counts per fine partition, zero
+    uint64_t* cursor;          // kGroupMaxParts: partition starts (plan), then ends (scatter)
+    uint32_t* path;            // [0] 1 grouping, 0 sort path; [1] log2 partitions; [2] log2 table slots
+    uint64_t* parts;           // n: fragment keys by partition
+    uint64_t* bricks; uint32_t* idx; uint64_t* masks; uint64_t cap;  // brick list (unsorted), masks[idx]
     uint64_t* d_count;         // bricks found
-    const uint64_t* sorted_bricks; const uint32_t* sorted_slots;   // after the brick sort
+    const uint64_t* sorted_bricks; const uint32_t* sorted_idx;      // after the brick sort
     uint64_t* parents; uint64_t* leaves;
     uint32_t* err;
 };
 void group_configure(int sms);
+int group_chunks(uint64_t n);                                      // `chunks` for n fragments
 void launch_group_sketch(const GroupArgs& a, cudaStream_t s);
-void launch_group_insert(const GroupArgs& a, cudaStream_t s);   // also picks the path
-void launch_group_collect(const GroupArgs& a, cudaStream_t s);
-void launch_group_gather(const GroupArgs& a, cudaStream_t s);  // one launch
+void launch_group_plan(const GroupArgs& a, cudaStream_t s);      // picks the path
+void launch_group_scatter(const GroupArgs& a, cudaStream_t s);
+void launch_group_aggregate(const GroupArgs& a, cudaStream_t s);
+void launch_group_gather(const GroupArgs& a, cudaStream_t s);
 
 // Unique over (key, perm) sorted by key: uid = rank of the key among distinct
 // keys; map[perm[i]] = uid; for the first of each run, out_keys[uid] = key and

@@ -4,25 +4,32 @@
 // the same arrays: the distinct bricks (code >> 6) in ascending order and,
 // per brick, the OR of 1 << (code & 63) over its fragments.
 //
-//   group_sketch  one read of the fragments: range check and a HyperLogLog
-//                 sketch (4096 registers) of the distinct bricks;
-//   group_insert  estimates the distinct bricks B from the sketch and picks
-//                 the path: grouping when the fragments hold at least
-//                 kGroupMinRedundancy per brick and a table of ~2.5 B slots
-//                 fits, else the sort path (every kernel of the other path
-//                 reads the decision and does nothing). Grouping: each
-//                 fragment finds or claims its brick's slot (linear probing,
-//                 atomicCAS) and ORs its bit into the slot's mask;
-//   group_collect the occupied slots become the brick list (brick, slot);
-//   (then the brick list is sorted by brick with the radix sort, values =
-//    slots: B items instead of N)
-//   group_gather  leaf masks read from the slots in sorted brick order,
-//                 parents written, slots cleared.
+// Bricks are split into partitions by the top bits of a hash of the brick, so
+// that one partition's distinct bricks fit a table in shared memory:
 //
-// The table holds kGroupMaxSlots keys (brick + 1) and, beside them,
-// kGroupMaxSlots masks; zero on entry, and left zero by the gather (each used
-// slot once). (Reading key and mask together, to skip the OR of a bit already
-// set, measured slower: the reads, not the fire-and-forget ORs, bound it.)
+//   group_sketch     one read of the fragments: range check, a HyperLogLog
+//                    sketch (4096 registers) of the distinct bricks, and the
+//                    fragment count of each of 2048 fine partitions;
+//   group_plan       one CTA: estimates the distinct bricks B from the sketch
+//                    and picks the path: grouping when the fragments hold at
+//                    least kGroupMinRedundancy per brick and B fits the
+//                    partition tables, else the sort path (every kernel of the
+//                    other path reads the decision and does nothing). Picks
+//                    2^k partitions (B / 384 bricks each) and their starts;
+//   group_scatter    the fragments, by partition: one CTA per SM walks its
+//                    chunk of the input in tiles of 8192 (the next tile
+//                    streams into shared memory while one is processed), a
+//                    counting sort per tile in shared memory, one atomic per
+//                    partition and tile reserves the tile's runs;
+//   group_aggregate  one CTA per partition: a table in shared memory of the
+//                    partition's bricks and their masks, then the brick list
+//                    (brick, index) and the masks;
+//   (then the brick list is sorted by brick with the radix sort, values =
+//    indices: B items instead of N)
+//   group_gather     parents and masks in sorted brick order.
+//
+// Every pass over the fragments reads or writes them in order (8 bytes per
+// fragment and pass); only the B-sized brick list is sorted.
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
@@ -40,6 +47,11 @@ __device__ __forceinline__ uint64_t fmix(uint64_t k) {
     return k;
 }
 
+// One hash per brick, used three ways: top 12 bits pick the sketch register
+// (the bits below give its rank), top kGroupPartLog bits the fine partition,
+// low bits the slot in the partition's table.
+__device__ __forceinline__ uint64_t brick_hash(uint64_t brick) { return fmix(brick ^ 0x9E3779B97F4A7C15ull); }
+
 __device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t count, uint64_t i) {
     uint32_t lo = 0, hi = count;  // off[lo] <= i < off[hi]
     while (hi - lo > 1) {
@@ -49,53 +61,71 @@ __device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t cou
     return lo;
 }
 
-// Brick key of fragment i: code >> 6, or for batched input the composite
-// ((segment << seg_shift) | local) >> 6. `bad` flags codes out of range.
-__device__ __forceinline__ uint64_t brick_of(const GroupArgs& a, uint64_t i, uint64_t code, bool* bad) {
+// Key of fragment i: the code, or for batched input the composite
+// (segment << seg_shift) | local code. `bad` flags codes out of range.
+__device__ __forceinline__ uint64_t key_of(const GroupArgs& a, uint64_t i, uint64_t code, bool* bad) {
     if (a.validate_bits > 0 && a.validate_bits < 64 && (code >> a.validate_bits)) *bad = true;
     if (a.seg_offsets) code |= (uint64_t)segment_of(a.seg_offsets, a.seg_count, i) << a.seg_shift;
-    return code >> 6;
+    return code;
+}
+
+__device__ __forceinline__ void chunk_range(const GroupArgs& a, uint64_t* lo, uint64_t* hi) {
+    const uint64_t len = (a.n + a.chunks - 1) / a.chunks;
+    const uint64_t l = (uint64_t)blockIdx.x * len;
+    *lo = l < a.n ? l : a.n;
+    *hi = *lo + len < a.n ? *lo + len : a.n;
 }
 
 constexpr int kSketchLog = 12;
 constexpr int kSketchRegs = 1 << kSketchLog;
+static_assert(kSketchRegs == kGroupSketchRegs, "sketch size");
+constexpr int kFrontThreads = 512;
+constexpr int kSketchIlp = 8;
 
-__global__ void __launch_bounds__(256) group_sketch(GroupArgs a) {
+__global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
     __shared__ uint32_t reg[kSketchRegs];
+    __shared__ uint32_t hist[kGroupMaxParts];
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) reg[i] = 0;
+    for (int i = threadIdx.x; i < kGroupMaxParts; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     bool bad = false;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += 4 * stride) {
-        uint64_t c[4];
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += kSketchIlp * stride) {
+        uint64_t c[kSketchIlp];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) c[u] = i0 + u * stride < a.n ? __ldg(a.frags + i0 + u * stride) : 0;
+        for (int u = 0; u < kSketchIlp; ++u) {
+            const uint64_t i = i0 + u * stride;
+            c[u] = i < a.n ? __ldcs(a.frags + i) : 0;
+        }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (i0 + u * stride >= a.n) continue;
-            const uint64_t h = fmix(brick_of(a, i0 + u * stride, c[u], &bad) ^ 0x9E3779B97F4A7C15ull);
-            const uint32_t idx = (uint32_t)(h >> (64 - kSketchLog));
+        for (int u = 0; u < kSketchIlp; ++u) {
+            const uint64_t i = i0 + u * stride;
+            if (i >= a.n) continue;
+            const uint64_t h = brick_hash(key_of(a, i, c[u], &bad) >> 6);
             const uint32_t rank = (uint32_t)__clzll((h << kSketchLog) | (1ull << (kSketchLog - 1))) + 1;
-            atomicMax(&reg[idx], rank);
+            atomicMax(&reg[h >> (64 - kSketchLog)], rank);
+            atomicAdd(&hist[h >> (64 - kGroupPartLog)], 1u);
         }
     }
     if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31) == 0) atomicOr(a.err, kErrBadInput);
     __syncthreads();
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x)
         if (reg[i]) atomicMax(a.sketch + i, reg[i]);
+    for (int i = threadIdx.x; i < kGroupMaxParts; i += blockDim.x)
+        if (hist[i]) atomicAdd((unsigned long long*)(a.hist + i), (unsigned long long)hist[i]);
 }
 
-constexpr int kIlp = 4;
-
-
 // Distinct-brick estimate from the sketch (HyperLogLog with the linear
-// counting correction for small counts); the whole CTA takes part.
-__device__ double sketch_estimate(const uint32_t* sketch, double* red) {
-    double sum = 0.0, zeros = 0.0;
+// counting correction for small counts); the whole CTA takes part. The
+// register sum is exact in fixed point (2^(52 - rank), rank >= 1, at most
+// 4096 * 2^51 < 2^64); one thread finishes it in double precision, which is
+// slow on this GPU.
+__device__ double sketch_estimate(const uint32_t* sketch, unsigned long long* red, double* out) {
+    unsigned long long sum = 0, zeros = 0;
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) {
         const uint32_t r = sketch[i];
-        sum += ldexp(1.0, -(int)r);
-        zeros += r == 0 ? 1.0 : 0.0;
+        sum += 1ull << (52 - (r < 52 ? r : 52));
+        zeros += r == 0;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -105,114 +135,279 @@ __device__ double sketch_estimate(const uint32_t* sketch, double* red) {
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if ((threadIdx.x & 31) == 0) { red[2 * warp] = sum; red[2 * warp + 1] = zeros; }
     __syncthreads();
-    sum = 0.0;
-    zeros = 0.0;
-    for (int w = 0; w < nw; ++w) { sum += red[2 * w]; zeros += red[2 * w + 1]; }
+    if (threadIdx.x == 0) {
+        sum = 0;
+        zeros = 0;
+        for (int w = 0; w < nw; ++w) { sum += red[2 * w]; zeros += red[2 * w + 1]; }
+        const double m = (double)kSketchRegs;
+        const double e = 0.7213 / (1.0 + 1.079 / m) * m * m / ((double)sum * 0x1p-52);
+        *out = e <= 2.5 * m && zeros > 0 ? m * log(m / (double)zeros) : e;
+    }
     __syncthreads();
-    const double m = (double)kSketchRegs;
-    const double e = 0.7213 / (1.0 + 1.079 / m) * m * m / sum;
-    if (e <= 2.5 * m && zeros > 0) return m * log(m / zeros);
-    return e;
+    return *out;
 }
 
-__global__ void __launch_bounds__(256) group_insert(GroupArgs a) {
-    __shared__ double red[2 * 8];
-    const double est = sketch_estimate(a.sketch, red);
-    // Path: group when bricks hold kGroupMinRedundancy fragments on average
-    // and ~2.5 slots per estimated brick fit the table and the L2 (random
-    // atomics on a table in HBM are slower than the sort).
-    uint64_t S = 1024;
-    while ((double)S < 2.5 * est + 1.0 && S < kGroupMaxSlots) S <<= 1;
-    const bool group = a.mode == 2 ||
-                       (a.mode == 1 && est * kGroupMinRedundancy <= (double)a.n && (double)S >= 2.5 * est);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.path[0] = group ? 1u : 0u;
-        a.path[1] = (uint32_t)(63 - __clzll(S));
-    }
-    if (!group) return;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t warps = gsize / 32, warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    bool bad = false, full = false;
-    // Each lane runs kIlp fragments' probes side by side; a probe reads the
-    // slot and takes an atomicCAS only when it is empty.
-    for (uint64_t base = warp * 32 * kIlp; base < a.n; base += warps * 32 * kIlp) {
-        uint64_t key[kIlp], s[kIlp], bit[kIlp];
-        bool live[kIlp];
-#pragma unroll
-        for (int k = 0; k < kIlp; ++k) {
-            const uint64_t i = base + k * 32 + lane;
-            live[k] = i < a.n;
-            const uint64_t code = live[k] ? __ldg(a.frags + i) : 0;
-            key[k] = live[k] ? brick_of(a, i, code, &bad) + 1 : 1;  // 0 marks an empty slot
-            bit[k] = 1ull << (code & 63);
-            s[k] = fmix(key[k]) & (S - 1);
-        }
-        // At most 4096 probes: an overfull table (a forced grouping) ends in
-        // kErrFallback and a rerun, not in a long walk.
-        const uint64_t max_probe = S < 4096 ? S : 4096;
-        for (uint64_t probe = 0; probe < max_probe; ++probe) {
-            bool any = false;
-#pragma unroll
-            for (int k = 0; k < kIlp; ++k) {
-                if (!live[k]) continue;
-                uint64_t cur = ld_relaxed(a.table + s[k]);
-                if (cur == 0) cur = atomicCAS((unsigned long long*)(a.table + s[k]), 0ull, (unsigned long long)key[k]);
-                if (cur == 0 || cur == key[k]) {
-                    atomicOr((unsigned long long*)(a.table + kGroupMaxSlots + s[k]), (unsigned long long)bit[k]);
-                    live[k] = false;
-                } else {
-                    s[k] = (s[k] + 1) & (S - 1);
-                    any = true;
-                }
-            }
-            if (!any) break;
-        }
-#pragma unroll
-        for (int k = 0; k < kIlp; ++k) full |= live[k];  // table full: cannot happen below ~40% load
-    }
-    if (bad) atomicOr(a.err, kErrBadInput);
-    if (full) atomicOr(a.err, kErrFallback);
-}
+constexpr int kPlanThreads = kGroupMaxParts / 2;  // two fine partitions per thread
 
-// The brick list: every occupied slot of the table, (brick, slot), in slot
-// order per 2048-slot tile, tiles in any order (the list is sorted next).
-// One atomicAdd per tile reserves its place.
-constexpr int kCollectItems = 8;
-__global__ void __launch_bounds__(256) group_collect(GroupArgs a) {
+__global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
+    __shared__ unsigned long long red[2 * (kPlanThreads / 32)];
+    __shared__ double est_s;
+    __shared__ int shape[3];  // log2 partitions, log2 slots, redundancy and size test passed
     __shared__ uint64_t scan[34];
-    __shared__ uint64_t base_s;
+    __shared__ uint64_t start[kGroupMaxParts];
+    __shared__ unsigned long long max_part;
+    const double est = sketch_estimate(a.sketch, red, &est_s);
+    if (threadIdx.x == 0) {
+        // The shape, from the estimate (one thread: double precision is slow).
+        int lp = 0;
+        while (lp < kGroupPartLog && (double)(1u << lp) * kGroupBricksPerPart < est) ++lp;
+        const double per_part = est / (double)(1u << lp);
+        // Slots: ~8 per expected brick (up to the shared-memory table's size),
+        // so that most probes end at their first slot and warps stay converged.
+        int lt = 9;  // at least one slot per thread of the aggregation
+        while (lt < kGroupPartSlotsLog && (double)(1u << lt) < 8.0 * per_part + 32.0) ++lt;
+        shape[0] = lp;
+        shape[1] = lt;
+        shape[2] = est * kGroupMinRedundancy <= (double)a.n && per_part <= kGroupMaxBricksPerPart;
+        max_part = 0;
+    }
+    __syncthreads();
+    const int lp = shape[0], lt = shape[1];
+    const int parts = 1 << lp, shift = kGroupPartLog - lp;
+    const uint32_t fine_mask = (1u << shift) - 1;
+    // Partition p covers fine partitions [p << shift, (p + 1) << shift).
+    const uint32_t f0 = 2 * threadIdx.x;
+    const uint64_t v0 = a.hist[f0], v1 = a.hist[f0 + 1];
+    uint64_t total;
+    const uint64_t ex = block_exclusive_sum<uint64_t>(v0 + v1, scan, &total);
+    if ((f0 & fine_mask) == 0) start[f0 >> shift] = ex;
+    if (((f0 + 1) & fine_mask) == 0) start[(f0 + 1) >> shift] = ex + v0;
+    __syncthreads();
+    unsigned long long biggest = 0;
+    for (int p = threadIdx.x; p < parts; p += blockDim.x) {
+        const uint64_t end = p + 1 < parts ? start[p + 1] : total;
+        biggest = end - start[p] > biggest ? end - start[p] : biggest;
+        a.cursor[p] = start[p];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xFFFFFFFFu, biggest, o);
+        biggest = other > biggest ? other : biggest;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&max_part, biggest);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool group = a.mode == 2 || (a.mode == 1 && shape[2] && max_part <= kGroupMaxPartFrags);
+        a.path[0] = group ? 1u : 0u;
+        a.path[1] = (uint32_t)lp;
+        a.path[2] = (uint32_t)lt;
+    }
+}
+
+// 8-byte asynchronous copy global -> shared (cp.async), and its completion.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+constexpr int kScatterThreads = 1024;  // one CTA per SM
+constexpr int kScatterPer = 8;
+constexpr int kScatterTile = kScatterThreads * kScatterPer;
+constexpr int kScatterMaxPer = (kGroupMaxParts + kScatterThreads - 1) / kScatterThreads;  // partitions per thread
+static_assert(kScatterTile <= 65536 && kGroupMaxParts <= 65536, "rank and partition share a word");
+
+struct ScatterSmem {
+    uint64_t in[kScatterTile];       // the next tile's keys, copied in while this tile is processed
+    uint64_t stage[kScatterTile];    // this tile's keys, by partition
+    uint32_t cnt[kGroupMaxParts];    // the tile's count per partition, then its offset in the tile
+    int32_t delta[kGroupMaxParts];   // output position - tile position, per partition
+    uint32_t scan[34];
+};
+
+__device__ __forceinline__ void scatter_prefetch(ScatterSmem& sm, const uint64_t* frags, uint64_t base, uint64_t hi) {
+    for (uint32_t q = threadIdx.x; q < (uint32_t)kScatterTile && base + q < hi; q += kScatterThreads)
+        cp_async8(&sm.in[q], frags + base + q);
+    cp_async_commit();
+}
+
+__device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
+    return lp ? (uint32_t)(brick_hash(key >> 6) >> (64 - lp)) : 0u;
+}
+
+__global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ScatterSmem& sm = *reinterpret_cast<ScatterSmem*>(smem_raw);
     if (a.path[0] != 1u) return;
-    const uint64_t S = (1ull << a.path[1]) < kGroupMaxSlots ? (1ull << a.path[1]) : kGroupMaxSlots;
-    const uint64_t tile = 256ull * kCollectItems;
-    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < S; t0 += (uint64_t)gridDim.x * tile) {
-        const uint64_t s0 = t0 + (uint64_t)threadIdx.x * kCollectItems;
-        uint64_t key[kCollectItems];
-        uint64_t cnt = 0;
+    const int lp = (int)a.path[1];
+    const int parts = 1 << lp;
+    uint64_t lo, hi;
+    chunk_range(a, &lo, &hi);
+    bool bad = false;  // reported by the sketch pass
+    const int per = (parts + kScatterThreads - 1) / kScatterThreads;
+    for (int p = threadIdx.x; p < parts; p += kScatterThreads) sm.cnt[p] = 0;
+    if (lo < hi) scatter_prefetch(sm, a.frags, lo, hi);
+    for (uint64_t base = lo; base < hi; base += kScatterTile) {
+        cp_async_wait_all();
+        __syncthreads();  // the tile is in `in`; cnt is zero
+        uint64_t key[kScatterPer];
 #pragma unroll
-        for (int j = 0; j < kCollectItems; ++j) {
-            key[j] = s0 + j < S ? a.table[s0 + j] : 0;
-            cnt += key[j] != 0;
+        for (int k = 0; k < kScatterPer; ++k) key[k] = sm.in[k * kScatterThreads + threadIdx.x];
+        __syncthreads();  // `in` is free for the next tile
+        if (base + kScatterTile < hi) scatter_prefetch(sm, a.frags, base + kScatterTile, hi);
+        uint32_t pr[kScatterPer];
+#pragma unroll
+        for (int k = 0; k < kScatterPer; ++k) {
+            const uint64_t i = base + (uint64_t)k * kScatterThreads + threadIdx.x;
+            if (i >= hi) continue;
+            key[k] = key_of(a, i, key[k], &bad);
+            const uint32_t pid = part_of(key[k], lp);
+            pr[k] = (pid << 16) | atomicAdd(&sm.cnt[pid], 1u);
         }
-        uint64_t total;
-        const uint64_t excl = block_exclusive_sum<uint64_t>(cnt, scan, &total);
-        if (threadIdx.x == 0) base_s = total ? atomicAdd((unsigned long long*)a.d_count, (unsigned long long)total) : 0;
         __syncthreads();
-        uint64_t pos = base_s + excl;
+        const int p0 = threadIdx.x * per;
+        uint32_t sum = 0;
+        for (int j = 0; j < per; ++j)
+            if (p0 + j < parts) sum += sm.cnt[p0 + j];
+        uint32_t tile_total;
+        uint32_t run = block_exclusive_sum<uint32_t>(sum, sm.scan, &tile_total);
+        // The tile's run of each partition goes right after the runs that
+        // tiles reserved before it, so that the partially written sectors of
+        // a partition's frontier are completed while they are in the L2.
+        uint32_t c[kScatterMaxPer], g[kScatterMaxPer];
 #pragma unroll
-        for (int j = 0; j < kCollectItems; ++j) {
-            if (key[j] == 0) continue;
+        for (int j = 0; j < kScatterMaxPer; ++j) {
+            const int p = p0 + j;
+            c[j] = j < per && p < parts ? sm.cnt[p] : 0u;
+            g[j] = c[j] ? (uint32_t)atomicAdd((unsigned long long*)(a.cursor + p), (unsigned long long)c[j]) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kScatterMaxPer; ++j) {
+            const int p = p0 + j;
+            if (j >= per || p >= parts) break;
+            sm.cnt[p] = run;
+            sm.delta[p] = (int32_t)g[j] - (int32_t)run;
+            run += c[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kScatterPer; ++k) {
+            const uint64_t i = base + (uint64_t)k * kScatterThreads + threadIdx.x;
+            if (i >= hi) continue;
+            sm.stage[sm.cnt[pr[k] >> 16] + (pr[k] & 0xFFFFu)] = key[k];
+        }
+        __syncthreads();
+        // Write-out in tile order: runs of one partition are contiguous. The
+        // partition is recomputed from the key (cheaper than storing it).
+        const uint32_t m = (uint32_t)(hi - base < (uint64_t)kScatterTile ? hi - base : (uint64_t)kScatterTile);
+#pragma unroll 4
+        for (uint32_t q = threadIdx.x; q < m; q += kScatterThreads) {
+            const uint64_t k = sm.stage[q];
+            a.parts[(int64_t)sm.delta[part_of(k, lp)] + q] = k;
+        }
+        for (int p = threadIdx.x; p < parts; p += kScatterThreads) sm.cnt[p] = 0;  // read last before the stage barrier
+    }
+}
+
+constexpr int kAggThreads = 512;
+constexpr int kAggIlp = 4;
+static_assert((1 << 9) >= kAggThreads, "at least one table slot per thread");
+
+// Slot of a brick in its partition's table (2^lt slots): a multiplicative
+// hash of the brick's two 32-bit halves (the partition was picked by the top
+// bits of brick_hash, independent of these).
+__device__ __forceinline__ uint32_t slot_hash(uint64_t brick, uint32_t lt) {
+    const uint32_t x = (uint32_t)brick ^ ((uint32_t)(brick >> 32) * 0x85EBCA6Bu);
+    return (x * 0x9E3779B1u) >> (32 - lt);
+}
+
+struct AggSmem {
+    uint64_t key[kGroupPartSlots];   // brick + 1, 0 = empty
+    uint64_t mask[kGroupPartSlots];  // OR of the fragments' bits
+    uint32_t scan[34];
+    uint64_t base;
+};
+
+__global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    AggSmem& sm = *reinterpret_cast<AggSmem*>(smem_raw);
+    if (a.path[0] != 1u) return;
+    const uint32_t parts = 1u << a.path[1], lt = a.path[2], slots = 1u << lt;
+    bool full = false;
+    for (uint32_t p = blockIdx.x; p < parts; p += gridDim.x) {
+        const uint64_t lo = p ? a.cursor[p - 1] : 0, hi = a.cursor[p];
+        for (uint32_t s = threadIdx.x; s < slots; s += kAggThreads) {
+            sm.key[s] = 0;
+            sm.mask[s] = 0;
+        }
+        __syncthreads();
+        for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kAggIlp * kAggThreads) {
+            uint64_t tag[kAggIlp];
+            uint32_t s[kAggIlp], bit[kAggIlp];
+            bool live[kAggIlp];
+#pragma unroll
+            for (int u = 0; u < kAggIlp; ++u) {
+                const uint64_t i = i0 + (uint64_t)u * kAggThreads;
+                live[u] = i < hi;
+                const uint64_t k = live[u] ? __ldcs(a.parts + i) : 0;
+                tag[u] = (k >> 6) + 1;
+                bit[u] = (uint32_t)(k & 63);
+                s[u] = slot_hash(k >> 6, lt);
+            }
+            // The kAggIlp probes of a thread advance side by side: one round
+            // reads every live probe's slot, then claims or moves on.
+            for (uint32_t probe = 0; probe < slots; ++probe) {
+                uint64_t cur[kAggIlp];
+#pragma unroll
+                for (int u = 0; u < kAggIlp; ++u)
+                    cur[u] = live[u] ? *reinterpret_cast<volatile uint64_t*>(&sm.key[s[u]]) : 0;
+                bool any = false;
+#pragma unroll
+                for (int u = 0; u < kAggIlp; ++u) {
+                    if (!live[u]) continue;
+                    uint64_t cv = cur[u];
+                    if (cv == 0) cv = atomicCAS((unsigned long long*)&sm.key[s[u]], 0ull, (unsigned long long)tag[u]);
+                    if (cv == 0 || cv == tag[u]) {
+                        atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s[u]]) + (bit[u] >> 5), 1u << (bit[u] & 31));
+                        live[u] = false;
+                    } else {
+                        s[u] = (s[u] + 1) & (slots - 1);
+                        any = true;
+                    }
+                }
+                if (!any) break;
+            }
+#pragma unroll
+            for (int u = 0; u < kAggIlp; ++u) full |= live[u];  // more bricks than slots: rerun on the sort path
+        }
+        __syncthreads();
+        const uint32_t per = slots / kAggThreads, s0 = threadIdx.x * per;
+        uint32_t cnt = 0;
+        for (uint32_t j = 0; j < per; ++j) cnt += sm.key[s0 + j] != 0;
+        uint32_t total;
+        const uint32_t ex = block_exclusive_sum<uint32_t>(cnt, sm.scan, &total);
+        if (threadIdx.x == 0)
+            sm.base = total ? atomicAdd((unsigned long long*)a.d_count, (unsigned long long)total) : 0ull;
+        __syncthreads();
+        uint64_t pos = sm.base + ex;
+        for (uint32_t j = 0; j < per; ++j) {
+            const uint64_t t = sm.key[s0 + j];
+            if (t == 0) continue;
             if (pos < a.cap) {
-                a.bricks[pos] = key[j] - 1;
-                a.slots[pos] = (uint32_t)(s0 + j);
+                a.bricks[pos] = t - 1;
+                a.idx[pos] = (uint32_t)pos;
+                a.masks[pos] = sm.mask[s0 + j];
             } else {
-                atomicOr(a.err, kErrFallback);
+                full = true;
             }
             ++pos;
         }
-        __syncthreads();  // base_s and scan are reused by the next tile
+        __syncthreads();  // the table is cleared for the next partition
     }
+    if (full) atomicOr(a.err, kErrFallback);
 }
+
+constexpr int kGatherIlp = 4;
 
 __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
     if (a.path[0] != 1u) return;
@@ -220,19 +415,19 @@ __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_count = count;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t lmask = a.seg_code ? (1ull << (a.seg_shift - 6)) - 1 : 0;
-    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < count; i0 += stride * kIlp) {
-        uint32_t s[kIlp];
-        uint64_t b[kIlp], m[kIlp];
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < count; i0 += stride * kGatherIlp) {
+        uint32_t j[kGatherIlp];
+        uint64_t b[kGatherIlp], m[kGatherIlp];
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) {
+        for (int k = 0; k < kGatherIlp; ++k) {
             const uint64_t i = i0 + k * stride;
-            s[k] = i < count ? a.sorted_slots[i] : 0xFFFFFFFFu;
+            j[k] = i < count ? a.sorted_idx[i] : 0xFFFFFFFFu;
             b[k] = i < count ? a.sorted_bricks[i] : 0;
         }
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) m[k] = s[k] < kGroupMaxSlots ? a.table[kGroupMaxSlots + s[k]] : 0;
+        for (int k = 0; k < kGatherIlp; ++k) m[k] = j[k] < a.cap ? a.masks[j[k]] : 0;
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) {
+        for (int k = 0; k < kGatherIlp; ++k) {
             const uint64_t i = i0 + k * stride;
             if (i >= count) continue;
             // Batched input: composite brick (segment << (seg_shift - 6)) | local
@@ -241,10 +436,6 @@ __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
             if (a.seg_code) parent = (__ldg(a.seg_code + (b[k] >> (a.seg_shift - 6))) << (a.seg_shift - 6)) | (b[k] & lmask);
             a.parents[i] = parent;
             a.leaves[i] = m[k];
-            if (s[k] < kGroupMaxSlots) {
-                a.table[s[k]] = 0;  // leave the table empty
-                a.table[kGroupMaxSlots + s[k]] = 0;
-            }
         }
     }
 }
@@ -253,15 +444,30 @@ int g_group_sms = 152;
 
 }  // namespace
 
-void group_configure(int sms) { g_group_sms = sms > 0 ? sms : 152; }
-
-static int front_grid(const GroupArgs& a) {
-    const uint64_t want = (a.n + 1023) / 1024;
-    return (int)(want < (uint64_t)(8 * g_group_sms) ? (want > 0 ? want : 1) : 8 * g_group_sms);
+void group_configure(int sms) {
+    g_group_sms = sms > 0 ? sms : 152;
+    cudaFuncSetAttribute(group_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ScatterSmem));
+    cudaFuncSetAttribute(group_aggregate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AggSmem));
 }
-void launch_group_sketch(const GroupArgs& a, cudaStream_t s) { group_sketch<<<front_grid(a), 256, 0, s>>>(a); }
-void launch_group_insert(const GroupArgs& a, cudaStream_t s) { group_insert<<<front_grid(a), 256, 0, s>>>(a); }
-void launch_group_collect(const GroupArgs& a, cudaStream_t s) { group_collect<<<8 * g_group_sms, 256, 0, s>>>(a); }
+
+int group_chunks(uint64_t n) {
+    const uint64_t want = (n + kScatterTile - 1) / kScatterTile;
+    const uint64_t most = (uint64_t)(g_group_sms < kGroupMaxChunks ? g_group_sms : kGroupMaxChunks);
+    return (int)(want < 1 ? 1 : (want < most ? want : most));
+}
+
+void launch_group_sketch(const GroupArgs& a, cudaStream_t s) {
+    const uint64_t want = (a.n + kFrontThreads * kSketchIlp - 1) / (kFrontThreads * kSketchIlp);
+    const int g = (int)(want < (uint64_t)(2 * g_group_sms) ? (want > 0 ? want : 1) : 2 * g_group_sms);
+    group_sketch<<<g, kFrontThreads, 0, s>>>(a);
+}
+void launch_group_plan(const GroupArgs& a, cudaStream_t s) { group_plan<<<1, kPlanThreads, 0, s>>>(a); }
+void launch_group_scatter(const GroupArgs& a, cudaStream_t s) {
+    group_scatter<<<a.chunks, kScatterThreads, sizeof(ScatterSmem), s>>>(a);
+}
+void launch_group_aggregate(const GroupArgs& a, cudaStream_t s) {
+    group_aggregate<<<3 * g_group_sms, kAggThreads, sizeof(AggSmem), s>>>(a);
+}
 
 void launch_group_gather(const GroupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.cap + 1023) / 1024;

@@ -30,8 +30,11 @@ constexpr int kRadix = 1 << kRadixBits;
 
 constexpr int kPassThreads = 256;  // one thread per digit
 
+// A device-resident count never exceeds the bound its buffers were sized for.
 __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
-    return d_n ? *d_n : n;
+    if (!d_n) return n;
+    const uint64_t v = *d_n;
+    return v < n ? v : n;
 }
 
 // Segment of position i (seg_offsets ascending, count + 1 entries): binary

@@ -192,10 +192,11 @@ int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
 #define DAGC_STAGE_MATERIALISE 5    /* copy of the level outputs into the DAG */
 #define DAGC_STAGE_FINAL 6          /* final word layout */
 #define DAGC_STAGE_MERGE 7          /* MergeDAGs */
-#define DAGC_STAGE_GROUP 8          /* fragment grouping by hash: brick list, brick sort, gather */
-#define DAGC_STAGE_GROUP_SKETCH 9   /* its distinct-brick sketch (one read of the fragments) */
-#define DAGC_STAGE_GROUP_INSERT 10  /* its table insert (one read of the fragments, table in the L2) */
-#define DAGC_NUM_STAGES 11
+#define DAGC_STAGE_GROUP 8             /* fragment grouping by hash: brick sort, gather */
+#define DAGC_STAGE_GROUP_SKETCH 9      /* its sketch + partition counts (one read of the fragments), path choice */
+#define DAGC_STAGE_GROUP_AGGREGATE 10  /* its per-partition tables (one read of the partitioned fragments) */
+#define DAGC_STAGE_GROUP_SCATTER 11    /* its partitioning (one read and one write of the fragments) */
+#define DAGC_NUM_STAGES 12
 int dagc_profile_enable(dagc_context ctx, int enable);
 int dagc_profile_reset(dagc_context ctx);
 int dagc_profile_read(dagc_context ctx, int stage, double* device_ms, uint64_t* launches,
