@@ -13,6 +13,7 @@
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 #include <algorithm>
 
@@ -69,6 +70,7 @@ __device__ __forceinline__ uint64_t global_code(const LeafBuildArgs& a, uint64_t
 // run of an earlier tile: their OR goes to lead_or[tile] and leaf_fixup folds
 // it in after this kernel.
 __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
+    pdl_prologue();
     __shared__ LeafSmem S;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (a.gate && *a.gate != a.gate_run) return;
@@ -174,6 +176,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
 // ORs every tile's leading keys into the run they continue (written by an
 // earlier tile of leaf_build, one launch before, with a plain store).
 __global__ void leaf_fixup(LeafBuildArgs a) {
+    pdl_prologue();
     if (a.gate && *a.gate != a.gate_run) return;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = leaf_tiles(n);
@@ -198,6 +201,7 @@ struct ExtractSmem {
 };
 
 __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ExtractSmem& S = *reinterpret_cast<ExtractSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -297,6 +301,7 @@ struct UniqueSmem {
 };
 
 __global__ void __launch_bounds__(kT) unique_runs(UniqueArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     UniqueSmem& S = *reinterpret_cast<UniqueSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -412,6 +417,7 @@ __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb,
 }
 
 __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TailSmem& S = *reinterpret_cast<TailSmem*>(smem_raw);
     const uint32_t tid = threadIdx.x;
@@ -555,6 +561,7 @@ struct FinalScanSmem {
 
 // word_pos[i] = sum over nodes j < i of (popc(mask_j) + 1); word_pos[n] = total.
 __global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
+    pdl_prologue();
     __shared__ FinalScanSmem S;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = a.num_nodes;
@@ -593,6 +600,7 @@ __global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
 }
 
 __global__ void __launch_bounds__(kT) final_write(FinalArgs a) {
+    pdl_prologue();
     __shared__ uint64_t s_off[24];
     if (threadIdx.x <= (unsigned)a.num_levels) s_off[threadIdx.x] = a.level_offsets[threadIdx.x];
     __syncthreads();
@@ -639,6 +647,7 @@ __global__ void __launch_bounds__(kT) final_write(FinalArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void remap_children(const uint32_t* __restrict__ in, const uint32_t* __restrict__ map,
                                uint32_t* __restrict__ out, uint64_t n_words) {
+    pdl_prologue();
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t c = in[i];
         out[i] = c == kEmptyChild ? kEmptyChild : map[c];
@@ -646,6 +655,7 @@ __global__ void remap_children(const uint32_t* __restrict__ in, const uint32_t* 
 }
 
 __global__ void iota_offset(uint32_t* out, uint64_t n, uint32_t offset) {
+    pdl_prologue();
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         out[i] = offset + (uint32_t)i;
 }
@@ -685,37 +695,37 @@ int occupancy_kernel(int which) {
 }
 
 void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s) {
-    leaf_build<<<a.grid, kT, 0, s>>>(a);
+    launch_pdl(leaf_build, dim3(a.grid), dim3(kT), 0, s, a);
     const uint64_t tiles = leaf_tiles(a.n_bound);
     const int grid = (int)std::min<uint64_t>((tiles + 255) / 256, (uint64_t)g_blocks_small);
-    leaf_fixup<<<grid > 0 ? grid : 1, 256, 0, s>>>(a);
+    launch_pdl(leaf_fixup, dim3(grid > 0 ? grid : 1), dim3(256), 0, s, a);
 }
 void launch_extract(const ExtractArgs& a, cudaStream_t s) {
-    extract_level<<<a.grid, kT, sizeof(ExtractSmem), s>>>(a);
+    launch_pdl(extract_level, dim3(a.grid), dim3(kT), sizeof(ExtractSmem), s, a);
 }
 void launch_unique(const UniqueArgs& a, cudaStream_t s) {
-    unique_runs<<<a.grid, kT, sizeof(UniqueSmem), s>>>(a);
+    launch_pdl(unique_runs, dim3(a.grid), dim3(kT), sizeof(UniqueSmem), s, a);
 }
 void launch_tail(const TailArgs& a, cudaStream_t s) {
-    tail_levels<<<1, kTailThreads, sizeof(TailSmem), s>>>(a);
+    launch_pdl(tail_levels, dim3(1), dim3(kTailThreads), sizeof(TailSmem), s, a);
 }
 void launch_final_positions(const FinalArgs& a, cudaStream_t s) {
-    final_positions<<<a.grid_scan, kT, 0, s>>>(a);
+    launch_pdl(final_positions, dim3(a.grid_scan), dim3(kT), 0, s, a);
 }
 void launch_final_write(const FinalArgs& a, cudaStream_t s) {
-    final_write<<<a.grid_write, kT, 0, s>>>(a);
+    launch_pdl(final_write, dim3(a.grid_write), dim3(kT), 0, s, a);
 }
 void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* out, uint64_t n_nodes,
                            cudaStream_t s) {
     if (n_nodes == 0) return;
     const uint64_t words = n_nodes * 8;
     const int grid = (int)std::min<uint64_t>((words + 255) / 256, (uint64_t)g_blocks_small);
-    remap_children<<<grid, 256, 0, s>>>(in, map, out, words);
+    launch_pdl(remap_children, dim3(grid), dim3(256), 0, s, in, map, out, words);
 }
 void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s) {
     if (n == 0) return;
     const int grid = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)g_blocks_small);
-    iota_offset<<<grid, 256, 0, s>>>(out, n, offset);
+    launch_pdl(iota_offset, dim3(grid), dim3(256), 0, s, out, n, offset);
 }
 
 }  // namespace dagc

@@ -10,6 +10,17 @@
 
 namespace dagc {
 
+// Programmatic dependent launch. Every kernel of a call first lets the next
+// kernel of its stream be scheduled (once all of its own CTAs run), then
+// waits until the previous kernel has completed and its memory is visible:
+// the next kernel's launch and CTA start-up overlap this kernel's tail, and no
+// kernel touches memory before its predecessor is done. Without the launch
+// attribute (dagc::launch_pdl) both instructions do nothing.
+__device__ __forceinline__ void pdl_prologue() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Upper limit on waits: ~2^20 polls with exponential back-off capped at 1 us,
 // i.e. about one second, after which the waiter flags kErrTimeout.
 constexpr uint32_t kSpinLimit = 1u << 20;

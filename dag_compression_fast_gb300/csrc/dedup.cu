@@ -32,6 +32,7 @@
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 namespace dagc {
 namespace {
@@ -70,6 +71,7 @@ __device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
 constexpr int kIlp = 4;
 
 __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
+    pdl_prologue();
     const uint64_t n = *a.d_n;
     const uint64_t S = table_size_for(n);
     const uint32_t lane = threadIdx.x & 31;
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
 constexpr int kSplitThreads = 1024;
 
 __global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* sample = reinterpret_cast<uint64_t*>(smem_raw);  // kDedupMaxSample
     const uint32_t tid = threadIdx.x;
@@ -195,6 +198,7 @@ __global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
 }
 
 __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // sampled form: kDedupMaxSampledBuckets
     const uint64_t u = unique_count(a);
@@ -248,6 +252,7 @@ __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
 constexpr int kBucketThreads = 256;
 
 __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint64_t* key = reinterpret_cast<uint64_t*>(smem_raw);  // bucket room: kDedupSampledCapMax or kDedupTopBitCap
     __shared__ uint32_t red[kBucketThreads / 32];
@@ -320,6 +325,7 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
 }
 
 __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
+    pdl_prologue();
     const uint64_t n = *a.d_n;
     if (table_size_for(n) > a.table_cap || n > a.item_cap) return;  // insert did nothing
     const uint32_t last = a.out_capacity ? (uint32_t)(a.out_capacity - 1) : 0u;
@@ -377,17 +383,17 @@ int launch_dedup(const DedupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.item_cap + 255) / 256;
     const int g = 8 * g_sms;  // full occupancy: 8 CTAs of 256 threads per SM
     const int gi = (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
-    dedup_insert<<<gi, 256, 0, s>>>(a);
+    launch_pdl(dedup_insert, dim3(gi), dim3(256), 0, s, a);
     int launches = 1;
     if (a.sampled) {
-        dedup_split<<<1, kSplitThreads, kDedupMaxSample * 8, s>>>(a);
+        launch_pdl(dedup_split, dim3(1), dim3(kSplitThreads), kDedupMaxSample * 8, s, a);
         ++launches;
     }
-    dedup_scatter<<<gi, 256, a.sampled ? kDedupMaxSampledBuckets * 8 : 0, s>>>(a);
+    launch_pdl(dedup_scatter, dim3(gi), dim3(256), a.sampled ? kDedupMaxSampledBuckets * 8 : 0, s, a);
     const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
     const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
-    dedup_sort<<<gs, kBucketThreads, (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s>>>(a);
-    dedup_map<<<gi, 256, 0, s>>>(a);
+    launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s, a);
+    launch_pdl(dedup_map, dim3(gi), dim3(256), 0, s, a);
     return launches + 3;
 }
 

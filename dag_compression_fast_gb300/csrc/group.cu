@@ -33,6 +33,7 @@
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 namespace dagc {
 namespace {
@@ -47,10 +48,20 @@ __device__ __forceinline__ uint64_t fmix(uint64_t k) {
     return k;
 }
 
-// One hash per brick, used three ways: top 12 bits pick the sketch register
-// (the bits below give its rank), top kGroupPartLog bits the fine partition,
-// low bits the slot in the partition's table.
+// The sketch's hash: top 12 bits pick the register, the bits below give its
+// rank (they must be close to uniform).
 __device__ __forceinline__ uint64_t brick_hash(uint64_t brick) { return fmix(brick ^ 0x9E3779B97F4A7C15ull); }
+
+// The partition's hash, one multiply (Fibonacci hashing): its top
+// kGroupPartLog bits are the fine partition, the bits below them the slot in
+// the partition's table.
+__device__ __forceinline__ uint64_t part_hash(uint64_t brick) { return brick * 0x9E3779B97F4A7C15ull; }
+__device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
+    return lp ? (uint32_t)(part_hash(key >> 6) >> (64 - lp)) : 0u;
+}
+__device__ __forceinline__ uint32_t slot_of(uint64_t brick, uint32_t lt) {
+    return (uint32_t)(part_hash(brick) >> (64 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+}
 
 __device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t count, uint64_t i) {
     uint32_t lo = 0, hi = count;  // off[lo] <= i < off[hi]
@@ -83,6 +94,7 @@ constexpr int kFrontThreads = 512;
 constexpr int kSketchIlp = 8;
 
 __global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
+    pdl_prologue();
     __shared__ uint32_t reg[kSketchRegs];
     __shared__ uint32_t hist[kGroupMaxParts];
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) reg[i] = 0;
@@ -101,10 +113,11 @@ __global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
         for (int u = 0; u < kSketchIlp; ++u) {
             const uint64_t i = i0 + u * stride;
             if (i >= a.n) continue;
-            const uint64_t h = brick_hash(key_of(a, i, c[u], &bad) >> 6);
+            const uint64_t brick = key_of(a, i, c[u], &bad) >> 6;
+            const uint64_t h = brick_hash(brick);
             const uint32_t rank = (uint32_t)__clzll((h << kSketchLog) | (1ull << (kSketchLog - 1))) + 1;
             atomicMax(&reg[h >> (64 - kSketchLog)], rank);
-            atomicAdd(&hist[h >> (64 - kGroupPartLog)], 1u);
+            atomicAdd(&hist[part_hash(brick) >> (64 - kGroupPartLog)], 1u);
         }
     }
     if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31) == 0) atomicOr(a.err, kErrBadInput);
@@ -150,6 +163,7 @@ __device__ double sketch_estimate(const uint32_t* sketch, unsigned long long* re
 constexpr int kPlanThreads = kGroupMaxParts / 2;  // two fine partitions per thread
 
 __global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
+    pdl_prologue();
     __shared__ unsigned long long red[2 * (kPlanThreads / 32)];
     __shared__ double est_s;
     __shared__ int shape[3];  // log2 partitions, log2 slots, redundancy and size test passed
@@ -231,11 +245,8 @@ __device__ __forceinline__ void scatter_prefetch(ScatterSmem& sm, const uint64_t
     cp_async_commit();
 }
 
-__device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
-    return lp ? (uint32_t)(brick_hash(key >> 6) >> (64 - lp)) : 0u;
-}
-
 __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ScatterSmem& sm = *reinterpret_cast<ScatterSmem*>(smem_raw);
     if (a.path[0] != 1u) return;
@@ -313,14 +324,6 @@ constexpr int kAggThreads = 512;
 constexpr int kAggIlp = 4;
 static_assert((1 << 9) >= kAggThreads, "at least one table slot per thread");
 
-// Slot of a brick in its partition's table (2^lt slots): a multiplicative
-// hash of the brick's two 32-bit halves (the partition was picked by the top
-// bits of brick_hash, independent of these).
-__device__ __forceinline__ uint32_t slot_hash(uint64_t brick, uint32_t lt) {
-    const uint32_t x = (uint32_t)brick ^ ((uint32_t)(brick >> 32) * 0x85EBCA6Bu);
-    return (x * 0x9E3779B1u) >> (32 - lt);
-}
-
 struct AggSmem {
     uint64_t key[kGroupPartSlots];   // brick + 1, 0 = empty
     uint64_t mask[kGroupPartSlots];  // OR of the fragments' bits
@@ -329,6 +332,7 @@ struct AggSmem {
 };
 
 __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     AggSmem& sm = *reinterpret_cast<AggSmem*>(smem_raw);
     if (a.path[0] != 1u) return;
@@ -342,43 +346,34 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
         }
         __syncthreads();
         for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kAggIlp * kAggThreads) {
-            uint64_t tag[kAggIlp];
-            uint32_t s[kAggIlp], bit[kAggIlp];
-            bool live[kAggIlp];
+            uint64_t k[kAggIlp];
 #pragma unroll
             for (int u = 0; u < kAggIlp; ++u) {
                 const uint64_t i = i0 + (uint64_t)u * kAggThreads;
-                live[u] = i < hi;
-                const uint64_t k = live[u] ? __ldcs(a.parts + i) : 0;
-                tag[u] = (k >> 6) + 1;
-                bit[u] = (uint32_t)(k & 63);
-                s[u] = slot_hash(k >> 6, lt);
+                k[u] = i < hi ? __ldcs(a.parts + i) : 0;
             }
-            // The kAggIlp probes of a thread advance side by side: one round
-            // reads every live probe's slot, then claims or moves on.
-            for (uint32_t probe = 0; probe < slots; ++probe) {
-                uint64_t cur[kAggIlp];
 #pragma unroll
-                for (int u = 0; u < kAggIlp; ++u)
-                    cur[u] = live[u] ? *reinterpret_cast<volatile uint64_t*>(&sm.key[s[u]]) : 0;
-                bool any = false;
-#pragma unroll
-                for (int u = 0; u < kAggIlp; ++u) {
-                    if (!live[u]) continue;
-                    uint64_t cv = cur[u];
-                    if (cv == 0) cv = atomicCAS((unsigned long long*)&sm.key[s[u]], 0ull, (unsigned long long)tag[u]);
-                    if (cv == 0 || cv == tag[u]) {
-                        atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s[u]]) + (bit[u] >> 5), 1u << (bit[u] & 31));
-                        live[u] = false;
-                    } else {
-                        s[u] = (s[u] + 1) & (slots - 1);
-                        any = true;
+            for (int u = 0; u < kAggIlp; ++u) {
+                if (i0 + (uint64_t)u * kAggThreads >= hi) continue;
+                const uint64_t brick = k[u] >> 6, tag = brick + 1;
+                uint32_t s = slot_of(brick, lt);
+                uint64_t cur = *reinterpret_cast<volatile uint64_t*>(&sm.key[s]);
+                if (cur != tag) {
+                    // Rare: the brick's first fragment here, or a collision.
+                    for (uint32_t probe = 0;; ) {
+                        if (cur == 0) {
+                            cur = atomicCAS((unsigned long long*)&sm.key[s], 0ull, (unsigned long long)tag);
+                            if (cur == 0 || cur == tag) break;
+                        }
+                        if (++probe == slots) { full = true; break; }  // more bricks than slots: sort path
+                        s = (s + 1) & (slots - 1);
+                        cur = *reinterpret_cast<volatile uint64_t*>(&sm.key[s]);
+                        if (cur == tag) break;
                     }
                 }
-                if (!any) break;
+                const uint32_t bit = (uint32_t)(k[u] & 63);
+                atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s]) + (bit >> 5), 1u << (bit & 31));
             }
-#pragma unroll
-            for (int u = 0; u < kAggIlp; ++u) full |= live[u];  // more bricks than slots: rerun on the sort path
         }
         __syncthreads();
         const uint32_t per = slots / kAggThreads, s0 = threadIdx.x * per;
@@ -410,6 +405,7 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
 constexpr int kGatherIlp = 4;
 
 __global__ void __launch_bounds__(256) group_gather(GroupArgs a) {
+    pdl_prologue();
     if (a.path[0] != 1u) return;
     const uint64_t count = *a.d_count < a.cap ? *a.d_count : a.cap;
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_count = count;
@@ -459,20 +455,20 @@ int group_chunks(uint64_t n) {
 void launch_group_sketch(const GroupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.n + kFrontThreads * kSketchIlp - 1) / (kFrontThreads * kSketchIlp);
     const int g = (int)(want < (uint64_t)(2 * g_group_sms) ? (want > 0 ? want : 1) : 2 * g_group_sms);
-    group_sketch<<<g, kFrontThreads, 0, s>>>(a);
+    launch_pdl(group_sketch, dim3(g), dim3(kFrontThreads), 0, s, a);
 }
-void launch_group_plan(const GroupArgs& a, cudaStream_t s) { group_plan<<<1, kPlanThreads, 0, s>>>(a); }
+void launch_group_plan(const GroupArgs& a, cudaStream_t s) { launch_pdl(group_plan, dim3(1), dim3(kPlanThreads), 0, s, a); }
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s) {
-    group_scatter<<<a.chunks, kScatterThreads, sizeof(ScatterSmem), s>>>(a);
+    launch_pdl(group_scatter, dim3(a.chunks), dim3(kScatterThreads), sizeof(ScatterSmem), s, a);
 }
 void launch_group_aggregate(const GroupArgs& a, cudaStream_t s) {
-    group_aggregate<<<3 * g_group_sms, kAggThreads, sizeof(AggSmem), s>>>(a);
+    launch_pdl(group_aggregate, dim3(3 * g_group_sms), dim3(kAggThreads), sizeof(AggSmem), s, a);
 }
 
 void launch_group_gather(const GroupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.cap + 1023) / 1024;
     const int g = (int)(want < (uint64_t)(8 * g_group_sms) ? (want > 0 ? want : 1) : 8 * g_group_sms);
-    group_gather<<<g, 256, 0, s>>>(a);
+    launch_pdl(group_gather, dim3(g), dim3(256), 0, s, a);
 }
 
 }  // namespace dagc

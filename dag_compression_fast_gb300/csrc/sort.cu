@@ -17,6 +17,7 @@
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 #include <algorithm>
 
@@ -57,6 +58,7 @@ radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t
                 int hi_bit, int validate_bits, uint32_t* __restrict__ hist, uint32_t* status0,
                 uint32_t* err, const uint64_t* seg_offsets, uint32_t seg_count, int seg_shift,
                 const uint32_t* gate, uint32_t gate_run) {
+    pdl_prologue();
     __shared__ uint32_t s_hist[kMaxPasses][kRadix];
     if (gate && *gate != gate_run) return;
     const uint64_t n = load_n(d_n, n_host);
@@ -194,6 +196,7 @@ struct PassSmem {
 // the work over both pipes.
 template <int kThreads, int kItems, bool kValues, int kMinCtas, int kMatch>
 __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p) {
+    pdl_prologue();
     using Smem = PassSmem<kThreads, kItems, kValues>;
     constexpr int kTile = Smem::kTile;
     constexpr int kW = Smem::kWarpsPerCta;
@@ -345,6 +348,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
 __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin, uint32_t* vout,
                           bool with_values, const uint64_t* d_n, uint64_t n_host, const uint32_t* gate,
                           uint32_t gate_run) {
+    pdl_prologue();
     if (gate && *gate != gate_run) return;
     const uint64_t n = load_n(d_n, n_host);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -430,12 +434,12 @@ static PassParams pass_params(const SortArgs& a, int i) {
 void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
     // The histogram pass also validates the key range, so it runs even when
     // there is no digit to sort.
-    radix_histogram<<<a.grid_hist, kSortThreads, 0, s>>>(a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
+    launch_pdl(radix_histogram, dim3(a.grid_hist), dim3(kSortThreads), 0, s, a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
                                                          a.validate_bits, a.hist, a.status[0], a.err,
                                                          a.seg_offsets, a.seg_count, a.seg_shift, a.gate,
                                                          a.gate_run);
     if (sort_passes(a.lo_bit, a.hi_bit) == 0)
-        copy_keys<<<a.grid_hist, 256, 0, s>>>(a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
+        launch_pdl(copy_keys, dim3(a.grid_hist), dim3(256), 0, s, a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
                                               a.d_n, a.n, a.gate, a.gate_run);
 }
 
@@ -443,8 +447,8 @@ void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
     const PassParams p = pass_params(a, i);
     const ShapeEntry& e = kShapes[a.shape < 0 || a.shape >= kNumSortShapes ? 1 : a.shape];
     void* args[] = {const_cast<PassParams*>(&p)};
-    cudaLaunchKernel(a.with_values ? (const void*)e.pairs : (const void*)e.keys, dim3(a.grid_pass),
-                     dim3(kPassThreads), args, a.with_values ? e.smem_pairs : e.smem_keys, s);
+    launch_pdl_c(a.with_values ? (const void*)e.pairs : (const void*)e.keys, dim3(a.grid_pass), dim3(kPassThreads),
+                 args, a.with_values ? e.smem_pairs : e.smem_keys, s);
 }
 
 void launch_sort(const SortArgs& a, cudaStream_t s) {
