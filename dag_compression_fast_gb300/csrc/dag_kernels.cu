@@ -654,6 +654,28 @@ __global__ void remap_children(const uint32_t* __restrict__ in, const uint32_t* 
     }
 }
 
+template <typename T>
+__device__ __forceinline__ void copy_units(const CopySeg& c, uint64_t t0, uint64_t stride) {
+    const T* src = static_cast<const T*>(c.src);
+    T* dst = static_cast<T*>(c.dst);
+    const uint64_t n = c.bytes / sizeof(T);
+    for (uint64_t i = t0; i < n; i += stride) dst[i] = src[i];
+}
+
+__global__ void __launch_bounds__(256) copy_segments(CopyTable t) {
+    pdl_prologue();
+    if (blockIdx.x == 0 && blockIdx.y == 0 && (int)threadIdx.x < t.lit_count) t.lit_dst[threadIdx.x] = t.lit[threadIdx.x];
+    if ((int)blockIdx.y >= t.count) return;
+    const CopySeg c = t.seg[blockIdx.y];
+    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t align = (uint64_t)(uintptr_t)c.src | (uint64_t)(uintptr_t)c.dst | c.bytes;
+    if ((align & 15) == 0) copy_units<uint4>(c, t0, stride);
+    else if ((align & 7) == 0) copy_units<uint64_t>(c, t0, stride);
+    else if ((align & 3) == 0) copy_units<uint32_t>(c, t0, stride);
+    else copy_units<uint8_t>(c, t0, stride);
+}
+
 __global__ void iota_offset(uint32_t* out, uint64_t n, uint32_t offset) {
     pdl_prologue();
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
@@ -721,6 +743,14 @@ void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* ou
     const uint64_t words = n_nodes * 8;
     const int grid = (int)std::min<uint64_t>((words + 255) / 256, (uint64_t)g_blocks_small);
     launch_pdl(remap_children, dim3(grid), dim3(256), 0, s, in, map, out, words);
+}
+void launch_copy_segments(const CopyTable& t, cudaStream_t s) {
+    if (t.count <= 0 && t.lit_count <= 0) return;
+    uint64_t most = 0;
+    for (int i = 0; i < t.count; ++i) most = std::max<uint64_t>(most, t.seg[i].bytes);
+    const uint64_t want = (most / 16 + 255) / 256;
+    const int gx = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)g_blocks_small));
+    launch_pdl(copy_segments, dim3(gx, (unsigned)std::max(t.count, 1)), dim3(256), 0, s, t);
 }
 void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s) {
     if (n == 0) return;

@@ -228,6 +228,11 @@ struct dagc_context_t {
     std::string last_error;
     std::vector<uint64_t> last_counts;
     uint64_t* h_stage = nullptr;  // pinned: counts + error word read back
+    // CreateDAG returns while its DAG is still being copied out of the arena:
+    // the next call that writes the arena waits for this event first.
+    cudaEvent_t arena_copy = nullptr;
+    bool arena_copy_pending = false;
+    std::vector<cudaEvent_t> free_sync_events;  // DAG readiness events, reused
     std::mutex mu;
 };
 
@@ -242,6 +247,10 @@ struct dagc_dag_t {
     uint8_t* masks = nullptr;
     uint64_t* leaves = nullptr;
     uint64_t* d_level_offset = nullptr;
+    // Recorded after the kernel that fills the block, when the call that made
+    // the DAG returned before that kernel finished (CreateDAG); null when the
+    // block was complete on return.
+    cudaEvent_t ready = nullptr;
     uint64_t num_nodes() const { return level_offset.empty() ? 0 : level_offset.back(); }
 };
 
@@ -276,6 +285,31 @@ cudaEvent_t take_event(dagc_context ctx) {
     cudaEvent_t e = nullptr;
     if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return nullptr; }
     return e;
+}
+
+cudaEvent_t take_sync_event(dagc_context ctx) {
+    if (!ctx->free_sync_events.empty()) {
+        cudaEvent_t e = ctx->free_sync_events.back();
+        ctx->free_sync_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return e;
+}
+
+// Work on stream `s` that reads DAG `d` waits until its block is complete.
+void dag_ready_wait(dagc_dag d, cudaStream_t s) {
+    if (d && d->ready) cudaStreamWaitEvent(s, d->ready, 0);
+}
+// The host waits until DAG `d`'s block is complete.
+void dag_ready_sync(dagc_dag d) {
+    if (d && d->ready) cudaEventSynchronize(d->ready);
+}
+// Work on stream `s` that writes the context's arena waits for the last copy
+// out of it.
+void arena_wait(dagc_context ctx, cudaStream_t s) {
+    if (ctx->arena_copy_pending) cudaStreamWaitEvent(s, ctx->arena_copy, 0);
 }
 
 // Brackets the launches of one stage with events on the call's stream when
@@ -462,7 +496,13 @@ int alloc_dag(dagc_context ctx, int num_levels, const std::vector<uint64_t>& lev
 
 void free_dag(dagc_dag d) {
     if (!d) return;
-    if (d->ctx) d->ctx->pool.release(d->block);
+    dag_ready_sync(d);  // the block returns to the pool only once nothing writes it
+    if (d->ctx) {
+        if (d->ready) d->ctx->free_sync_events.push_back(d->ready);
+        d->ctx->pool.release(d->block);
+    } else if (d->ready) {
+        cudaEventDestroy(d->ready);
+    }
     delete d;
 }
 
@@ -665,6 +705,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     const size_t zero_bytes = Lo.zero_bytes;
     (void)capmax;
     DAGC_CUDA(ctx, ctx->arena.reserve(Lo.total));
+    arena_wait(ctx, s);
     if (use_dedup) {
         const int st = reserve_table(ctx, Lo.table_slots, s);
         if (st) return st;
@@ -1030,17 +1071,36 @@ int materialise(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, 
     uint64_t total_u = 0;
     for (int l = 0; l < nl; ++l) total_u += p.unique[l];
     StageTimer t(ctx, DAGC_STAGE_MATERIALISE, s);
+    // Every level's arrays and the leaves in one copy kernel; the level
+    // offsets from the host. No wait: the words (CreateFinalDAG) or any read
+    // of the DAG follow on the same stream.
+    CopyTable ct{};
+    auto add = [&](const void* src, void* dst, uint64_t bytes) {
+        if (bytes) ct.seg[ct.count++] = CopySeg{src, dst, bytes};
+    };
     for (int l = 0; l < nl; ++l) {
         const uint64_t o = d->level_offset[l], u = p.unique[l];
-        if (!u) continue;
-        cudaMemcpyAsync(d->hashes + o, p.hashes[l], u * 8, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(d->children + o * 8, p.children[l], u * 32, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(d->masks + o, p.masks[l], u, cudaMemcpyDeviceToDevice, s);
+        add(p.hashes[l], d->hashes + o, u * 8);
+        add(p.children[l], d->children + o * 8, u * 32);
+        add(p.masks[l], d->masks + o, u);
     }
-    if (p.num_leaves) cudaMemcpyAsync(d->leaves, p.leaves, p.num_leaves * 8, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (nl + 1) * 8, cudaMemcpyHostToDevice, s);
+    add(p.leaves, d->leaves, p.num_leaves * 8);
+    static_assert(3 * (kMaxDepth - 2) + 1 <= kMaxCopySegs && kMaxDepth - 1 <= 24, "copy table");
+    ct.lit_dst = d->d_level_offset;
+    ct.lit_count = nl + 1;
+    for (int l = 0; l <= nl; ++l) ct.lit[l] = d->level_offset[l];
+    launch_copy_segments(ct, s);
+    ++ctx->launches;
     t.stop(2 * (41 * total_u + 8 * p.num_leaves));
-    const cudaError_t e = cudaStreamSynchronize(s);
+    cudaError_t e = cudaGetLastError();
+    d->ready = take_sync_event(ctx);
+    if (!ctx->arena_copy && cudaEventCreateWithFlags(&ctx->arena_copy, cudaEventDisableTiming) != cudaSuccess)
+        ctx->arena_copy = nullptr;
+    if (e == cudaSuccess && d->ready) e = cudaEventRecord(d->ready, s);
+    if (e == cudaSuccess && ctx->arena_copy) e = cudaEventRecord(ctx->arena_copy, s);
+    if (e == cudaSuccess && (!d->ready || !ctx->arena_copy)) e = cudaStreamSynchronize(s);  // no events: wait here
+    ctx->arena_copy_pending = ctx->arena_copy != nullptr;
+    if (ctx->profiling && e == cudaSuccess) e = cudaStreamSynchronize(s);
     settle_profile(ctx);
     if (e != cudaSuccess) {
         free_dag(d);
@@ -1068,6 +1128,8 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     const size_t zero_bytes = L.off;
     const size_t o_pos = L.take<uint32_t>(nn + 1);
     DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    arena_wait(ctx, s);
+    dag_ready_wait(d, s);
     char* b = static_cast<char*>(ctx->arena.base);
     CallHeader* h = reinterpret_cast<CallHeader*>(b + o_hdr);
     uint32_t* pos = reinterpret_cast<uint32_t*>(b + o_pos);
@@ -1087,33 +1149,43 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     a.err = &h->err;
     a.grid_scan = grid_for(ctx->grid_scan / ctx->sms, ctx->sms, scan_tiles(nn));
     a.grid_write = grid_for(8, ctx->sms, (nn + d->num_leaves + 255) / 256);
+    // Words: at most 1 + 8 per node and 2 per leaf. Allocating that bound
+    // lets the positions and the write run back to back; the exact count
+    // comes back with the error word in the call's one read-back.
+    const uint64_t bound = 9 * nn + 2 * d->num_leaves;
+    const bool by_bound = bound < (1ull << 32);
     uint64_t node_words = 0;
+    void* w = nullptr;
     StageTimer t(ctx, DAGC_STAGE_FINAL, s);
     if (nn) {
         launch_final_positions(a, s);
         ++ctx->launches;
         DAGC_LAUNCHED(ctx);
-        DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, &h->counts[0], 8, cudaMemcpyDeviceToHost, s));
-        DAGC_CUDA(ctx, cudaStreamSynchronize(s));
-        node_words = ctx->h_stage[0];
+        if (!by_bound) {
+            DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, &h->counts[0], 8, cudaMemcpyDeviceToHost, s));
+            DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+            node_words = ctx->h_stage[0];
+            if (node_words + 2 * d->num_leaves >= (1ull << 32))
+                return set_error(ctx, DAGC_ERR_TOO_LARGE, "final DAG exceeds 2^32 words");
+        }
     } else {
         DAGC_CUDA(ctx, cudaMemsetAsync(pos, 0, 4, s));
     }
-    const uint64_t total = node_words + 2 * d->num_leaves;
-    if (total >= (1ull << 32)) return set_error(ctx, DAGC_ERR_TOO_LARGE, "final DAG exceeds 2^32 words");
-    void* w = nullptr;
-    DAGC_CUDA(ctx, ctx->pool.alloc(&w, total * 4));
+    DAGC_CUDA(ctx, ctx->pool.alloc(&w, (by_bound ? bound : node_words + 2 * d->num_leaves) * 4));
     a.words = static_cast<uint32_t*>(w);
     launch_final_write(a, s);
     ++ctx->launches;
-    t.stop(nn * 2 + (41 * nn + 8 * d->num_leaves) + 4 * total);
+    t.stop();
     cudaError_t le = cudaGetLastError();
-    if (le == cudaSuccess) le = cudaMemcpyAsync(ctx->h_stage, h, 8, cudaMemcpyDeviceToHost, s);
+    if (le == cudaSuccess) le = cudaMemcpyAsync(ctx->h_stage, h, 16, cudaMemcpyDeviceToHost, s);  // err, counts[0]
     if (le == cudaSuccess) le = cudaStreamSynchronize(s);
     if (le != cudaSuccess) {
         ctx->pool.release(w);
         return set_error(ctx, cuda_status(le), std::string("final: ") + cudaGetErrorString(le));
     }
+    if (nn) node_words = ctx->h_stage[1];
+    const uint64_t total = node_words + 2 * d->num_leaves;
+    set_pending_bytes(ctx, DAGC_STAGE_FINAL, nn * 2 + (41 * nn + 8 * d->num_leaves) + 4 * total);
     settle_profile(ctx);
     std::string msg;
     const int st = device_error_status((uint32_t)ctx->h_stage[0], msg);
@@ -1173,6 +1245,8 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
     const size_t o_root_hash = L.take<uint64_t>(k);
     const size_t o_root_uid = L.take<uint32_t>(k);
     DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    arena_wait(ctx, s);
+    for (uint64_t i = 0; i < k; ++i) dag_ready_wait(in[i], s);
     char* b = static_cast<char*>(ctx->arena.base);
     auto P64 = [&](size_t o) { return reinterpret_cast<uint64_t*>(b + o); };
     auto P32 = [&](size_t o) { return reinterpret_cast<uint32_t*>(b + o); };
@@ -1450,6 +1524,8 @@ void dagc_context_destroy(dagc_context ctx) {
     cudaDeviceSynchronize();
     settle_profile(ctx);
     for (cudaEvent_t e : ctx->free_events) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->free_sync_events) cudaEventDestroy(e);
+    if (ctx->arena_copy) cudaEventDestroy(ctx->arena_copy);
     drop_graphs(ctx);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     ctx->arena.release();
@@ -1555,6 +1631,7 @@ int dagc_dag_num_leaves(dagc_dag d, uint64_t* n) {
 
 int dagc_dag_level_device(dagc_dag d, int level, const uint8_t** m, const uint32_t** c, const uint64_t** h) {
     if (!d || level < 0 || level >= d->num_levels) return DAGC_ERR_INVALID_ARGUMENT;
+    dag_ready_sync(d);
     const uint64_t o = d->level_offset[level];
     if (m) *m = d->masks + o;
     if (c) *c = d->children + o * 8;
@@ -1564,6 +1641,7 @@ int dagc_dag_level_device(dagc_dag d, int level, const uint8_t** m, const uint32
 
 int dagc_dag_leaves_device(dagc_dag d, const uint64_t** leaves) {
     if (!d || !leaves) return DAGC_ERR_INVALID_ARGUMENT;
+    dag_ready_sync(d);
     *leaves = d->leaves;
     return DAGC_OK;
 }
@@ -1573,6 +1651,7 @@ int dagc_dag_download_level(dagc_dag d, int level, uint8_t* m, uint32_t* c, uint
     dagc_context ctx = d->ctx;
     const uint64_t o = d->level_offset[level], u = d->level_offset[level + 1] - o;
     if (!u) return DAGC_OK;
+    dag_ready_sync(d);
     if (m) DAGC_CUDA(ctx, cudaMemcpy(m, d->masks + o, u, cudaMemcpyDeviceToHost));
     if (c) DAGC_CUDA(ctx, cudaMemcpy(c, d->children + o * 8, u * 32, cudaMemcpyDeviceToHost));
     if (h) DAGC_CUDA(ctx, cudaMemcpy(h, d->hashes + o, u * 8, cudaMemcpyDeviceToHost));
@@ -1581,6 +1660,7 @@ int dagc_dag_download_level(dagc_dag d, int level, uint8_t* m, uint32_t* c, uint
 
 int dagc_dag_download_leaves(dagc_dag d, uint64_t* leaves) {
     if (!d || (!leaves && d->num_leaves)) return DAGC_ERR_INVALID_ARGUMENT;
+    dag_ready_sync(d);
     if (d->num_leaves) DAGC_CUDA(d->ctx, cudaMemcpy(leaves, d->leaves, d->num_leaves * 8, cudaMemcpyDeviceToHost));
     return DAGC_OK;
 }
@@ -1649,6 +1729,7 @@ int dagc_dag_copy(dagc_context ctx, dagc_dag src, void* stream, dagc_dag* out) {
     // Same layout: one copy of the whole block.
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t bytes = reinterpret_cast<char*>(d->masks + d->num_nodes()) - reinterpret_cast<char*>(d->block);
+    dag_ready_wait(src, s);
     cudaError_t e = cudaMemcpyAsync(d->block, src->block, bytes, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -2015,6 +2096,7 @@ int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_key
     const size_t o_ka = L.take<uint64_t>(n);
     const size_t o_va = L.take<uint32_t>(with_values ? n : 0);
     DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    arena_wait(ctx, s);
     char* b = static_cast<char*>(ctx->arena.base);
     CallSlots cs;
     cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);

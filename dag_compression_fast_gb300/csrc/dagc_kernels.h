@@ -289,6 +289,24 @@ void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* ou
                            cudaStream_t s);
 void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s);
 
+// Several device-to-device copies in one launch (a DAG's levels out of the
+// call's scratch): each copy moves 16, 8, 4 or 1 bytes per thread step,
+// whichever its addresses and size allow.
+struct CopySeg {
+    const void* src;
+    void* dst;
+    uint64_t bytes;
+};
+constexpr int kMaxCopySegs = 64;
+struct CopyTable {
+    CopySeg seg[kMaxCopySegs];
+    int count;
+    uint64_t* lit_dst;  // and up to 24 words given by value (a DAG's level offsets)
+    uint64_t lit[24];
+    int lit_count;
+};
+void launch_copy_segments(const CopyTable& t, cudaStream_t s);
+
 void kernels_configure();
 
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
