@@ -662,18 +662,25 @@ __device__ __forceinline__ void copy_units(const CopySeg& c, uint64_t t0, uint64
     for (uint64_t i = t0; i < n; i += stride) dst[i] = src[i];
 }
 
+// CTA b copies piece b - first_cta[k] of segment k, where first_cta[k] <= b <
+// first_cta[k + 1]; a piece is up to kCopyPiece bytes.
 __global__ void __launch_bounds__(256) copy_segments(CopyTable t) {
     pdl_prologue();
-    if (blockIdx.x == 0 && blockIdx.y == 0 && (int)threadIdx.x < t.lit_count) t.lit_dst[threadIdx.x] = t.lit[threadIdx.x];
-    if ((int)blockIdx.y >= t.count) return;
-    const CopySeg c = t.seg[blockIdx.y];
-    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    if (blockIdx.x == 0 && (int)threadIdx.x < t.lit_count) t.lit_dst[threadIdx.x] = t.lit[threadIdx.x];
+    int k = 0;
+    while (k + 1 < t.count && t.first_cta[k + 1] <= blockIdx.x) ++k;
+    if (k >= t.count || blockIdx.x >= t.first_cta[t.count]) return;
+    CopySeg c = t.seg[k];
+    const uint64_t off = (uint64_t)(blockIdx.x - t.first_cta[k]) * kCopyPiece;
+    const uint64_t len = c.bytes - off < kCopyPiece ? c.bytes - off : kCopyPiece;
+    c.src = static_cast<const char*>(c.src) + off;
+    c.dst = static_cast<char*>(c.dst) + off;
+    c.bytes = len;
     const uint64_t align = (uint64_t)(uintptr_t)c.src | (uint64_t)(uintptr_t)c.dst | c.bytes;
-    if ((align & 15) == 0) copy_units<uint4>(c, t0, stride);
-    else if ((align & 7) == 0) copy_units<uint64_t>(c, t0, stride);
-    else if ((align & 3) == 0) copy_units<uint32_t>(c, t0, stride);
-    else copy_units<uint8_t>(c, t0, stride);
+    if ((align & 15) == 0) copy_units<uint4>(c, threadIdx.x, blockDim.x);
+    else if ((align & 7) == 0) copy_units<uint64_t>(c, threadIdx.x, blockDim.x);
+    else if ((align & 3) == 0) copy_units<uint32_t>(c, threadIdx.x, blockDim.x);
+    else copy_units<uint8_t>(c, threadIdx.x, blockDim.x);
 }
 
 __global__ void iota_offset(uint32_t* out, uint64_t n, uint32_t offset) {
@@ -746,11 +753,14 @@ void launch_remap_children(const uint32_t* in, const uint32_t* map, uint32_t* ou
 }
 void launch_copy_segments(const CopyTable& t, cudaStream_t s) {
     if (t.count <= 0 && t.lit_count <= 0) return;
-    uint64_t most = 0;
-    for (int i = 0; i < t.count; ++i) most = std::max<uint64_t>(most, t.seg[i].bytes);
-    const uint64_t want = (most / 16 + 255) / 256;
-    const int gx = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)g_blocks_small));
-    launch_pdl(copy_segments, dim3(gx, (unsigned)std::max(t.count, 1)), dim3(256), 0, s, t);
+    CopyTable c = t;
+    uint64_t ctas = 0;
+    for (int i = 0; i < c.count; ++i) {
+        c.first_cta[i] = (uint32_t)ctas;
+        ctas += (c.seg[i].bytes + kCopyPiece - 1) / kCopyPiece;
+    }
+    c.first_cta[c.count] = (uint32_t)ctas;
+    launch_pdl(copy_segments, dim3((unsigned)std::max<uint64_t>(ctas, 1)), dim3(256), 0, s, c);
 }
 void launch_iota_offset(uint32_t* out, uint64_t n, uint32_t offset, cudaStream_t s) {
     if (n == 0) return;

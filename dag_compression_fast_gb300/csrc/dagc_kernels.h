@@ -298,8 +298,10 @@ struct CopySeg {
     uint64_t bytes;
 };
 constexpr int kMaxCopySegs = 64;
+constexpr uint64_t kCopyPiece = 4096;  // bytes per CTA: one 16-byte unit per thread
 struct CopyTable {
     CopySeg seg[kMaxCopySegs];
+    uint32_t first_cta[kMaxCopySegs + 1];  // filled by launch_copy_segments
     int count;
     uint64_t* lit_dst;  // and up to 24 words given by value (a DAG's level offsets)
     uint64_t lit[24];

@@ -105,16 +105,36 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         bool found[kIlp];
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) found[k] = false;
+        // Leaf masks repeat (many items per key): read first, so that hot
+        // slots are not serialised on atomics. Node hashes are nearly all
+        // distinct: claim directly (one round trip instead of two).
+        // Each round issues every pending item's read, then every claim,
+        // back to back (no result is used before the last one is issued).
+        const bool read_first = a.sampled;
         for (uint64_t probe = 0; probe < S; ++probe) {
+            bool pend[kIlp], claim[kIlp];
+            uint64_t cur[kIlp];
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k) {
+                pend[k] = live[k] && !won[k] && !found[k];
+                cur[k] = 0;
+            }
+            if (read_first) {
+#pragma unroll
+                for (int k = 0; k < kIlp; ++k)
+                    if (pend[k]) cur[k] = ld_relaxed(a.table_key + s[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k) claim[k] = pend[k] && cur[k] == 0;
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k)
+                if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + s[k]), 0ull, (unsigned long long)h[k]);
             bool any = false;
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
-                if (!live[k] || won[k] || found[k]) continue;
-                uint64_t cur = ld_relaxed(a.table_key + s[k]);
-                if (cur == 0)
-                    cur = atomicCAS((unsigned long long*)(a.table_key + s[k]), 0ull, (unsigned long long)h[k]);
-                if (cur == 0) won[k] = true;
-                else if (cur == h[k]) found[k] = true;
+                if (!pend[k]) continue;
+                if (cur[k] == 0) won[k] = true;
+                else if (cur[k] == h[k]) found[k] = true;
                 else { s[k] = (s[k] + 1) & (S - 1); any = true; }
             }
             if (!any) break;
@@ -128,18 +148,24 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                 a.item_slot[i] = placed ? (uint32_t)s[k] : 0xFFFFFFFFu;
             }
         }
-        // Winners append to the unique list (one atomic per warp and item
-        // row). Every lane takes part in the ballots and shuffles.
+        // Winners append to the unique list: one atomic per warp for all its
+        // item rows. Every lane takes part in the ballots and shuffles.
+        uint32_t wm[kIlp];
+        uint32_t wtotal = 0;
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
-            const uint32_t wm = __ballot_sync(0xFFFFFFFFu, won[k]);
-            uint64_t pos0 = 0;
-            if (lane == 0 && wm)
-                pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)__popc(wm));
-            pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+            wm[k] = __ballot_sync(0xFFFFFFFFu, won[k]);
+            wtotal += __popc(wm[k]);
+        }
+        uint64_t pos0 = 0;
+        if (lane == 0 && wtotal)
+            pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)wtotal);
+        pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
             if (won[k]) {
                 const uint64_t i = base + k * 32 + lane;
-                const uint64_t pos = pos0 + __popc(wm & lanemask_lt());
+                const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
                 aux[2 * s[k]] = (uint32_t)i;
                 if (pos < a.uniq_cap) {
                     a.uniq_key[pos] = h[k];
@@ -149,6 +175,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     full = true;
                 }
             }
+            pos0 += __popc(wm[k]);
         }
     }
     if (bad) atomicOr(a.err, kErrBadInput);
@@ -342,21 +369,34 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
         }
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) aux[k] = s[k] < a.table_cap ? a.table_aux[s[k]] : 0;
+        // Duplicates are compared in full with their representative: every
+        // item's loads are issued before any comparison.
+        bool cmp[kIlp];
+        uint4 x0[kIlp], x1[kIlp], y0[kIlp], y1[kIlp];
+        uint8_t mx[kIlp], my[kIlp];
+#pragma unroll
+        for (int k = 0; k < kIlp; ++k) {
+            const uint64_t i = i0 + k * stride;
+            const uint32_t rep = (uint32_t)aux[k];
+            cmp[k] = a.masks && i < n && s[k] < a.table_cap && rep != (uint32_t)i && rep < n;
+            if (cmp[k]) {
+                const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
+                const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                x0[k] = x[0]; x1[k] = x[1]; y0[k] = y[0]; y1[k] = y[1];
+                mx[k] = a.masks[i]; my[k] = a.masks[rep];
+            }
+        }
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
             const uint64_t i = i0 + k * stride;
             if (i >= n) continue;
             uint32_t uid = 0;
             if (s[k] < a.table_cap) {
-                const uint32_t rep = (uint32_t)aux[k];
                 uid = (uint32_t)(aux[k] >> 32);
-                if (a.masks && rep != (uint32_t)i && rep < n) {
-                    const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
-                    const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
-                    const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
-                    collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
-                                 x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
-                }
+                if (cmp[k])
+                    collision |= mx[k] != my[k] || x0[k].x != y0[k].x || x0[k].y != y0[k].y || x0[k].z != y0[k].z ||
+                                 x0[k].w != y0[k].w || x1[k].x != y1[k].x || x1[k].y != y1[k].y ||
+                                 x1[k].z != y1[k].z || x1[k].w != y1[k].w;
                 a.table_key[s[k]] = 0;  // leave the table empty for the next level
             }
             // Ids stay inside the next level's arrays even when a fallback or
