@@ -33,6 +33,7 @@ OPT_GRAPHS = 3
 OPT_DEDUP = 4
 OPT_DEDUP_UNIQUE_LIMIT = 5
 OPT_GROUP = 6
+OPT_PDL = 7
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
 NUM_SORT_SHAPES = 8

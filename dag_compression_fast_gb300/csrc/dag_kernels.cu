@@ -654,12 +654,22 @@ __global__ void remap_children(const uint32_t* __restrict__ in, const uint32_t* 
     }
 }
 
+// Up to kCopyUnroll units per thread: every load is issued before any store.
+constexpr int kCopyUnroll = 8;
 template <typename T>
 __device__ __forceinline__ void copy_units(const CopySeg& c, uint64_t t0, uint64_t stride) {
     const T* src = static_cast<const T*>(c.src);
     T* dst = static_cast<T*>(c.dst);
     const uint64_t n = c.bytes / sizeof(T);
-    for (uint64_t i = t0; i < n; i += stride) dst[i] = src[i];
+    for (uint64_t i0 = t0; i0 < n; i0 += stride * kCopyUnroll) {
+        T v[kCopyUnroll];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u)
+            if (i0 + u * stride < n) v[u] = src[i0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u)
+            if (i0 + u * stride < n) dst[i0 + u * stride] = v[u];
+    }
 }
 
 // CTA b copies piece b - first_cta[k] of segment k, where first_cta[k] <= b <

@@ -13,6 +13,7 @@
 #include "../../include/dagc.h"
 #include "dagc_hash.h"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 #include <algorithm>
 #include <cmath>
@@ -216,6 +217,7 @@ struct dagc_context_t {
     // scratch (kGroupScratchBytes): the brick masks.
     bool use_dedup = true;
     int group_mode = 1;  // DAGC_OPT_GROUP
+    bool pdl = false;    // DAGC_OPT_PDL
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
     void* gtable = nullptr;  // fragment grouping scratch
@@ -414,6 +416,7 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
              uint32_t* vals_alt, bool with_values, uint64_t n_bound, const uint64_t* d_n, int lo, int hi,
              int validate_bits, cudaStream_t s, int hist_stage = -1, int pass_stage = -1,
              const SegmentSpec* seg = nullptr, const uint32_t* gate = nullptr, uint32_t gate_run = 0) {
+    t_pdl = ctx->pdl;
     if (cs.next_hist >= kMaxSorts || cs.next_counter + kMaxPasses > kMaxTileCounters)
         return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many sorts in one call");
     SortArgs a{};
@@ -696,6 +699,7 @@ constexpr int kStatusFallback = -1000;
 
 int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int depth, cudaStream_t s,
                     CreatePools& out, const BatchSpec* batch, bool use_dedup) {
+    t_pdl = ctx->pdl;
     const int group_mode = ctx->group_mode;
     const int nl = depth - 2;
     const int bits = 3 * depth;
@@ -1065,6 +1069,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
 }
 
 int materialise(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, dagc_dag* out) {
+    t_pdl = ctx->pdl;
     dagc_dag d = nullptr;
     int st = alloc_dag(ctx, nl, p.unique, p.num_leaves, &d);
     if (st) return st;
@@ -1117,6 +1122,7 @@ int empty_dag(dagc_context ctx, int nl, dagc_dag* out) {
 
 // --------------------------------------------------------- CreateFinalDAG --
 int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, uint64_t* n_words) {
+    t_pdl = ctx->pdl;
     *d_words = nullptr;
     *n_words = 0;
     if (d->num_leaves == 0) return DAGC_OK;
@@ -1203,6 +1209,7 @@ struct HostNode {
 };
 
 int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_dag* out) {
+    t_pdl = ctx->pdl;
     const int nl = in[0]->num_levels;
     int m = 0;
     for (uint64_t x = k; x > 1; x /= 8) ++m;
@@ -1489,6 +1496,7 @@ int dagc_context_create(int device, dagc_context* out) {
     if (const char* g = std::getenv("DAGC_GRAPHS")) c->use_graphs = std::atoi(g) != 0;
     if (const char* d = std::getenv("DAGC_DEDUP")) c->use_dedup = std::atoi(d) != 0;
     if (const char* gm = std::getenv("DAGC_GROUP")) c->group_mode = std::min(2, std::max(0, std::atoi(gm)));
+    if (const char* pd = std::getenv("DAGC_PDL")) c->pdl = std::atoi(pd) != 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumSortShapes; ++sh) {
         c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
@@ -1877,6 +1885,10 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
             return DAGC_OK;
         case DAGC_OPT_DEDUP:
             ctx->use_dedup = value != 0;
+            return DAGC_OK;
+        case DAGC_OPT_PDL:
+            if (ctx->pdl != (value != 0)) drop_graphs(ctx);  // recorded graphs keep their launch attributes
+            ctx->pdl = value != 0;
             return DAGC_OK;
         case DAGC_OPT_GROUP:
             if (value < 0 || value > 2) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "group mode must be 0, 1 or 2");

@@ -298,7 +298,7 @@ struct CopySeg {
     uint64_t bytes;
 };
 constexpr int kMaxCopySegs = 64;
-constexpr uint64_t kCopyPiece = 4096;  // bytes per CTA: one 16-byte unit per thread
+constexpr uint64_t kCopyPiece = 32768;  // bytes per CTA: eight 16-byte units per thread
 struct CopyTable {
     CopySeg seg[kMaxCopySegs];
     uint32_t first_cta[kMaxCopySegs + 1];  // filled by launch_copy_segments

@@ -1,12 +1,18 @@
 // Host side of programmatic dependent launch: kernels whose first statement
-// is pdl_prologue() are launched with programmatic stream serialization, so
-// that a chain of small dependent kernels (and the CUDA graph recorded from
-// it) does not pay a full launch gap per kernel.
+// is pdl_prologue() can be launched with programmatic stream serialization, so
+// that the next kernel is scheduled while the previous one runs. Off unless
+// the context's DAGC_OPT_PDL asks for it: on GB300 plain stream order measured
+// faster for this pipeline.
 #pragma once
 
 #include <cuda_runtime.h>
 
 namespace dagc {
+
+// Whether launch_pdl sets the attribute; set from the calling context's
+// DAGC_OPT_PDL at the start of each call that launches kernels (the launches
+// of a call happen on the calling thread).
+inline thread_local bool t_pdl = false;
 
 inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                                      cudaLaunchAttribute* attr) {
@@ -18,7 +24,7 @@ inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, size_t smem, cudaStr
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = t_pdl ? 1 : 0;
     return cfg;
 }
 

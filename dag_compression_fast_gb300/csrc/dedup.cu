@@ -70,6 +70,8 @@ __device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
 // Items per lane in flight at once (independent probe chains).
 constexpr int kIlp = 4;
 
+constexpr uint64_t kDedupClaimFirstMax = 1ull << 20;  // items
+
 __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     pdl_prologue();
     const uint64_t n = *a.d_n;
@@ -105,12 +107,13 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         bool found[kIlp];
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) found[k] = false;
-        // Leaf masks repeat (many items per key): read first, so that hot
-        // slots are not serialised on atomics. Node hashes are nearly all
-        // distinct: claim directly (one round trip instead of two).
-        // Each round issues every pending item's read, then every claim,
-        // back to back (no result is used before the last one is issued).
-        const bool read_first = a.sampled;
+        // Leaf masks repeat (many items per key), and large levels are bound
+        // by L2 atomic throughput: read first, claim only an empty slot.
+        // Small node levels are bound by latency: claim directly (one round
+        // trip instead of two). Each round issues every pending item's read,
+        // then every claim, back to back (no result is used before the last
+        // one is issued).
+        const bool read_first = a.sampled || n > kDedupClaimFirstMax;
         for (uint64_t probe = 0; probe < S; ++probe) {
             bool pend[kIlp], claim[kIlp];
             uint64_t cur[kIlp];
@@ -369,34 +372,21 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
         }
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) aux[k] = s[k] < a.table_cap ? a.table_aux[s[k]] : 0;
-        // Duplicates are compared in full with their representative: every
-        // item's loads are issued before any comparison.
-        bool cmp[kIlp];
-        uint4 x0[kIlp], x1[kIlp], y0[kIlp], y1[kIlp];
-        uint8_t mx[kIlp], my[kIlp];
-#pragma unroll
-        for (int k = 0; k < kIlp; ++k) {
-            const uint64_t i = i0 + k * stride;
-            const uint32_t rep = (uint32_t)aux[k];
-            cmp[k] = a.masks && i < n && s[k] < a.table_cap && rep != (uint32_t)i && rep < n;
-            if (cmp[k]) {
-                const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
-                const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
-                x0[k] = x[0]; x1[k] = x[1]; y0[k] = y[0]; y1[k] = y[1];
-                mx[k] = a.masks[i]; my[k] = a.masks[rep];
-            }
-        }
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
             const uint64_t i = i0 + k * stride;
             if (i >= n) continue;
             uint32_t uid = 0;
             if (s[k] < a.table_cap) {
+                const uint32_t rep = (uint32_t)aux[k];
                 uid = (uint32_t)(aux[k] >> 32);
-                if (cmp[k])
-                    collision |= mx[k] != my[k] || x0[k].x != y0[k].x || x0[k].y != y0[k].y || x0[k].z != y0[k].z ||
-                                 x0[k].w != y0[k].w || x1[k].x != y1[k].x || x1[k].y != y1[k].y ||
-                                 x1[k].z != y1[k].z || x1[k].w != y1[k].w;
+                if (a.masks && rep != (uint32_t)i && rep < n) {
+                    const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
+                    const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
+                    const uint4 x0 = x[0], x1 = x[1], y0 = y[0], y1 = y[1];
+                    collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
+                                 x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
+                }
                 a.table_key[s[k]] = 0;  // leave the table empty for the next level
             }
             // Ids stay inside the next level's arrays even when a fallback or

@@ -174,6 +174,12 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * average, else the radix sort; 0 always the radix sort; 2 always the hash
  * table. Results are identical. */
 #define DAGC_OPT_GROUP 6
+/* 1: launch every kernel of a call with programmatic dependent launch (the
+ * next kernel is scheduled while the previous one runs and waits for it on the
+ * device); 0 (default): plain stream order, which measured faster on GB300 for
+ * every workload here (config 3: 7.1 ms against 8.3 ms). Results are
+ * identical. */
+#define DAGC_OPT_PDL 7
 int dagc_set_option(dagc_context ctx, int option, int value);
 /* Calls of this context rerun in the radix form so far. */
 int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
