@@ -223,7 +223,7 @@ struct DedupArgs {
     uint32_t* err;
 };
 void dedup_configure(int sms);
-int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (4 or 5)
+int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (3 or 5)
 
 // Headless tracer (trace.cu): one primary ray per pixel through the final
 // word layout of a depth-`depth` DAG (depth >= 3).

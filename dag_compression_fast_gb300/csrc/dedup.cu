@@ -8,15 +8,19 @@
 //
 //   dedup_insert   every item inserts its key into an open-addressing table
 //                  (linear probing, atomicCAS on the key); the first inserter
-//                  of a key appends (key, slot, itself) to the unique list and
-//                  records itself as the slot's representative;
+//                  of a key records itself as the slot's representative and
+//                  appends (key, slot, itself) to the unique list (leaf
+//                  masks) or straight to its bucket (node hashes: the bucket
+//                  count follows from the item count, so no other pass is
+//                  needed; dedup_map of the previous level zeroed the bucket
+//                  counters);
 //   dedup_split    (leaf masks only) one CTA sorts a strided sample of 4 keys
 //                  per bucket and picks the bucket splitters: the keys are
 //                  distinct, so bucket sizes depend only on ranks, whatever
 //                  the key distribution. Node hashes are MurmurHash outputs:
 //                  their top bits are the bucket, no sample needed;
-//   dedup_scatter  unique keys, with their slot and representative, go to
-//                  fixed-capacity buckets (4x to 8x the
+//   dedup_scatter  (leaf masks only) unique keys, with their slot and
+//                  representative, go to fixed-capacity buckets (4x to 8x the
 //                  expected keys; sampled buckets grow past 256 expected keys
 //                  once there are 4096 of them);
 //   dedup_sort     each bucket is ranked in shared memory (rank = number of
@@ -79,10 +83,24 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t b = gtid; b < kDedupMaxBuckets; b += gsize) a.bucket_count[b] = 0;
+    // Leaf masks: the bucket counters are zeroed here (dedup_scatter fills
+    // them after this kernel). Node hashes are uniform, so their top bits
+    // give the bucket at once: winners append straight to their bucket, and
+    // the previous level's dedup_map left the counters zero.
+    if (a.sampled)
+        for (uint64_t b = gtid; b < kDedupMaxBuckets; b += gsize) a.bucket_count[b] = 0;
     if (S > a.table_cap || n > a.item_cap) {
         if (gtid == 0) atomicOr(a.err, kErrFallback);
         return;
+    }
+    int shift = 64;
+    const uint32_t nb = a.sampled ? 0u : topbit_buckets(n, &shift);
+    if (!a.sampled) {
+        if ((uint64_t)nb * kDedupTopBitCap > a.bucket_area) {
+            if (gtid == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
+            return;
+        }
+        if (gtid == 0) a.state->nbuckets = nb;
     }
     uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);  // [2s] representative, [2s+1] unique id
     const uint64_t warps = gsize / 32;
@@ -164,21 +182,49 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         if (lane == 0 && wtotal)
             pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)wtotal);
         pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+        if (a.sampled) {
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) {
-            if (won[k]) {
-                const uint64_t i = base + k * 32 + lane;
-                const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
-                aux[2 * s[k]] = (uint32_t)i;
-                if (pos < a.uniq_cap) {
-                    a.uniq_key[pos] = h[k];
-                    a.uniq_slot[pos] = (uint32_t)s[k];
-                    a.uniq_item[pos] = (uint32_t)i;
-                } else {
-                    full = true;
+            for (int k = 0; k < kIlp; ++k) {
+                if (won[k]) {
+                    const uint64_t i = base + k * 32 + lane;
+                    const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
+                    aux[2 * s[k]] = (uint32_t)i;
+                    if (pos < a.uniq_cap) {
+                        a.uniq_key[pos] = h[k];
+                        a.uniq_slot[pos] = (uint32_t)s[k];
+                        a.uniq_item[pos] = (uint32_t)i;
+                    } else {
+                        full = true;
+                    }
                 }
+                pos0 += __popc(wm[k]);
             }
-            pos0 += __popc(wm[k]);
+        } else {
+            // Every winner's bucket slot is reserved before any is used.
+            uint32_t bslot[kIlp];
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k) {
+                const uint32_t b = shift >= 64 ? 0u : (uint32_t)(h[k] >> shift);
+                bslot[k] = won[k] ? atomicAdd(a.bucket_count + b, 1u) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < kIlp; ++k) {
+                if (won[k]) {
+                    const uint64_t i = base + k * 32 + lane;
+                    const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
+                    const uint32_t b = shift >= 64 ? 0u : (uint32_t)(h[k] >> shift);
+                    aux[2 * s[k]] = (uint32_t)i;
+                    if (pos < a.uniq_cap && bslot[k] < kDedupTopBitCap) {
+                        const uint64_t e = (uint64_t)b * kDedupTopBitCap + bslot[k];
+                        a.bucket_key[e] = h[k];
+                        a.bucket_slot[e] = (uint32_t)s[k];
+                        a.bucket_rep[e] = (uint32_t)i;
+                    } else {
+                        full = true;
+                    }
+                }
+                pos0 += __popc(wm[k]);
+            }
         }
     }
     if (bad) atomicOr(a.err, kErrBadInput);
@@ -288,6 +334,7 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     __shared__ uint32_t red[kBucketThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nb = a.state->nbuckets;
+    if (!a.sampled && blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = unique_count(a);
     if (nb == 0) return;
     const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
     const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
@@ -356,6 +403,10 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
 
 __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
     pdl_prologue();
+    // The bucket counters, read by dedup_sort, start the next level at zero.
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < kDedupMaxBuckets;
+         b += (uint64_t)gridDim.x * blockDim.x)
+        a.bucket_count[b] = 0;
     const uint64_t n = *a.d_n;
     if (table_size_for(n) > a.table_cap || n > a.item_cap) return;  // insert did nothing
     const uint32_t last = a.out_capacity ? (uint32_t)(a.out_capacity - 1) : 0u;
@@ -419,12 +470,15 @@ int launch_dedup(const DedupArgs& a, cudaStream_t s) {
         launch_pdl(dedup_split, dim3(1), dim3(kSplitThreads), kDedupMaxSample * 8, s, a);
         ++launches;
     }
-    launch_pdl(dedup_scatter, dim3(gi), dim3(256), a.sampled ? kDedupMaxSampledBuckets * 8 : 0, s, a);
+    if (a.sampled) {  // node levels appended to their buckets in dedup_insert
+        launch_pdl(dedup_scatter, dim3(gi), dim3(256), kDedupMaxSampledBuckets * 8, s, a);
+        ++launches;
+    }
     const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
     const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
     launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s, a);
     launch_pdl(dedup_map, dim3(gi), dim3(256), 0, s, a);
-    return launches + 3;
+    return launches + 2;
 }
 
 }  // namespace dagc

@@ -129,8 +129,9 @@ def test_dedup_rerun_when_unique_list_is_full():
 
 
 def test_dedup_form_is_the_one_that_runs():
-    """Four or five launches per deduplicated level instead of a radix sort's
-    ten or more: the launch counter tells the two forms apart."""
+    """Three (node levels) or five (leaves) launches per deduplicated level
+    instead of a radix sort's ten or more: the launch counter tells the two
+    forms apart."""
     codes, depth = CASES["clustered_d10"]()
     launches = {}
     for form in (0, 1):
