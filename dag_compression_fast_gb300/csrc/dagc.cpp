@@ -758,6 +758,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.seg_code = batch ? P64(Lo.o_seg_code) : nullptr;
             g.validate_bits = validate;
             g.mode = group_mode;
+            g.narrow = sort_hi <= 37 ? 1 : 0;
             g.chunks = group_chunks(n);
             g.sketch = cs.h->sketch;
             g.hist = cs.h->ghist;

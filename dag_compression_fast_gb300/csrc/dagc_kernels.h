@@ -135,6 +135,7 @@ struct GroupArgs {
     const uint64_t* seg_code;                                         // chunk Morton index per segment
     int validate_bits;
     int mode;                  // 1: choose by the sketch, 2: always group (tests)
+    int narrow;                // every key below 2^37 (bricks below 2^31): 32-bit hashes and table keys
     int chunks;                // CTAs of the scatter: chunk c = [c*L, (c+1)*L), L = ceil(n / chunks)
     uint32_t* sketch;          // kGroupSketchRegs words, zero
     uint64_t* hist;            // kGroupMaxParts fragment counts per fine partition, zero

@@ -35,6 +35,8 @@
 #include "dagc_kernels.h"
 #include "dagc_launch.h"
 
+#include <type_traits>
+
 namespace dagc {
 namespace {
 
@@ -54,13 +56,21 @@ __device__ __forceinline__ uint64_t brick_hash(uint64_t brick) { return fmix(bri
 
 // The partition's hash, one multiply (Fibonacci hashing): its top
 // kGroupPartLog bits are the fine partition, the bits below them the slot in
-// the partition's table.
-__device__ __forceinline__ uint64_t part_hash(uint64_t brick) { return brick * 0x9E3779B97F4A7C15ull; }
-__device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
-    return lp ? (uint32_t)(part_hash(key >> 6) >> (64 - lp)) : 0u;
+// the partition's table. Narrow form (every brick below 2^31): a 32-bit
+// multiply of the brick, and 32-bit table keys.
+template <bool kNarrow>
+__device__ __forceinline__ uint32_t fine_part(uint64_t brick) {
+    if (kNarrow) return ((uint32_t)brick * 0x9E3779B1u) >> (32 - kGroupPartLog);
+    return (uint32_t)((brick * 0x9E3779B97F4A7C15ull) >> (64 - kGroupPartLog));
 }
+template <bool kNarrow>
+__device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
+    return lp ? fine_part<kNarrow>(key >> 6) >> (kGroupPartLog - lp) : 0u;
+}
+template <bool kNarrow>
 __device__ __forceinline__ uint32_t slot_of(uint64_t brick, uint32_t lt) {
-    return (uint32_t)(part_hash(brick) >> (64 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+    if (kNarrow) return (((uint32_t)brick * 0x9E3779B1u) >> (32 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+    return (uint32_t)((brick * 0x9E3779B97F4A7C15ull) >> (64 - kGroupPartLog - lt)) & ((1u << lt) - 1);
 }
 
 __device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t count, uint64_t i) {
@@ -93,6 +103,7 @@ static_assert(kSketchRegs == kGroupSketchRegs, "sketch size");
 constexpr int kFrontThreads = 512;
 constexpr int kSketchIlp = 8;
 
+template <bool kNarrow>
 __global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
     pdl_prologue();
     __shared__ uint32_t reg[kSketchRegs];
@@ -117,7 +128,7 @@ __global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
             const uint64_t h = brick_hash(brick);
             const uint32_t rank = (uint32_t)__clzll((h << kSketchLog) | (1ull << (kSketchLog - 1))) + 1;
             atomicMax(&reg[h >> (64 - kSketchLog)], rank);
-            atomicAdd(&hist[part_hash(brick) >> (64 - kGroupPartLog)], 1u);
+            atomicAdd(&hist[fine_part<kNarrow>(brick)], 1u);
         }
     }
     if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31) == 0) atomicOr(a.err, kErrBadInput);
@@ -245,6 +256,7 @@ __device__ __forceinline__ void scatter_prefetch(ScatterSmem& sm, const uint64_t
     cp_async_commit();
 }
 
+template <bool kNarrow>
 __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -272,7 +284,7 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
             const uint64_t i = base + (uint64_t)k * kScatterThreads + threadIdx.x;
             if (i >= hi) continue;
             key[k] = key_of(a, i, key[k], &bad);
-            const uint32_t pid = part_of(key[k], lp);
+            const uint32_t pid = part_of<kNarrow>(key[k], lp);
             pr[k] = (pid << 16) | atomicAdd(&sm.cnt[pid], 1u);
         }
         __syncthreads();
@@ -314,7 +326,7 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
 #pragma unroll 4
         for (uint32_t q = threadIdx.x; q < m; q += kScatterThreads) {
             const uint64_t k = sm.stage[q];
-            a.parts[(int64_t)sm.delta[part_of(k, lp)] + q] = k;
+            a.parts[(int64_t)sm.delta[part_of<kNarrow>(k, lp)] + q] = k;
         }
         for (int p = threadIdx.x; p < parts; p += kScatterThreads) sm.cnt[p] = 0;  // read last before the stage barrier
     }
@@ -324,17 +336,22 @@ constexpr int kAggThreads = 512;
 constexpr int kAggIlp = 4;
 static_assert((1 << 9) >= kAggThreads, "at least one table slot per thread");
 
+template <bool kNarrow>
 struct AggSmem {
-    uint64_t key[kGroupPartSlots];   // brick + 1, 0 = empty
+    using Key = typename std::conditional<kNarrow, uint32_t, unsigned long long>::type;
     uint64_t mask[kGroupPartSlots];  // OR of the fragments' bits
+    Key key[kGroupPartSlots];        // brick + 1, 0 = empty
     uint32_t scan[34];
     uint64_t base;
 };
 
+template <bool kNarrow>
 __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    AggSmem& sm = *reinterpret_cast<AggSmem*>(smem_raw);
+    using Smem = AggSmem<kNarrow>;
+    using Key = typename Smem::Key;
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     if (a.path[0] != 1u) return;
     const uint32_t parts = 1u << a.path[1], lt = a.path[2], slots = 1u << lt;
     bool full = false;
@@ -355,19 +372,20 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
 #pragma unroll
             for (int u = 0; u < kAggIlp; ++u) {
                 if (i0 + (uint64_t)u * kAggThreads >= hi) continue;
-                const uint64_t brick = k[u] >> 6, tag = brick + 1;
-                uint32_t s = slot_of(brick, lt);
-                uint64_t cur = *reinterpret_cast<volatile uint64_t*>(&sm.key[s]);
+                const uint64_t brick = k[u] >> 6;
+                const Key tag = (Key)brick + 1;
+                uint32_t s = slot_of<kNarrow>(brick, lt);
+                Key cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
                 if (cur != tag) {
                     // Rare: the brick's first fragment here, or a collision.
                     for (uint32_t probe = 0;; ) {
                         if (cur == 0) {
-                            cur = atomicCAS((unsigned long long*)&sm.key[s], 0ull, (unsigned long long)tag);
+                            cur = atomicCAS(&sm.key[s], (Key)0, tag);
                             if (cur == 0 || cur == tag) break;
                         }
                         if (++probe == slots) { full = true; break; }  // more bricks than slots: sort path
                         s = (s + 1) & (slots - 1);
-                        cur = *reinterpret_cast<volatile uint64_t*>(&sm.key[s]);
+                        cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
                         if (cur == tag) break;
                     }
                 }
@@ -386,7 +404,7 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
         __syncthreads();
         uint64_t pos = sm.base + ex;
         for (uint32_t j = 0; j < per; ++j) {
-            const uint64_t t = sm.key[s0 + j];
+            const uint64_t t = (uint64_t)sm.key[s0 + j];
             if (t == 0) continue;
             if (pos < a.cap) {
                 a.bricks[pos] = t - 1;
@@ -442,8 +460,12 @@ int g_group_sms = 152;
 
 void group_configure(int sms) {
     g_group_sms = sms > 0 ? sms : 152;
-    cudaFuncSetAttribute(group_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ScatterSmem));
-    cudaFuncSetAttribute(group_aggregate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(AggSmem));
+    cudaFuncSetAttribute(group_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ScatterSmem));
+    cudaFuncSetAttribute(group_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ScatterSmem));
+    cudaFuncSetAttribute(group_aggregate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(AggSmem<false>));
+    cudaFuncSetAttribute(group_aggregate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(AggSmem<true>));
 }
 
 int group_chunks(uint64_t n) {
@@ -455,14 +477,19 @@ int group_chunks(uint64_t n) {
 void launch_group_sketch(const GroupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.n + kFrontThreads * kSketchIlp - 1) / (kFrontThreads * kSketchIlp);
     const int g = (int)(want < (uint64_t)(2 * g_group_sms) ? (want > 0 ? want : 1) : 2 * g_group_sms);
-    launch_pdl(group_sketch, dim3(g), dim3(kFrontThreads), 0, s, a);
+    if (a.narrow) launch_pdl(group_sketch<true>, dim3(g), dim3(kFrontThreads), 0, s, a);
+    else launch_pdl(group_sketch<false>, dim3(g), dim3(kFrontThreads), 0, s, a);
 }
 void launch_group_plan(const GroupArgs& a, cudaStream_t s) { launch_pdl(group_plan, dim3(1), dim3(kPlanThreads), 0, s, a); }
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s) {
-    launch_pdl(group_scatter, dim3(a.chunks), dim3(kScatterThreads), sizeof(ScatterSmem), s, a);
+    if (a.narrow) launch_pdl(group_scatter<true>, dim3(a.chunks), dim3(kScatterThreads), sizeof(ScatterSmem), s, a);
+    else launch_pdl(group_scatter<false>, dim3(a.chunks), dim3(kScatterThreads), sizeof(ScatterSmem), s, a);
 }
 void launch_group_aggregate(const GroupArgs& a, cudaStream_t s) {
-    launch_pdl(group_aggregate, dim3(3 * g_group_sms), dim3(kAggThreads), sizeof(AggSmem), s, a);
+    if (a.narrow)  // 48 KB of table: four CTAs per SM
+        launch_pdl(group_aggregate<true>, dim3(4 * g_group_sms), dim3(kAggThreads), sizeof(AggSmem<true>), s, a);
+    else
+        launch_pdl(group_aggregate<false>, dim3(3 * g_group_sms), dim3(kAggThreads), sizeof(AggSmem<false>), s, a);
 }
 
 void launch_group_gather(const GroupArgs& a, cudaStream_t s) {
