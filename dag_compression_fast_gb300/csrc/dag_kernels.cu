@@ -207,6 +207,27 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = load_count(a.d_n, a.n_bound);
     const uint32_t ntiles = scan_tiles(n);
+    // Fused insert (node levels of the hash-set form): table and buckets sized
+    // by the child count n, which bounds the node count.
+    const DedupArgs& dd = a.dedup;
+    bool fuse = a.fuse_insert != 0 && n <= kFuseInsertMax;
+    uint64_t tslots = 0;
+    int shift = 64;
+    uint32_t nb = 0;
+    if (fuse) {
+        tslots = table_size_for(n);
+        nb = topbit_buckets(n, &shift);
+        if (tslots > dd.table_cap || n > dd.item_cap || (uint64_t)nb * kDedupTopBitCap > dd.bucket_area) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) { atomicOr(a.err, kErrFallback); dd.state->nbuckets = 0; }
+            fuse = false;
+        } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dd.state->nbuckets = nb;
+            dd.state->inserted = 1u;
+        }
+    }
+    const bool read_first = n > kDedupClaimFirstMax;
+    uint32_t* aux = reinterpret_cast<uint32_t*>(dd.table_aux);  // [2s] representative, [2s+1] unique id
+    bool bad = false, full = false;
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
@@ -275,7 +296,40 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
             uint4* dst = reinterpret_cast<uint4*>(a.node_children + p * 8);
             dst[0] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
             dst[1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
-            a.node_hashes[p] = hash_children(h);
+            const uint64_t hv = hash_children(h);
+            a.node_hashes[p] = hv;
+            if (fuse) {
+                // The node's hash into the dedup table; the first inserter of
+                // a hash is its representative and appends it to its bucket.
+                uint64_t sl = slot_hash(hv) & (tslots - 1);
+                bool won = false, placed = false;
+                if (hv == 0) {
+                    bad = true;  // 0 marks an empty slot
+                } else {
+                    for (uint64_t probe = 0; probe < tslots; ++probe) {
+                        uint64_t cur = read_first ? ld_relaxed(dd.table_key + sl) : 0ull;
+                        if (cur == 0)
+                            cur = atomicCAS((unsigned long long*)(dd.table_key + sl), 0ull, (unsigned long long)hv);
+                        if (cur == 0 || cur == hv) { won = cur == 0; placed = true; break; }
+                        sl = (sl + 1) & (tslots - 1);
+                    }
+                }
+                if (!placed && hv != 0) full = true;
+                dd.item_slot[p] = placed ? (uint32_t)sl : 0xFFFFFFFFu;
+                if (won) {
+                    aux[2 * sl] = (uint32_t)p;
+                    const uint32_t b = shift >= 64 ? 0u : (uint32_t)(hv >> shift);
+                    const uint32_t bs = atomicAdd(dd.bucket_count + b, 1u);
+                    if (bs < kDedupTopBitCap) {
+                        const uint64_t e = (uint64_t)b * kDedupTopBitCap + bs;
+                        dd.bucket_key[e] = hv;
+                        dd.bucket_slot[e] = (uint32_t)sl;
+                        dd.bucket_rep[e] = (uint32_t)p;
+                    } else {
+                        full = true;
+                    }
+                }
+            }
             ++p;
         }
         if (overflow) atomicOr(a.err, kErrCapacity);
@@ -285,6 +339,8 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
         }
         __syncthreads();
     }
+    if (bad) atomicOr(a.err, kErrBadInput);
+    if (full) atomicOr(a.err, kErrFallback);
 }
 
 // ---------------------------------------------------------------------------

@@ -935,16 +935,20 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             e.tile_counter = cs.counter();
             e.err = err;
             e.grid = grid_for(ctx->grid_extract / ctx->sms, ctx->sms, scan_tiles(child_bound));
+            DedupArgs d{};
+            if (use_dedup) {
+                // The node hashes go into the dedup table inside extract_level.
+                d = dedup_args(P64(Lo.o_NH), cs.count(kCntNodes + l), P8(Lo.o_NM), P32(Lo.o_NCH), P64(Lo.o_ph[l]),
+                               P8(Lo.o_pm[l]), P32(Lo.o_pc[l]), cap[l], cs.count(kCntUnique + l), maps[it & 1]);
+                e.fuse_insert = 1;
+                e.dedup = d;
+            }
             launch_extract(e, s);
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
 
             if (use_dedup) {
-                ctx->launches += launch_dedup(dedup_args(P64(Lo.o_NH), cs.count(kCntNodes + l), P8(Lo.o_NM),
-                                                         P32(Lo.o_NCH), P64(Lo.o_ph[l]), P8(Lo.o_pm[l]),
-                                                         P32(Lo.o_pc[l]), cap[l], cs.count(kCntUnique + l),
-                                                         maps[it & 1]),
-                                              s);
+                ctx->launches += launch_dedup(d, s);
                 DAGC_LAUNCHED(ctx);
                 child_codes = node_codes[it & 1];
                 child_map = maps[it & 1];

@@ -21,6 +21,39 @@ __device__ __forceinline__ void pdl_prologue() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// ------------------------------------------------ hash-set dedup table ----
+// Table slots for n items: a power of two >= 2n (at least 1024).
+__device__ __forceinline__ uint64_t table_size_for(uint64_t n) {
+    const uint64_t want = n < 512 ? 1024 : 2 * n;
+    return 1ull << (64 - __clzll(want - 1));
+}
+
+__device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
+    // Finaliser of MurmurHash3 (published constants): spreads leaf masks,
+    // whose bits are far from uniform, over the table.
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// Buckets of the top-bit form: a power of two with ~kDedupPerBucket keys each
+// for u keys; a key's bucket is key >> *shift.
+__device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
+    uint32_t nb = 1;
+    int lg = 0;
+    while ((uint64_t)nb * kDedupPerBucket < u && nb < kDedupMaxBuckets) { nb <<= 1; ++lg; }
+    *shift = 64 - lg;
+    return nb;
+}
+
+// Up to this many items a node level claims its slot with one atomicCAS (one
+// round trip, latency-bound sizes); above it, it reads first and claims only
+// an empty slot (L2 atomic throughput).
+constexpr uint64_t kDedupClaimFirstMax = 1ull << 20;
+
 // Upper limit on waits: ~2^20 polls with exponential back-off capped at 1 us,
 // i.e. about one second, after which the waiter flags kErrTimeout.
 constexpr uint32_t kSpinLimit = 1u << 20;

@@ -178,15 +178,6 @@ void launch_unique(const UniqueArgs& a, cudaStream_t s);
 
 // ExtractLevel + ComputeHashes: from the sorted unique codes of the child
 // level and their child ids, build one parent node per distinct code >> 3.
-struct ExtractArgs {
-    const uint64_t* child_codes; const uint32_t* child_map; const uint64_t* d_n; uint64_t n_bound;
-    const uint64_t* child_hashes;  // unique child hashes (or leaf masks), indexed by child id
-    uint64_t* node_codes; uint8_t* node_masks; uint32_t* node_children; uint64_t* node_hashes;
-    uint64_t out_capacity;
-    uint64_t* d_out_n;
-    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
-};
-void launch_extract(const ExtractArgs& a, cudaStream_t s);
 
 // Level dedup by hash set + bucket sort (dedup.cu): same outputs as sort
 // pairs + unique_runs on (key, item) for one level.
@@ -204,6 +195,7 @@ DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) { return 8 * uniq_cap + 8 
 struct DedupState {
     unsigned long long u;  // distinct keys found (zero before the level)
     uint32_t nbuckets, bucket_cap;
+    uint32_t inserted, pad;  // 1: extract_level already inserted the level's hashes
 };
 struct DedupArgs {
     const uint64_t* keys; const uint64_t* d_n;       // items: key per item
@@ -225,6 +217,24 @@ struct DedupArgs {
 };
 void dedup_configure(int sms);
 int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (3 or 5)
+
+constexpr uint64_t kFuseInsertMax = 1ull << 20;
+struct ExtractArgs {
+    const uint64_t* child_codes; const uint32_t* child_map; const uint64_t* d_n; uint64_t n_bound;
+    const uint64_t* child_hashes;  // unique child hashes (or leaf masks), indexed by child id
+    uint64_t* node_codes; uint8_t* node_masks; uint32_t* node_children; uint64_t* node_hashes;
+    uint64_t out_capacity;
+    uint64_t* d_out_n;
+    uint64_t* status; uint32_t* tile_counter; uint32_t* err; int grid;
+    // Node levels of the hash-set form with at most kFuseInsertMax children:
+    // every node's hash goes straight into the dedup table and its top-bit
+    // bucket here (table and bucket count sized by the child count, a bound
+    // on the node count), and the level's dedup_insert returns at once.
+    // Larger levels keep the separate insert, whose probes overlap.
+    int fuse_insert;
+    DedupArgs dedup;
+};
+void launch_extract(const ExtractArgs& a, cudaStream_t s);
 
 // Headless tracer (trace.cu): one primary ray per pixel through the final
 // word layout of a depth-`depth` DAG (depth >= 3).

@@ -41,43 +41,17 @@
 namespace dagc {
 namespace {
 
-__device__ __forceinline__ uint64_t table_size_for(uint64_t n) {
-    const uint64_t want = n < 512 ? 1024 : 2 * n;
-    return 1ull << (64 - __clzll(want - 1));
-}
-
-__device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
-    // Finaliser of MurmurHash3 (published constants): spreads leaf masks,
-    // whose bits are far from uniform, over the table.
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdull;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ull;
-    k ^= k >> 33;
-    return k;
-}
-
 __device__ __forceinline__ uint64_t unique_count(const DedupArgs& a) {
     const uint64_t u = a.state->u;
     return u < a.uniq_cap ? u : a.uniq_cap;
 }
 
-// Buckets of the top-bit form: a power of two with ~kDedupPerBucket keys each.
-__device__ __forceinline__ uint32_t topbit_buckets(uint64_t u, int* shift) {
-    uint32_t nb = 1;
-    int lg = 0;
-    while ((uint64_t)nb * kDedupPerBucket < u && nb < kDedupMaxBuckets) { nb <<= 1; ++lg; }
-    *shift = 64 - lg;
-    return nb;
-}
-
 // Items per lane in flight at once (independent probe chains).
 constexpr int kIlp = 4;
 
-constexpr uint64_t kDedupClaimFirstMax = 1ull << 20;  // items
-
 __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     pdl_prologue();
+    if (!a.sampled && a.state->inserted) return;  // extract_level inserted this level's hashes
     const uint64_t n = *a.d_n;
     const uint64_t S = table_size_for(n);
     const uint32_t lane = threadIdx.x & 31;
@@ -334,7 +308,23 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     __shared__ uint32_t red[kBucketThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nb = a.state->nbuckets;
-    if (!a.sampled && blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = unique_count(a);
+    if (!a.sampled && blockIdx.x == 0) {
+        // Top-bit form: the distinct keys are the bucket entries (the insert
+        // appended every first inserter to its bucket).
+        __shared__ uint32_t tot[kBucketThreads / 32];
+        uint32_t part = 0;
+        for (uint32_t b = tid; b < nb; b += kBucketThreads) part += min(a.bucket_count[b], kDedupTopBitCap);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+        if (lane == 0) tot[warp] = part;
+        __syncthreads();
+        if (tid == 0) {
+            uint64_t u = 0;
+            for (int w = 0; w < kBucketThreads / 32; ++w) u += tot[w];
+            if (u > a.uniq_cap) atomicOr(a.err, kErrFallback);
+            *a.d_out_n = u < a.uniq_cap ? u : a.uniq_cap;
+        }
+    }
     if (nb == 0) return;
     const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
     const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
@@ -464,7 +454,7 @@ int launch_dedup(const DedupArgs& a, cudaStream_t s) {
     const uint64_t want = (a.item_cap + 255) / 256;
     const int g = 8 * g_sms;  // full occupancy: 8 CTAs of 256 threads per SM
     const int gi = (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
-    launch_pdl(dedup_insert, dim3(gi), dim3(256), 0, s, a);
+    launch_pdl(dedup_insert, dim3(gi), dim3(256), 0, s, a);  // returns at once when extract_level inserted
     int launches = 1;
     if (a.sampled) {
         launch_pdl(dedup_split, dim3(1), dim3(kSplitThreads), kDedupMaxSample * 8, s, a);
