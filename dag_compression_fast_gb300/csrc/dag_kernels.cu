@@ -463,6 +463,7 @@ struct TailSmem {
     uint64_t key[kTailCap];       // node hashes, sorted with idx
     uint32_t idx[kTailCap];
     uint32_t map[2][kTailCap];    // node -> unique id, per level (ping-pong)
+    uint64_t uhash[kTailCap];     // the level's unique hashes: the next level's child hashes
     uint8_t mask[kTailCap];
     uint32_t scan[34];
     uint32_t flags;
@@ -470,6 +471,58 @@ struct TailSmem {
 
 __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb, uint32_t ib) {
     return ka < kb || (ka == kb && ia < ib);
+}
+
+// Bitonic compare-exchange stages of strides `from` down to 1 (all < 32) on
+// the 32-element chunks a warp holds in registers: element e = 32*chunk +
+// lane, partner e ^ stride, through shuffles. `size` is the merge size
+// (0: the first sizes 2..32, whose direction varies within a chunk).
+__device__ __forceinline__ void tail_warp_stages(TailSmem& S, uint32_t P, uint32_t size, uint32_t from) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t c = warp; c < P / 32; c += kTailThreads / 32) {
+        const uint32_t e = c * 32 + lane;
+        uint64_t k = S.key[e];
+        uint32_t i = S.idx[e];
+        const uint32_t s0 = size ? size : 2, s1 = size ? size : 32;
+        for (uint32_t sz = s0; sz <= s1; sz <<= 1) {
+            const bool up = (e & sz) == 0;
+            for (uint32_t st = size ? from : sz >> 1; st > 0; st >>= 1) {
+                const uint64_t ko = __shfl_xor_sync(0xFFFFFFFFu, k, st);
+                const uint32_t io = __shfl_xor_sync(0xFFFFFFFFu, i, st);
+                const bool lower = (lane & st) == 0;
+                const bool other_less = pair_less(ko, io, k, i);
+                if (lower == up ? other_less : !other_less) { k = ko; i = io; }
+            }
+        }
+        S.key[e] = k;
+        S.idx[e] = i;
+    }
+}
+
+// Bitonic sort of S.key/S.idx[0, P), P a power of two >= 32: strides of 32
+// and more through shared memory, smaller ones within warps.
+__device__ void tail_sort(TailSmem& S, uint32_t P) {
+    const uint32_t tid = threadIdx.x;
+    tail_warp_stages(S, P, 0, 0);  // sizes 2..32
+    __syncthreads();
+    for (uint32_t size = 64; size <= P; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride >= 32; stride >>= 1) {
+            for (uint32_t t = tid; t < P / 2; t += kTailThreads) {
+                const uint32_t lo = 2 * t - (t & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t ka = S.key[lo], kb = S.key[hi];
+                const uint32_t ia = S.idx[lo], ib = S.idx[hi];
+                if (pair_less(kb, ib, ka, ia) == up) {
+                    S.key[lo] = kb; S.key[hi] = ka;
+                    S.idx[lo] = ib; S.idx[hi] = ia;
+                }
+            }
+            __syncthreads();
+        }
+        tail_warp_stages(S, P, size, 16);
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
@@ -535,26 +588,11 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
         const uint32_t n = (uint32_t)(nn < cap ? nn : cap);
         // Bitonic sort of (hash, node) pairs, padded to a power of two with
         // (max, max) which sorts after every real pair.
-        uint32_t P = 1;
+        uint32_t P = 32;
         while (P < n) P <<= 1;
         for (uint32_t i = n + tid; i < P; i += kTailThreads) { S.key[i] = ~0ull; S.idx[i] = 0xFFFFFFFFu; }
         __syncthreads();
-        for (uint32_t size = 2; size <= P; size <<= 1) {
-            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                for (uint32_t t = tid; t < P / 2; t += kTailThreads) {
-                    const uint32_t lo = 2 * t - (t & (stride - 1));
-                    const uint32_t hi = lo + stride;
-                    const bool up = (lo & size) == 0;
-                    const uint64_t ka = S.key[lo], kb = S.key[hi];
-                    const uint32_t ia = S.idx[lo], ib = S.idx[hi];
-                    if (pair_less(kb, ib, ka, ia) == up) {
-                        S.key[lo] = kb; S.key[hi] = ka;
-                        S.idx[lo] = ib; S.idx[hi] = ia;
-                    }
-                }
-                __syncthreads();
-            }
-        }
+        tail_sort(S, P);
         // Unique with the full compare; node -> unique id into node_map.
         uint64_t uid_base = 0;
         for (uint32_t c0 = 0; c0 < n; c0 += kTailThreads) {
@@ -581,6 +619,7 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
                 node_map[x] = (uint32_t)uid;
                 if (head && uid < out.capacity) {
                     out.hashes[uid] = S.key[i];
+                    S.uhash[uid] = S.key[i];
                     out.masks[uid] = S.mask[x];
                     const uint4* src = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)x * 8);
                     uint4* dst = reinterpret_cast<uint4*>(out.children + uid * 8);
@@ -598,7 +637,7 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
         // The next level's children are this level's nodes.
         cc = node_code;
         cm = node_map;
-        ch = out.hashes;
+        ch = S.uhash;
         nc = n;
         ping ^= 1;
         __syncthreads();
