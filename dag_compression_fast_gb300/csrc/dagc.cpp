@@ -43,6 +43,7 @@ enum : int {
     kCntNodes = 3,                 // + level
     kCntUnique = 3 + kMaxDepth,    // + level
     kCntSlots = 3 + 2 * kMaxDepth + 1,
+    kCntOverflow = 63,             // fragments the grouping spilled past their partition's slab
 };
 
 struct CallHeader {
@@ -52,12 +53,12 @@ struct CallHeader {
     uint32_t tile_counters[kMaxTileCounters];
     uint32_t hist[kMaxSorts][kMaxPasses * 256];
     DedupState dedup[kMaxDepth + 1];  // leaves + one per level
-    uint32_t sketch[kGroupSketchRegs];  // distinct-brick sketch of the fragment grouping
-    uint64_t ghist[kGroupMaxParts];     // its fragment counts per fine partition
+    uint32_t sketch[kGroupSketchRegs];  // distinct-brick sketch of the fragment grouping's probe
+    uint32_t gover[kGroupMaxParts];     // its partitions that spilled past their slabs
     uint64_t gcursor[kGroupMaxParts];   // its partition starts, then ends
     uint32_t path[4];                   // [0] 1: fragments grouped by hash, 0: sorted; [1], [2] its shape
 };
-static_assert(kCntSlots <= 64, "count slots");
+static_assert(kCntSlots <= kCntOverflow, "count slots");
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -607,12 +608,17 @@ struct CreateLayout {
     size_t zero_bytes = 0, total = 0;
     size_t o_hdr, o_sv, o_ss0, o_ss1, o_A, o_B, o_P, o_LM, o_SK, o_SKa, o_V, o_Va, o_M0, o_M1;
     size_t o_NC0, o_NC1, o_NM, o_NCH, o_NH, o_PL, o_lead_or, o_lead_run, o_seg_off, o_seg_code;
+    // Fragment grouping (when `grouping`): the partition slabs.
+    int group_parts_log = 0;
+    uint64_t group_slab_cap = 0;
+    size_t o_slab = 0, o_over = 0;
     std::vector<size_t> o_ph, o_pc, o_pm;
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
     size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bslot = 0, o_brep = 0;
-    CreateLayout(uint64_t n, int depth, uint32_t k_batch, bool use_dedup, uint64_t unique_limit = kDedupMaxUnique) {
+    CreateLayout(uint64_t n, int depth, uint32_t k_batch, bool use_dedup, uint64_t unique_limit = kDedupMaxUnique,
+                 bool grouping = false) {
         const int nl = depth - 2;
         cap.resize(nl);
         for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
@@ -627,6 +633,11 @@ struct CreateLayout {
         o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
         o_A = L.take<uint64_t>(n);
         o_B = L.take<uint64_t>(n);
+        if (grouping) {
+            group_shape(n, &group_parts_log, &group_slab_cap);
+            o_slab = L.take<uint64_t>((uint64_t)group_slab_cap << group_parts_log);
+            o_over = L.take<uint64_t>(n);
+        }
         o_P = L.take<uint64_t>(p0cap);
         o_LM = L.take<uint64_t>(p0cap);
         dedup = use_dedup;
@@ -703,7 +714,8 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     const int group_mode = ctx->group_mode;
     const int nl = depth - 2;
     const int bits = 3 * depth;
-    const CreateLayout Lo(n, depth, batch ? batch->k : 0u, use_dedup, ctx->dedup_unique_limit);
+    const CreateLayout Lo(n, depth, batch ? batch->k : 0u, use_dedup, ctx->dedup_unique_limit,
+                          group_mode != 0 && use_dedup);
     const std::vector<uint64_t>& cap = Lo.cap;
     const uint64_t capmax = Lo.capmax, p0cap = Lo.p0cap, sv_total = Lo.sv_total;
     const size_t zero_bytes = Lo.zero_bytes;
@@ -761,10 +773,15 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.narrow = sort_hi <= 37 ? 1 : 0;
             g.chunks = group_chunks(n);
             g.sketch = cs.h->sketch;
-            g.hist = cs.h->ghist;
+            g.parts_log = Lo.group_parts_log;
+            g.slab_cap = Lo.group_slab_cap;
             g.cursor = cs.h->gcursor;
             g.path = cs.h->path;
-            g.parts = P64(Lo.o_B);
+            g.parts = P64(Lo.o_slab);
+            g.overflow = P64(Lo.o_over);
+            g.overflow_cap = n;
+            g.overflow_count = cs.count(kCntOverflow);
+            g.part_over = cs.h->gover;
             g.bricks = P64(Lo.o_A);
             g.idx = P32(Lo.o_M0);
             g.masks = static_cast<uint64_t*>(ctx->gtable);
@@ -777,7 +794,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.err = err;
             {
                 StageTimer t1(ctx, DAGC_STAGE_GROUP_SKETCH, s);
-                launch_group_sketch(g, s);
+                launch_group_probe(g, s);
                 launch_group_plan(g, s);
                 ctx->launches += 2;
                 t1.stop();
@@ -1034,10 +1051,10 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // Algorithmic bytes: the minimum each stage must read and write.
         const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
-        // Grouping: the sketch and the aggregation read 8 bytes per fragment,
-        // the scatter reads and writes 8; the brick sort and the gather move
-        // ~60 bytes per brick.
-        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SKETCH, 8 * n);
+        // Grouping: the probe reads a sixteenth of the fragments, the
+        // aggregation 8 bytes per fragment, the scatter reads and writes 8;
+        // the brick sort and the gather move ~60 bytes per brick.
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SKETCH, n / 2);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, 16 * n);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, 8 * n + 20 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP, 60 * p0);
@@ -1620,7 +1637,7 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
 
 uint64_t dagc_create_footprint(uint64_t n, int depth) {
     if (depth < 2 || depth > kMaxDepth || n == 0) return 0;
-    const CreateLayout L(n, depth, 0, true);
+    const CreateLayout L(n, depth, 0, true, kDedupMaxUnique, true);
     return L.total + L.table_slots * 16 + kGroupScratchBytes;
 }
 

@@ -123,9 +123,7 @@ constexpr int kGroupPartLog = 11;                        // fine partitions coun
 constexpr int kGroupMaxParts = 1 << kGroupPartLog;
 constexpr int kGroupPartSlotsLog = 12;                   // shared-memory table of one partition
 constexpr int kGroupPartSlots = 1 << kGroupPartSlotsLog;
-constexpr double kGroupBricksPerPart = 384.0;            // partition count target: estimate / this
-constexpr double kGroupMaxBricksPerPart = 0.45 * kGroupPartSlots;  // beyond this, the sort path
-constexpr uint64_t kGroupMaxPartFrags = 1ull << 18;      // one CTA reads one partition
+constexpr double kGroupMaxBricksPerPart = 0.45 * kGroupPartSlots;  // planned table load
 constexpr uint64_t kGroupMaxBricks = (uint64_t)kGroupMaxParts * kGroupPartSlots;
 constexpr int kGroupMaxChunks = 512;                     // CTAs of the sketch and scatter passes
 constexpr uint64_t kGroupScratchBytes = kGroupMaxBricks * 8;  // the brick masks
@@ -137,11 +135,15 @@ struct GroupArgs {
     int mode;                  // 1: choose by the sketch, 2: always group (tests)
     int narrow;                // every key below 2^37 (bricks below 2^31): 32-bit hashes and table keys
     int chunks;                // CTAs of the scatter: chunk c = [c*L, (c+1)*L), L = ceil(n / chunks)
-    uint32_t* sketch;          // kGroupSketchRegs words, zero
-    uint64_t* hist;            // kGroupMaxParts fragment counts per fine partition, zero
-    uint64_t* cursor;          // kGroupMaxParts: partition starts (plan), then ends (scatter)
+    uint32_t* sketch;          // kGroupSketchRegs words, zero: the probe's distinct-brick sketch
+    int parts_log;             // 2^parts_log partitions (group_shape)
+    uint64_t slab_cap;         // fragments each partition's slab of `parts` holds (group_shape)
+    uint64_t* cursor;          // kGroupMaxParts: partition p's next free position in its slab
     uint32_t* path;            // [0] 1 grouping, 0 sort path; [1] log2 partitions; [2] log2 table slots
-    uint64_t* parts;           // n: fragment keys by partition
+    uint64_t* parts;           // partition slabs: 2^parts_log * slab_cap fragment keys
+    uint64_t* overflow; uint64_t overflow_cap;  // fragments past their slab's end, any partition
+    uint64_t* overflow_count;  // zero on entry
+    uint32_t* part_over;       // kGroupMaxParts flags, zero on entry: the partition spilled
     uint64_t* bricks; uint32_t* idx; uint64_t* masks; uint64_t cap;  // brick list (unsorted), masks[idx]
     uint64_t* d_count;         // bricks found
     const uint64_t* sorted_bricks; const uint32_t* sorted_idx;      // after the brick sort
@@ -150,7 +152,9 @@ struct GroupArgs {
 };
 void group_configure(int sms);
 int group_chunks(uint64_t n);                                      // `chunks` for n fragments
-void launch_group_sketch(const GroupArgs& a, cudaStream_t s);
+// Partition count and slab size for n fragments (host side, before the call).
+void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap);
+void launch_group_probe(const GroupArgs& a, cudaStream_t s);
 void launch_group_plan(const GroupArgs& a, cudaStream_t s);      // picks the path
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s);
 void launch_group_aggregate(const GroupArgs& a, cudaStream_t s);

@@ -101,42 +101,42 @@ constexpr int kSketchLog = 12;
 constexpr int kSketchRegs = 1 << kSketchLog;
 static_assert(kSketchRegs == kGroupSketchRegs, "sketch size");
 constexpr int kFrontThreads = 512;
-constexpr int kSketchIlp = 8;
+// The probe samples one 64-byte line (8 fragments) in kProbeStride, or every
+// fragment of inputs up to kProbeAllMax.
+constexpr uint32_t kProbeStride = 16;
+constexpr uint64_t kProbeAllMax = 1ull << 20;
 
-template <bool kNarrow>
-__global__ void __launch_bounds__(kFrontThreads) group_sketch(GroupArgs a) {
+__device__ __forceinline__ void sketch_add(uint32_t* reg, uint64_t brick) {
+    const uint64_t h = brick_hash(brick);
+    const uint32_t rank = (uint32_t)__clzll((h << kSketchLog) | (1ull << (kSketchLog - 1))) + 1;
+    atomicMax(&reg[h >> (64 - kSketchLog)], rank);
+}
+
+__global__ void __launch_bounds__(kFrontThreads) group_probe(GroupArgs a) {
     pdl_prologue();
     __shared__ uint32_t reg[kSketchRegs];
-    __shared__ uint32_t hist[kGroupMaxParts];
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) reg[i] = 0;
-    for (int i = threadIdx.x; i < kGroupMaxParts; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    bool bad = false;
+    bool unused = false;  // the range check is the scatter's
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < a.n; i0 += kSketchIlp * stride) {
-        uint64_t c[kSketchIlp];
+    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.n <= kProbeAllMax) {
+        for (uint64_t i = t0; i < a.n; i += stride) sketch_add(reg, key_of(a, i, __ldcs(a.frags + i), &unused) >> 6);
+    } else {
+        // Line u of the sample: fragments [8 * (u * kProbeStride + kProbeStride / 2), + 8).
+        const uint64_t lines = a.n / 8 / kProbeStride;
+        for (uint64_t u = t0; u < lines; u += stride) {
+            const uint64_t i0 = 8 * (u * kProbeStride + kProbeStride / 2);
+            uint64_t c[8];
 #pragma unroll
-        for (int u = 0; u < kSketchIlp; ++u) {
-            const uint64_t i = i0 + u * stride;
-            c[u] = i < a.n ? __ldcs(a.frags + i) : 0;
-        }
+            for (int k = 0; k < 8; ++k) c[k] = __ldcs(a.frags + i0 + k);
 #pragma unroll
-        for (int u = 0; u < kSketchIlp; ++u) {
-            const uint64_t i = i0 + u * stride;
-            if (i >= a.n) continue;
-            const uint64_t brick = key_of(a, i, c[u], &bad) >> 6;
-            const uint64_t h = brick_hash(brick);
-            const uint32_t rank = (uint32_t)__clzll((h << kSketchLog) | (1ull << (kSketchLog - 1))) + 1;
-            atomicMax(&reg[h >> (64 - kSketchLog)], rank);
-            atomicAdd(&hist[fine_part<kNarrow>(brick)], 1u);
+            for (int k = 0; k < 8; ++k) sketch_add(reg, key_of(a, i0 + k, c[k], &unused) >> 6);
         }
     }
-    if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31) == 0) atomicOr(a.err, kErrBadInput);
     __syncthreads();
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x)
         if (reg[i]) atomicMax(a.sketch + i, reg[i]);
-    for (int i = threadIdx.x; i < kGroupMaxParts; i += blockDim.x)
-        if (hist[i]) atomicAdd((unsigned long long*)(a.hist + i), (unsigned long long)hist[i]);
 }
 
 // Distinct-brick estimate from the sketch (HyperLogLog with the linear
@@ -171,62 +171,37 @@ __device__ double sketch_estimate(const uint32_t* sketch, unsigned long long* re
     return *out;
 }
 
-constexpr int kPlanThreads = kGroupMaxParts / 2;  // two fine partitions per thread
+constexpr int kPlanThreads = 1024;
+
+// Fragments per distinct brick in the probe's sample when every brick of the
+// input holds rho fragments and the sample keeps each fragment with
+// probability q: q * rho / (1 - (1 - q)^rho) (rho itself when q = 1).
+__device__ double sampled_ratio(double q, double rho) { return q * rho / (1.0 - pow(1.0 - q, rho)); }
 
 __global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
     pdl_prologue();
     __shared__ unsigned long long red[2 * (kPlanThreads / 32)];
     __shared__ double est_s;
-    __shared__ int shape[3];  // log2 partitions, log2 slots, redundancy and size test passed
-    __shared__ uint64_t scan[34];
-    __shared__ uint64_t start[kGroupMaxParts];
-    __shared__ unsigned long long max_part;
     const double est = sketch_estimate(a.sketch, red, &est_s);
     if (threadIdx.x == 0) {
-        // The shape, from the estimate (one thread: double precision is slow).
-        int lp = 0;
-        while (lp < kGroupPartLog && (double)(1u << lp) * kGroupBricksPerPart < est) ++lp;
-        const double per_part = est / (double)(1u << lp);
-        // Slots: ~8 per expected brick (up to the shared-memory table's size),
-        // so that most probes end at their first slot and warps stay converged.
-        int lt = 9;  // at least one slot per thread of the aggregation
-        while (lt < kGroupPartSlotsLog && (double)(1u << lt) < 8.0 * per_part + 32.0) ++lt;
-        shape[0] = lp;
-        shape[1] = lt;
-        shape[2] = est * kGroupMinRedundancy <= (double)a.n && per_part <= kGroupMaxBricksPerPart;
-        max_part = 0;
-    }
-    __syncthreads();
-    const int lp = shape[0], lt = shape[1];
-    const int parts = 1 << lp, shift = kGroupPartLog - lp;
-    const uint32_t fine_mask = (1u << shift) - 1;
-    // Partition p covers fine partitions [p << shift, (p + 1) << shift).
-    const uint32_t f0 = 2 * threadIdx.x;
-    const uint64_t v0 = a.hist[f0], v1 = a.hist[f0 + 1];
-    uint64_t total;
-    const uint64_t ex = block_exclusive_sum<uint64_t>(v0 + v1, scan, &total);
-    if ((f0 & fine_mask) == 0) start[f0 >> shift] = ex;
-    if (((f0 + 1) & fine_mask) == 0) start[(f0 + 1) >> shift] = ex + v0;
-    __syncthreads();
-    unsigned long long biggest = 0;
-    for (int p = threadIdx.x; p < parts; p += blockDim.x) {
-        const uint64_t end = p + 1 < parts ? start[p + 1] : total;
-        biggest = end - start[p] > biggest ? end - start[p] : biggest;
-        a.cursor[p] = start[p];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long other = __shfl_xor_sync(0xFFFFFFFFu, biggest, o);
-        biggest = other > biggest ? other : biggest;
-    }
-    if ((threadIdx.x & 31) == 0) atomicMax(&max_part, biggest);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const bool group = a.mode == 2 || (a.mode == 1 && shape[2] && max_part <= kGroupMaxPartFrags);
+        // The path: grouping when the sample says the fragments hold about
+        // kGroupMinRedundancy or more per brick (the sampling model inverted).
+        // It also covers capacity: the partitions' tables hold
+        // kGroupMaxBricksPerPart bricks each, so the fragments must hold at
+        // least n / (that * partitions) per brick. The model's ratio grows
+        // with the redundancy, so the larger of the two bounds decides.
+        const bool all = a.n <= kProbeAllMax;
+        const double q = all ? 1.0 : 1.0 / kProbeStride;
+        const double sampled = all ? (double)a.n : (double)(a.n / 8 / kProbeStride) * 8.0;
+        const double need = fmax(kGroupMinRedundancy, (double)a.n / (kGroupMaxBricksPerPart * (double)(1u << a.parts_log)));
+        const bool redundant = est > 0.0 && sampled / est >= sampled_ratio(q, need);
+        const bool group = a.mode == 2 || (a.mode == 1 && redundant);
         a.path[0] = group ? 1u : 0u;
-        a.path[1] = (uint32_t)lp;
-        a.path[2] = (uint32_t)lt;
+        a.path[1] = (uint32_t)a.parts_log;
+        a.path[2] = (uint32_t)kGroupPartSlotsLog;
     }
+    // Partition p fills the slab [p * slab_cap, (p + 1) * slab_cap).
+    for (uint32_t p = threadIdx.x; p < (1u << a.parts_log); p += blockDim.x) a.cursor[p] = (uint64_t)p * a.slab_cap;
 }
 
 // 8-byte asynchronous copy global -> shared (cp.async), and its completion.
@@ -246,7 +221,7 @@ struct ScatterSmem {
     uint64_t in[kScatterTile];       // the next tile's keys, copied in while this tile is processed
     uint64_t stage[kScatterTile];    // this tile's keys, by partition
     uint32_t cnt[kGroupMaxParts];    // the tile's count per partition, then its offset in the tile
-    int32_t delta[kGroupMaxParts];   // output position - tile position, per partition
+    int64_t delta[kGroupMaxParts];   // output position - tile position, per partition
     uint32_t scan[34];
 };
 
@@ -266,7 +241,7 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
     const int parts = 1 << lp;
     uint64_t lo, hi;
     chunk_range(a, &lo, &hi);
-    bool bad = false;  // reported by the sketch pass
+    bool bad = false, over = false;  // codes out of range; the overflow area full
     const int per = (parts + kScatterThreads - 1) / kScatterThreads;
     for (int p = threadIdx.x; p < parts; p += kScatterThreads) sm.cnt[p] = 0;
     if (lo < hi) scatter_prefetch(sm, a.frags, lo, hi);
@@ -297,19 +272,20 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
         // The tile's run of each partition goes right after the runs that
         // tiles reserved before it, so that the partially written sectors of
         // a partition's frontier are completed while they are in the L2.
-        uint32_t c[kScatterMaxPer], g[kScatterMaxPer];
+        uint32_t c[kScatterMaxPer];
+        unsigned long long g[kScatterMaxPer];
 #pragma unroll
         for (int j = 0; j < kScatterMaxPer; ++j) {
             const int p = p0 + j;
             c[j] = j < per && p < parts ? sm.cnt[p] : 0u;
-            g[j] = c[j] ? (uint32_t)atomicAdd((unsigned long long*)(a.cursor + p), (unsigned long long)c[j]) : 0u;
+            g[j] = c[j] ? atomicAdd((unsigned long long*)(a.cursor + p), (unsigned long long)c[j]) : 0ull;
         }
 #pragma unroll
         for (int j = 0; j < kScatterMaxPer; ++j) {
             const int p = p0 + j;
             if (j >= per || p >= parts) break;
             sm.cnt[p] = run;
-            sm.delta[p] = (int32_t)g[j] - (int32_t)run;
+            sm.delta[p] = (int64_t)g[j] - (int64_t)run;
             run += c[j];
         }
         __syncthreads();
@@ -323,27 +299,86 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
         // Write-out in tile order: runs of one partition are contiguous. The
         // partition is recomputed from the key (cheaper than storing it).
         const uint32_t m = (uint32_t)(hi - base < (uint64_t)kScatterTile ? hi - base : (uint64_t)kScatterTile);
+        const uint32_t lane = threadIdx.x & 31;
 #pragma unroll 4
-        for (uint32_t q = threadIdx.x; q < m; q += kScatterThreads) {
-            const uint64_t k = sm.stage[q];
-            a.parts[(int64_t)sm.delta[part_of<kNarrow>(k, lp)] + q] = k;
+        for (uint32_t q0 = 0; q0 < m; q0 += kScatterThreads) {  // uniform over the CTA: every lane votes
+            const uint32_t q = q0 + threadIdx.x;
+            uint64_t k = 0;
+            bool spill = false;
+            if (q < m) {
+                k = sm.stage[q];
+                const uint32_t pid = part_of<kNarrow>(k, lp);
+                const uint64_t pos = (uint64_t)((int64_t)sm.delta[pid] + q);
+                if (pos < (uint64_t)(pid + 1) * a.slab_cap) {
+                    a.parts[pos] = k;
+                } else {
+                    // The partition's slab is full (a brick with very many
+                    // fragments): to the shared overflow area.
+                    spill = true;
+                    a.part_over[pid] = 1u;
+                }
+            }
+            const uint32_t sm_mask = __ballot_sync(0xFFFFFFFFu, spill);
+            if (sm_mask) {
+                unsigned long long ob = 0;
+                if (lane == 0) ob = atomicAdd((unsigned long long*)a.overflow_count, (unsigned long long)__popc(sm_mask));
+                ob = __shfl_sync(0xFFFFFFFFu, ob, 0);
+                if (spill) {
+                    const uint64_t o = ob + __popc(sm_mask & lanemask_lt());
+                    if (o < a.overflow_cap) a.overflow[o] = k;
+                    else over = true;
+                }
+            }
         }
         for (int p = threadIdx.x; p < parts; p += kScatterThreads) sm.cnt[p] = 0;  // read last before the stage barrier
     }
+    if (bad) atomicOr(a.err, kErrBadInput);
+    if (over) atomicOr(a.err, kErrFallback);
 }
 
 constexpr int kAggThreads = 512;
 constexpr int kAggIlp = 4;
+// Longest probe chain before a partition's table counts as full: at the
+// planned load (< 0.45) chains stay far shorter.
+constexpr uint32_t kAggMaxProbe = 256;
 static_assert((1 << 9) >= kAggThreads, "at least one table slot per thread");
 
 template <bool kNarrow>
 struct AggSmem {
     using Key = typename std::conditional<kNarrow, uint32_t, unsigned long long>::type;
+    uint32_t full;                   // a probe chain ran out: the partition gives up
     uint64_t mask[kGroupPartSlots];  // OR of the fragments' bits
     Key key[kGroupPartSlots];        // brick + 1, 0 = empty
     uint32_t scan[34];
     uint64_t base;
 };
+
+// One fragment into the partition's table: find or claim its brick's slot
+// (linear probing), OR its bit into the mask. False when the table is full.
+template <bool kNarrow>
+__device__ __forceinline__ bool agg_insert(AggSmem<kNarrow>& sm, uint64_t key, uint32_t lt, uint32_t slots) {
+    using Key = typename AggSmem<kNarrow>::Key;
+    const uint64_t brick = key >> 6;
+    const Key tag = (Key)brick + 1;
+    uint32_t s = slot_of<kNarrow>(brick, lt);
+    Key cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
+    if (cur != tag) {
+        // Rare: the brick's first fragment here, or a collision.
+        for (uint32_t probe = 0;; ) {
+            if (cur == 0) {
+                cur = atomicCAS(&sm.key[s], (Key)0, tag);
+                if (cur == 0 || cur == tag) break;
+            }
+            if (++probe == kAggMaxProbe) return false;  // the table is (nearly) full: the sort path
+            s = (s + 1) & (slots - 1);
+            cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
+            if (cur == tag) break;
+        }
+    }
+    const uint32_t bit = (uint32_t)(key & 63);
+    atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s]) + (bit >> 5), 1u << (bit & 31));
+    return true;
+}
 
 template <bool kNarrow>
 __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
@@ -356,11 +391,13 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
     const uint32_t parts = 1u << a.path[1], lt = a.path[2], slots = 1u << lt;
     bool full = false;
     for (uint32_t p = blockIdx.x; p < parts; p += gridDim.x) {
-        const uint64_t lo = p ? a.cursor[p - 1] : 0, hi = a.cursor[p];
+        const uint64_t lo = (uint64_t)p * a.slab_cap;
+        const uint64_t hi = a.cursor[p] < lo + a.slab_cap ? a.cursor[p] : lo + a.slab_cap;
         for (uint32_t s = threadIdx.x; s < slots; s += kAggThreads) {
             sm.key[s] = 0;
             sm.mask[s] = 0;
         }
+        if (threadIdx.x == 0) sm.full = 0;
         __syncthreads();
         for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kAggIlp * kAggThreads) {
             uint64_t k[kAggIlp];
@@ -370,30 +407,22 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
                 k[u] = i < hi ? __ldcs(a.parts + i) : 0;
             }
 #pragma unroll
-            for (int u = 0; u < kAggIlp; ++u) {
-                if (i0 + (uint64_t)u * kAggThreads >= hi) continue;
-                const uint64_t brick = k[u] >> 6;
-                const Key tag = (Key)brick + 1;
-                uint32_t s = slot_of<kNarrow>(brick, lt);
-                Key cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
-                if (cur != tag) {
-                    // Rare: the brick's first fragment here, or a collision.
-                    for (uint32_t probe = 0;; ) {
-                        if (cur == 0) {
-                            cur = atomicCAS(&sm.key[s], (Key)0, tag);
-                            if (cur == 0 || cur == tag) break;
-                        }
-                        if (++probe == slots) { full = true; break; }  // more bricks than slots: sort path
-                        s = (s + 1) & (slots - 1);
-                        cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
-                        if (cur == tag) break;
-                    }
-                }
-                const uint32_t bit = (uint32_t)(k[u] & 63);
-                atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s]) + (bit >> 5), 1u << (bit & 31));
+            for (int u = 0; u < kAggIlp; ++u)
+                if (i0 + (uint64_t)u * kAggThreads < hi && !agg_insert<kNarrow>(sm, k[u], lt, slots)) sm.full = 1;
+            if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;  // fail fast: the call reruns
+        }
+        if (a.part_over[p]) {
+            // The partition's slab was full: the rest of its fragments are in
+            // the shared overflow area, among other partitions'.
+            const uint64_t no = *a.overflow_count;
+            for (uint64_t i = threadIdx.x; i < no; i += kAggThreads) {
+                const uint64_t k = a.overflow[i];
+                if (part_of<kNarrow>(k, (int)a.path[1]) == p && !agg_insert<kNarrow>(sm, k, lt, slots)) sm.full = 1;
+                if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;
             }
         }
         __syncthreads();
+        full |= sm.full != 0;
         const uint32_t per = slots / kAggThreads, s0 = threadIdx.x * per;
         uint32_t cnt = 0;
         for (uint32_t j = 0; j < per; ++j) cnt += sm.key[s0 + j] != 0;
@@ -474,11 +503,22 @@ int group_chunks(uint64_t n) {
     return (int)(want < 1 ? 1 : (want < most ? want : most));
 }
 
-void launch_group_sketch(const GroupArgs& a, cudaStream_t s) {
-    const uint64_t want = (a.n + kFrontThreads * kSketchIlp - 1) / (kFrontThreads * kSketchIlp);
+void launch_group_probe(const GroupArgs& a, cudaStream_t s) {
+    const uint64_t units = a.n <= kProbeAllMax ? a.n : a.n / 8 / kProbeStride;
+    const uint64_t want = (units + kFrontThreads - 1) / kFrontThreads;
     const int g = (int)(want < (uint64_t)(2 * g_group_sms) ? (want > 0 ? want : 1) : 2 * g_group_sms);
-    if (a.narrow) launch_pdl(group_sketch<true>, dim3(g), dim3(kFrontThreads), 0, s, a);
-    else launch_pdl(group_sketch<false>, dim3(g), dim3(kFrontThreads), 0, s, a);
+    launch_pdl(group_probe, dim3(g), dim3(kFrontThreads), 0, s, a);
+}
+
+void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap) {
+    // Partitions of ~4096 fragments (up to kGroupMaxParts): a partition of an
+    // input with kGroupMinRedundancy fragments per brick holds far fewer
+    // bricks than its table's kGroupPartSlots. Slabs: 1.25 x the mean + 1024.
+    int lp = 0;
+    while (lp < kGroupPartLog && (n >> lp) > 4096) ++lp;
+    const uint64_t mean = (n + (1ull << lp) - 1) >> lp;
+    *parts_log = lp;
+    *slab_cap = mean + mean / 4 + 1024;
 }
 void launch_group_plan(const GroupArgs& a, cudaStream_t s) { launch_pdl(group_plan, dim3(1), dim3(kPlanThreads), 0, s, a); }
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s) {

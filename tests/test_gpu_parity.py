@@ -104,6 +104,38 @@ def test_grouping_forms_bit_exact(mode, case):
         assert np.array_equal(decode_final(w, depth), np.unique(codes))
 
 
+def test_forced_grouping_with_overfull_tables_reruns():
+    """Grouping forced on an input whose partitions hold more distinct bricks
+    than their tables (10M random bricks over 2048 tables of 4096 slots): the
+    full tables are detected, the call reruns on the sort path and the DAG is
+    exact."""
+    rng = np.random.default_rng(21)
+    depth = 12
+    codes = rng.integers(0, 1 << (3 * depth), 10_000_000, dtype=np.uint64)
+    ref = O.create_dag(codes, depth, threads=8)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, 2)
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() >= 1
+
+
+def test_grouping_spills_a_brick_larger_than_its_slab():
+    """One brick holds most fragments (duplicates of a few codes): its
+    partition's slab overflows into the shared overflow area, and the DAG is
+    exact."""
+    rng = np.random.default_rng(22)
+    depth = 9
+    bulk = rng.integers(0, 1 << (3 * depth), 300_000, dtype=np.uint64)
+    heavy = np.repeat(np.array([12345 << 6 | k for k in range(0, 64, 3)], np.uint64), 40_000)
+    codes = np.concatenate([bulk, heavy])
+    rng.shuffle(codes)
+    ref = O.create_dag(codes, depth)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, 2)
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 0
+
+
 def test_grouping_rejects_out_of_range_codes():
     with D.Context(0) as c:
         c.set_option(D.OPT_GROUP, 2)
