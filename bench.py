@@ -323,8 +323,8 @@ def main():
     peak, peak_kind = measured_peaks()
     pass_traffic = profile_figure("onesweep_pass_keys_20M_27bit.md", "dram_bytes_per_key_per_pass", n)
     group_kernels = {
-        "group_sketch": ("group_sketch + group_plan (sketch and partition counts, one read)",
-                         "group_sketch_terrain_d11.md"),
+        "group_sketch": ("group_probe + group_plan (sampled sketch, path choice)",
+                         "group_probe_terrain_d11.md"),
         "group_scatter": ("group_scatter (fragments by partition: one read, one write)",
                           "group_scatter_terrain_d11.md"),
         "group_aggregate": ("group_aggregate (per-partition tables in shared memory: one read)",

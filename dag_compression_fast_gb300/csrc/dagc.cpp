@@ -611,6 +611,7 @@ struct CreateLayout {
     // Fragment grouping (when `grouping`): the partition slabs.
     int group_parts_log = 0;
     uint64_t group_slab_cap = 0;
+    float group_probe_max = 0.0f;
     size_t o_slab = 0, o_over = 0;
     std::vector<size_t> o_ph, o_pc, o_pm;
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
@@ -634,7 +635,7 @@ struct CreateLayout {
         o_A = L.take<uint64_t>(n);
         o_B = L.take<uint64_t>(n);
         if (grouping) {
-            group_shape(n, &group_parts_log, &group_slab_cap);
+            group_shape(n, &group_parts_log, &group_slab_cap, &group_probe_max);
             o_slab = L.take<uint64_t>((uint64_t)group_slab_cap << group_parts_log);
             o_over = L.take<uint64_t>(n);
         }
@@ -775,6 +776,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.sketch = cs.h->sketch;
             g.parts_log = Lo.group_parts_log;
             g.slab_cap = Lo.group_slab_cap;
+            g.probe_max_distinct = Lo.group_probe_max;
             g.cursor = cs.h->gcursor;
             g.path = cs.h->path;
             g.parts = P64(Lo.o_slab);

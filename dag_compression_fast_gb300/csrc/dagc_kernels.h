@@ -138,6 +138,7 @@ struct GroupArgs {
     uint32_t* sketch;          // kGroupSketchRegs words, zero: the probe's distinct-brick sketch
     int parts_log;             // 2^parts_log partitions (group_shape)
     uint64_t slab_cap;         // fragments each partition's slab of `parts` holds (group_shape)
+    float probe_max_distinct;  // grouping when the probe's sample shows at most this many distinct bricks
     uint64_t* cursor;          // kGroupMaxParts: partition p's next free position in its slab
     uint32_t* path;            // [0] 1 grouping, 0 sort path; [1] log2 partitions; [2] log2 table slots
     uint64_t* parts;           // partition slabs: 2^parts_log * slab_cap fragment keys
@@ -153,7 +154,7 @@ struct GroupArgs {
 void group_configure(int sms);
 int group_chunks(uint64_t n);                                      // `chunks` for n fragments
 // Partition count and slab size for n fragments (host side, before the call).
-void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap);
+void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap, float* probe_max_distinct);
 void launch_group_probe(const GroupArgs& a, cudaStream_t s);
 void launch_group_plan(const GroupArgs& a, cudaStream_t s);      // picks the path
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s);

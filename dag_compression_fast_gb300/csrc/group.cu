@@ -35,6 +35,8 @@
 #include "dagc_kernels.h"
 #include "dagc_launch.h"
 
+#include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 namespace dagc {
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(kFrontThreads) group_probe(GroupArgs a) {
 // register sum is exact in fixed point (2^(52 - rank), rank >= 1, at most
 // 4096 * 2^51 < 2^64); one thread finishes it in double precision, which is
 // slow on this GPU.
-__device__ double sketch_estimate(const uint32_t* sketch, unsigned long long* red, double* out) {
+__device__ float sketch_estimate(const uint32_t* sketch, unsigned long long* red, float* out) {
     unsigned long long sum = 0, zeros = 0;
     for (int i = threadIdx.x; i < kSketchRegs; i += blockDim.x) {
         const uint32_t r = sketch[i];
@@ -163,9 +165,11 @@ __device__ double sketch_estimate(const uint32_t* sketch, unsigned long long* re
         sum = 0;
         zeros = 0;
         for (int w = 0; w < nw; ++w) { sum += red[2 * w]; zeros += red[2 * w + 1]; }
-        const double m = (double)kSketchRegs;
-        const double e = 0.7213 / (1.0 + 1.079 / m) * m * m / ((double)sum * 0x1p-52);
-        *out = e <= 2.5 * m && zeros > 0 ? m * log(m / (double)zeros) : e;
+        // Single precision: the estimate only steers a choice, and double
+        // precision is slow on this part.
+        const float m = (float)kSketchRegs;
+        const float e = 0.7213f / (1.0f + 1.079f / m) * m * m / ((float)sum * 0x1p-52f);
+        *out = e <= 2.5f * m && zeros > 0 ? m * logf(m / (float)zeros) : e;
     }
     __syncthreads();
     return *out;
@@ -176,25 +180,15 @@ constexpr int kPlanThreads = 1024;
 // Fragments per distinct brick in the probe's sample when every brick of the
 // input holds rho fragments and the sample keeps each fragment with
 // probability q: q * rho / (1 - (1 - q)^rho) (rho itself when q = 1).
-__device__ double sampled_ratio(double q, double rho) { return q * rho / (1.0 - pow(1.0 - q, rho)); }
-
 __global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
     pdl_prologue();
     __shared__ unsigned long long red[2 * (kPlanThreads / 32)];
-    __shared__ double est_s;
-    const double est = sketch_estimate(a.sketch, red, &est_s);
+    __shared__ float est_s;
+    const float est = sketch_estimate(a.sketch, red, &est_s);
     if (threadIdx.x == 0) {
-        // The path: grouping when the sample says the fragments hold about
-        // kGroupMinRedundancy or more per brick (the sampling model inverted).
-        // It also covers capacity: the partitions' tables hold
-        // kGroupMaxBricksPerPart bricks each, so the fragments must hold at
-        // least n / (that * partitions) per brick. The model's ratio grows
-        // with the redundancy, so the larger of the two bounds decides.
-        const bool all = a.n <= kProbeAllMax;
-        const double q = all ? 1.0 : 1.0 / kProbeStride;
-        const double sampled = all ? (double)a.n : (double)(a.n / 8 / kProbeStride) * 8.0;
-        const double need = fmax(kGroupMinRedundancy, (double)a.n / (kGroupMaxBricksPerPart * (double)(1u << a.parts_log)));
-        const bool redundant = est > 0.0 && sampled / est >= sampled_ratio(q, need);
+        // The path: grouping when the sample holds at most probe_max_distinct
+        // distinct bricks (group_shape derives it from the sampling model).
+        const bool redundant = est > 0.0f && est <= a.probe_max_distinct;
         const bool group = a.mode == 2 || (a.mode == 1 && redundant);
         a.path[0] = group ? 1u : 0u;
         a.path[1] = (uint32_t)a.parts_log;
@@ -510,7 +504,7 @@ void launch_group_probe(const GroupArgs& a, cudaStream_t s) {
     launch_pdl(group_probe, dim3(g), dim3(kFrontThreads), 0, s, a);
 }
 
-void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap) {
+void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap, float* probe_max_distinct) {
     // Partitions of ~4096 fragments (up to kGroupMaxParts): a partition of an
     // input with kGroupMinRedundancy fragments per brick holds far fewer
     // bricks than its table's kGroupPartSlots. Slabs: 1.25 x the mean + 1024.
@@ -519,6 +513,19 @@ void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap) {
     const uint64_t mean = (n + (1ull << lp) - 1) >> lp;
     *parts_log = lp;
     *slab_cap = mean + mean / 4 + 1024;
+    // The path's test. If every brick held rho fragments, a sample keeping
+    // each fragment with probability q would hold q * rho / (1 - (1 - q)^rho)
+    // fragments per distinct brick (rho when q = 1), a ratio that grows with
+    // rho. Grouping needs kGroupMinRedundancy fragments per brick, and the
+    // tables' capacity needs n / (kGroupMaxBricksPerPart * partitions): the
+    // larger bound sets the least ratio, hence the most distinct bricks the
+    // sample may show.
+    const bool all = n <= kProbeAllMax;
+    const double q = all ? 1.0 : 1.0 / kProbeStride;
+    const double sampled = all ? (double)n : (double)(n / 8 / kProbeStride) * 8.0;
+    const double rho = std::max(kGroupMinRedundancy, (double)n / (kGroupMaxBricksPerPart * (double)(1ull << lp)));
+    const double ratio = all ? rho : q * rho / (1.0 - std::pow(1.0 - q, rho));
+    *probe_max_distinct = (float)(sampled / ratio);
 }
 void launch_group_plan(const GroupArgs& a, cudaStream_t s) { launch_pdl(group_plan, dim3(1), dim3(kPlanThreads), 0, s, a); }
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s) {
