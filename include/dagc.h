@@ -170,9 +170,11 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
 #define DAGC_OPT_DEDUP_UNIQUE_LIMIT 5
 /* How fragments are grouped into bricks (SortKeys + SelectUnique +
  * ReduceByKey): 1 (default) choose on the device per call, from a sketch of
- * the distinct bricks: a hash table when fragments hold >= 8 per brick on
- * average, else the radix sort; 0 always the radix sort; 2 always the hash
- * table. Results are identical. */
+ * the distinct bricks in a sample of the fragments: hash partitions and
+ * per-partition tables when the fragments hold >= 8 per brick (and the
+ * tables can hold the bricks), else the radix sort; 0 always the radix sort;
+ * 2 always the hash partitions (an input they cannot hold reruns on the radix
+ * sort). Results are identical. */
 #define DAGC_OPT_GROUP 6
 /* 1: launch every kernel of a call with programmatic dependent launch (the
  * next kernel is scheduled while the previous one runs and waits for it on the
@@ -199,7 +201,7 @@ int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
 #define DAGC_STAGE_FINAL 6          /* final word layout */
 #define DAGC_STAGE_MERGE 7          /* MergeDAGs */
 #define DAGC_STAGE_GROUP 8             /* fragment grouping by hash: brick sort, gather */
-#define DAGC_STAGE_GROUP_SKETCH 9      /* its sketch + partition counts (one read of the fragments), path choice */
+#define DAGC_STAGE_GROUP_SKETCH 9      /* its probe (a sampled sketch of the distinct bricks) and the path choice */
 #define DAGC_STAGE_GROUP_AGGREGATE 10  /* its per-partition tables (one read of the partitioned fragments) */
 #define DAGC_STAGE_GROUP_SCATTER 11    /* its partitioning (one read and one write of the fragments) */
 #define DAGC_NUM_STAGES 12
