@@ -609,8 +609,7 @@ struct CreateLayout {
     size_t o_hdr, o_sv, o_ss0, o_ss1, o_A, o_B, o_P, o_LM, o_SK, o_SKa, o_V, o_Va, o_M0, o_M1;
     size_t o_NC0, o_NC1, o_NM, o_NCH, o_NH, o_PL, o_lead_or, o_lead_run, o_seg_off, o_seg_code;
     // Fragment grouping (when `grouping`): the partition slabs.
-    int group_parts_log = 0;
-    uint64_t group_slab_cap = 0;
+    uint64_t group_slab_total = 0;
     float group_probe_max = 0.0f;
     size_t o_slab = 0, o_over = 0;
     std::vector<size_t> o_ph, o_pc, o_pm;
@@ -635,8 +634,8 @@ struct CreateLayout {
         o_A = L.take<uint64_t>(n);
         o_B = L.take<uint64_t>(n);
         if (grouping) {
-            group_shape(n, &group_parts_log, &group_slab_cap, &group_probe_max);
-            o_slab = L.take<uint64_t>((uint64_t)group_slab_cap << group_parts_log);
+            group_shape(n, &group_slab_total, &group_probe_max);
+            o_slab = L.take<uint64_t>(group_slab_total);
             o_over = L.take<uint64_t>(n);
         }
         o_P = L.take<uint64_t>(p0cap);
@@ -774,8 +773,6 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             g.narrow = sort_hi <= 37 ? 1 : 0;
             g.chunks = group_chunks(n);
             g.sketch = cs.h->sketch;
-            g.parts_log = Lo.group_parts_log;
-            g.slab_cap = Lo.group_slab_cap;
             g.probe_max_distinct = Lo.group_probe_max;
             g.cursor = cs.h->gcursor;
             g.path = cs.h->path;

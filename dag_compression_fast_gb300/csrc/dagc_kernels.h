@@ -123,7 +123,8 @@ constexpr int kGroupPartLog = 11;                        // fine partitions coun
 constexpr int kGroupMaxParts = 1 << kGroupPartLog;
 constexpr int kGroupPartSlotsLog = 12;                   // shared-memory table of one partition
 constexpr int kGroupPartSlots = 1 << kGroupPartSlotsLog;
-constexpr double kGroupMaxBricksPerPart = 0.45 * kGroupPartSlots;  // planned table load
+constexpr double kGroupMaxBricksPerPart = 0.45 * kGroupPartSlots;  // most bricks per table (load 0.45)
+constexpr float kGroupTargetBricksPerPart = 1536.0f;     // partitions chosen for ~this many (load ~0.3)
 constexpr uint64_t kGroupMaxBricks = (uint64_t)kGroupMaxParts * kGroupPartSlots;
 constexpr int kGroupMaxChunks = 512;                     // CTAs of the sketch and scatter passes
 constexpr uint64_t kGroupScratchBytes = kGroupMaxBricks * 8;  // the brick masks
@@ -136,12 +137,10 @@ struct GroupArgs {
     int narrow;                // every key below 2^37 (bricks below 2^31): 32-bit hashes and table keys
     int chunks;                // CTAs of the scatter: chunk c = [c*L, (c+1)*L), L = ceil(n / chunks)
     uint32_t* sketch;          // kGroupSketchRegs words, zero: the probe's distinct-brick sketch
-    int parts_log;             // 2^parts_log partitions (group_shape)
-    uint64_t slab_cap;         // fragments each partition's slab of `parts` holds (group_shape)
     float probe_max_distinct;  // grouping when the probe's sample shows at most this many distinct bricks
     uint64_t* cursor;          // kGroupMaxParts: partition p's next free position in its slab
-    uint32_t* path;            // [0] 1 grouping, 0 sort path; [1] log2 partitions; [2] log2 table slots
-    uint64_t* parts;           // partition slabs: 2^parts_log * slab_cap fragment keys
+    uint32_t* path;            // [0] 1 grouping, 0 sort path; [1] log2 partitions; [2] log2 table slots; [3] slab size
+    uint64_t* parts;           // partition slabs (group_shape's slab_total fragment keys)
     uint64_t* overflow; uint64_t overflow_cap;  // fragments past their slab's end, any partition
     uint64_t* overflow_count;  // zero on entry
     uint32_t* part_over;       // kGroupMaxParts flags, zero on entry: the partition spilled
@@ -153,8 +152,9 @@ struct GroupArgs {
 };
 void group_configure(int sms);
 int group_chunks(uint64_t n);                                      // `chunks` for n fragments
-// Partition count and slab size for n fragments (host side, before the call).
-void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap, float* probe_max_distinct);
+// Room for the partition slabs of n fragments, and the probe's limit (host
+// side, before the call).
+void group_shape(uint64_t n, uint64_t* slab_total, float* probe_max_distinct);
 void launch_group_probe(const GroupArgs& a, cudaStream_t s);
 void launch_group_plan(const GroupArgs& a, cudaStream_t s);      // picks the path
 void launch_group_scatter(const GroupArgs& a, cudaStream_t s);

@@ -69,6 +69,13 @@ template <bool kNarrow>
 __device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
     return lp ? fine_part<kNarrow>(key >> 6) >> (kGroupPartLog - lp) : 0u;
 }
+// Sub-range of a brick within its partition: the low bits of the same
+// product (the partition and the slot take the top ones).
+template <bool kNarrow>
+__device__ __forceinline__ uint32_t sub_of(uint64_t brick) {
+    if (kNarrow) return (uint32_t)brick * 0x9E3779B1u;
+    return (uint32_t)(brick * 0x9E3779B97F4A7C15ull);
+}
 template <bool kNarrow>
 __device__ __forceinline__ uint32_t slot_of(uint64_t brick, uint32_t lt) {
     if (kNarrow) return (((uint32_t)brick * 0x9E3779B1u) >> (32 - kGroupPartLog - lt)) & ((1u << lt) - 1);
@@ -185,17 +192,47 @@ __global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
     __shared__ unsigned long long red[2 * (kPlanThreads / 32)];
     __shared__ float est_s;
     const float est = sketch_estimate(a.sketch, red, &est_s);
+    __shared__ uint32_t shape[2];
     if (threadIdx.x == 0) {
         // The path: grouping when the sample holds at most probe_max_distinct
         // distinct bricks (group_shape derives it from the sampling model).
         const bool redundant = est > 0.0f && est <= a.probe_max_distinct;
         const bool group = a.mode == 2 || (a.mode == 1 && redundant);
+        // The bricks: the sample's distinct count, scaled back by the
+        // sampling model (the redundancy whose sampled ratio matches, by
+        // bisection; the model grows with the redundancy).
+        float bricks = est;
+        if (a.n > kProbeAllMax && est > 0.0f) {
+            const float q = 1.0f / kProbeStride;
+            const float r = (float)(a.n / 8 / kProbeStride) * 8.0f / est;
+            float lo = 1.0f, hi = (float)a.n;
+            for (int it = 0; it < 40; ++it) {
+                const float mid = 0.5f * (lo + hi);
+                if (q * mid / (1.0f - powf(1.0f - q, mid)) < r) lo = mid; else hi = mid;
+            }
+            bricks = (float)a.n / lo;
+        }
+        // Partitions: at most kGroupMaxParts, and enough that each holds
+        // ~kGroupTargetBricksPerPart bricks (table load ~0.35), at most 65536
+        // fragments on average, and that small inputs still spread over 256
+        // CTAs (4096 fragments each). Fewer, larger partitions make the
+        // scatter's runs per tile longer.
+        const uint64_t spread = a.n / 4096 < 256 ? a.n / 4096 : 256;
+        int lp = 0;
+        while (lp < kGroupPartLog && ((float)(1u << lp) * kGroupTargetBricksPerPart < bricks ||
+                                      (a.n >> lp) > 65536 || (1ull << lp) < spread))
+            ++lp;
+        const uint64_t mean = (a.n + (1ull << lp) - 1) >> lp;
+        shape[0] = (uint32_t)lp;
+        shape[1] = (uint32_t)(mean + mean / 4 + 1024);
         a.path[0] = group ? 1u : 0u;
-        a.path[1] = (uint32_t)a.parts_log;
+        a.path[1] = (uint32_t)lp;
         a.path[2] = (uint32_t)kGroupPartSlotsLog;
+        a.path[3] = shape[1];
     }
+    __syncthreads();
     // Partition p fills the slab [p * slab_cap, (p + 1) * slab_cap).
-    for (uint32_t p = threadIdx.x; p < (1u << a.parts_log); p += blockDim.x) a.cursor[p] = (uint64_t)p * a.slab_cap;
+    for (uint32_t p = threadIdx.x; p < (1u << shape[0]); p += blockDim.x) a.cursor[p] = (uint64_t)p * shape[1];
 }
 
 // 8-byte asynchronous copy global -> shared (cp.async), and its completion.
@@ -233,6 +270,7 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
     if (a.path[0] != 1u) return;
     const int lp = (int)a.path[1];
     const int parts = 1 << lp;
+    const uint64_t slab_cap = a.path[3];
     uint64_t lo, hi;
     chunk_range(a, &lo, &hi);
     bool bad = false, over = false;  // codes out of range; the overflow area full
@@ -303,7 +341,7 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
                 k = sm.stage[q];
                 const uint32_t pid = part_of<kNarrow>(k, lp);
                 const uint64_t pos = (uint64_t)((int64_t)sm.delta[pid] + q);
-                if (pos < (uint64_t)(pid + 1) * a.slab_cap) {
+                if (pos < (uint64_t)(pid + 1) * slab_cap) {
                     a.parts[pos] = k;
                 } else {
                     // The partition's slab is full (a brick with very many
@@ -335,6 +373,9 @@ constexpr int kAggIlp = 4;
 // Longest probe chain before a partition's table counts as full: at the
 // planned load (< 0.45) chains stay far shorter.
 constexpr uint32_t kAggMaxProbe = 256;
+// A partition whose bricks overfill its table is done again in halves of its
+// hash range, down to 1/2^kAggMaxSplitLog of it.
+constexpr uint32_t kAggMaxSplitLog = 6;
 static_assert((1 << 9) >= kAggThreads, "at least one table slot per thread");
 
 template <bool kNarrow>
@@ -383,62 +424,93 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     if (a.path[0] != 1u) return;
     const uint32_t parts = 1u << a.path[1], lt = a.path[2], slots = 1u << lt;
+    const uint64_t slab_cap = a.path[3];
     bool full = false;
     for (uint32_t p = blockIdx.x; p < parts; p += gridDim.x) {
-        const uint64_t lo = (uint64_t)p * a.slab_cap;
-        const uint64_t hi = a.cursor[p] < lo + a.slab_cap ? a.cursor[p] : lo + a.slab_cap;
-        for (uint32_t s = threadIdx.x; s < slots; s += kAggThreads) {
-            sm.key[s] = 0;
-            sm.mask[s] = 0;
-        }
-        if (threadIdx.x == 0) sm.full = 0;
-        __syncthreads();
-        for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kAggIlp * kAggThreads) {
-            uint64_t k[kAggIlp];
+        const uint64_t lo = (uint64_t)p * slab_cap;
+        const uint64_t hi = a.cursor[p] < lo + slab_cap ? a.cursor[p] : lo + slab_cap;
+        // Work list of sub-ranges (low `level` bits of the brick's sub-hash
+        // equal to `sub`), depth first: a sub-range whose bricks overfill the
+        // table is done again as its two halves. The whole partition is the
+        // one sub-range of level 0.
+        uint32_t todo_sub[kAggMaxSplitLog + 2], todo_level[kAggMaxSplitLog + 2];
+        int ntodo = 1;
+        todo_sub[0] = 0;
+        todo_level[0] = 0;
+        while (ntodo > 0) {  // uniform over the CTA
+            --ntodo;
+            const uint32_t sub = todo_sub[ntodo], level = todo_level[ntodo];
+            const uint32_t sub_mask = (1u << level) - 1;
+            for (uint32_t s = threadIdx.x; s < slots; s += kAggThreads) {
+                sm.key[s] = 0;
+                sm.mask[s] = 0;
+            }
+            if (threadIdx.x == 0) sm.full = 0;
+            __syncthreads();
+            for (uint64_t i0 = lo + threadIdx.x; i0 < hi; i0 += (uint64_t)kAggIlp * kAggThreads) {
+                uint64_t k[kAggIlp];
 #pragma unroll
-            for (int u = 0; u < kAggIlp; ++u) {
-                const uint64_t i = i0 + (uint64_t)u * kAggThreads;
-                k[u] = i < hi ? __ldcs(a.parts + i) : 0;
-            }
+                for (int u = 0; u < kAggIlp; ++u) {
+                    const uint64_t i = i0 + (uint64_t)u * kAggThreads;
+                    k[u] = i < hi ? __ldcs(a.parts + i) : 0;
+                }
 #pragma unroll
-            for (int u = 0; u < kAggIlp; ++u)
-                if (i0 + (uint64_t)u * kAggThreads < hi && !agg_insert<kNarrow>(sm, k[u], lt, slots)) sm.full = 1;
-            if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;  // fail fast: the call reruns
-        }
-        if (a.part_over[p]) {
-            // The partition's slab was full: the rest of its fragments are in
-            // the shared overflow area, among other partitions'.
-            const uint64_t no = *a.overflow_count;
-            for (uint64_t i = threadIdx.x; i < no; i += kAggThreads) {
-                const uint64_t k = a.overflow[i];
-                if (part_of<kNarrow>(k, (int)a.path[1]) == p && !agg_insert<kNarrow>(sm, k, lt, slots)) sm.full = 1;
-                if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;
+                for (int u = 0; u < kAggIlp; ++u)
+                    if (i0 + (uint64_t)u * kAggThreads < hi &&
+                        (level == 0 || (sub_of<kNarrow>(k[u] >> 6) & sub_mask) == sub) &&
+                        !agg_insert<kNarrow>(sm, k[u], lt, slots))
+                        sm.full = 1;
+                if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;  // fail fast
             }
-        }
-        __syncthreads();
-        full |= sm.full != 0;
-        const uint32_t per = slots / kAggThreads, s0 = threadIdx.x * per;
-        uint32_t cnt = 0;
-        for (uint32_t j = 0; j < per; ++j) cnt += sm.key[s0 + j] != 0;
-        uint32_t total;
-        const uint32_t ex = block_exclusive_sum<uint32_t>(cnt, sm.scan, &total);
-        if (threadIdx.x == 0)
-            sm.base = total ? atomicAdd((unsigned long long*)a.d_count, (unsigned long long)total) : 0ull;
-        __syncthreads();
-        uint64_t pos = sm.base + ex;
-        for (uint32_t j = 0; j < per; ++j) {
-            const uint64_t t = (uint64_t)sm.key[s0 + j];
-            if (t == 0) continue;
-            if (pos < a.cap) {
-                a.bricks[pos] = t - 1;
-                a.idx[pos] = (uint32_t)pos;
-                a.masks[pos] = sm.mask[s0 + j];
-            } else {
-                full = true;
+            if (a.part_over[p]) {
+                // The partition's slab was full: the rest of its fragments are
+                // in the shared overflow area, among other partitions'.
+                const uint64_t no = *a.overflow_count;
+                for (uint64_t i = threadIdx.x; i < no; i += kAggThreads) {
+                    const uint64_t k = a.overflow[i];
+                    if (part_of<kNarrow>(k, (int)a.path[1]) == p &&
+                        (level == 0 || (sub_of<kNarrow>(k >> 6) & sub_mask) == sub) &&
+                        !agg_insert<kNarrow>(sm, k, lt, slots))
+                        sm.full = 1;
+                    if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;
+                }
             }
-            ++pos;
+            __syncthreads();
+            if (sm.full) {
+                __syncthreads();  // everyone has read the flag before the table is cleared again
+                if (level < kAggMaxSplitLog) {
+                    todo_sub[ntodo] = sub | (1u << level);
+                    todo_level[ntodo++] = level + 1;
+                    todo_sub[ntodo] = sub;
+                    todo_level[ntodo++] = level + 1;
+                } else {
+                    full = true;  // too many bricks even in a 1/64 sub-range: the call reruns on the sort path
+                }
+                continue;
+            }
+            const uint32_t per = slots / kAggThreads, s0 = threadIdx.x * per;
+            uint32_t cnt = 0;
+            for (uint32_t j = 0; j < per; ++j) cnt += sm.key[s0 + j] != 0;
+            uint32_t total;
+            const uint32_t ex = block_exclusive_sum<uint32_t>(cnt, sm.scan, &total);
+            if (threadIdx.x == 0)
+                sm.base = total ? atomicAdd((unsigned long long*)a.d_count, (unsigned long long)total) : 0ull;
+            __syncthreads();
+            uint64_t pos = sm.base + ex;
+            for (uint32_t j = 0; j < per; ++j) {
+                const uint64_t t = (uint64_t)sm.key[s0 + j];
+                if (t == 0) continue;
+                if (pos < a.cap) {
+                    a.bricks[pos] = t - 1;
+                    a.idx[pos] = (uint32_t)pos;
+                    a.masks[pos] = sm.mask[s0 + j];
+                } else {
+                    full = true;
+                }
+                ++pos;
+            }
+            __syncthreads();  // the table is cleared for the next sub-range
         }
-        __syncthreads();  // the table is cleared for the next partition
     }
     if (full) atomicOr(a.err, kErrFallback);
 }
@@ -504,15 +576,11 @@ void launch_group_probe(const GroupArgs& a, cudaStream_t s) {
     launch_pdl(group_probe, dim3(g), dim3(kFrontThreads), 0, s, a);
 }
 
-void group_shape(uint64_t n, int* parts_log, uint64_t* slab_cap, float* probe_max_distinct) {
-    // Partitions of ~4096 fragments (up to kGroupMaxParts): a partition of an
-    // input with kGroupMinRedundancy fragments per brick holds far fewer
-    // bricks than its table's kGroupPartSlots. Slabs: 1.25 x the mean + 1024.
-    int lp = 0;
-    while (lp < kGroupPartLog && (n >> lp) > 4096) ++lp;
-    const uint64_t mean = (n + (1ull << lp) - 1) >> lp;
-    *parts_log = lp;
-    *slab_cap = mean + mean / 4 + 1024;
+void group_shape(uint64_t n, uint64_t* slab_total, float* probe_max_distinct) {
+    // The partitions (2^k of them, chosen on the device) split the slab
+    // region into slabs of 1.25 x the mean + 1024 fragments.
+    *slab_total = n + n / 4 + (uint64_t)kGroupMaxParts * 1026;
+    const int lp = kGroupPartLog;
     // The path's test. If every brick held rho fragments, a sample keeping
     // each fragment with probability q would hold q * rho / (1 - (1 - q)^rho)
     // fragments per distinct brick (rho when q = 1), a ratio that grows with
