@@ -250,43 +250,26 @@ __global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
 __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // sampled form: kDedupMaxSampledBuckets
+    uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // kDedupMaxSampledBuckets splitters
     const uint64_t u = unique_count(a);
-    const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
-    uint32_t nb;
-    int shift = 64;
-    if (a.sampled) {
-        nb = a.state->nbuckets;
-        if (nb == 0) return;
-        for (uint32_t b = threadIdx.x; b + 1 < nb; b += blockDim.x) spl[b] = a.splitters[b];
-        __syncthreads();
-    } else {
-        nb = topbit_buckets(u, &shift);
-        if ((uint64_t)nb * kDedupPerBucket < u || (uint64_t)nb * cap > a.bucket_area) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
-            return;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) a.state->nbuckets = nb;
-    }
+    const uint32_t cap = a.state->bucket_cap;
+    const uint32_t nb = a.state->nbuckets;
+    if (nb == 0) return;
+    for (uint32_t b = threadIdx.x; b + 1 < nb; b += blockDim.x) spl[b] = a.splitters[b];
+    __syncthreads();
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = u;
     bool over = false;
     for (uint64_t pos = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < u;
          pos += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = a.uniq_key[pos];
-        uint32_t b;
-        if (a.sampled) {
-            uint32_t lo = 0, hi = nb - 1;  // number of splitters <= key
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (spl[mid] <= key) lo = mid + 1; else hi = mid;
-            }
-            b = lo;
-        } else {
-            b = shift >= 64 ? 0u : (uint32_t)(key >> shift);
+        uint32_t lo = 0, hi = nb - 1;  // number of splitters <= key
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (spl[mid] <= key) lo = mid + 1; else hi = mid;
         }
-        const uint32_t slot = atomicAdd(a.bucket_count + b, 1u);
+        const uint32_t slot = atomicAdd(a.bucket_count + lo, 1u);
         if (slot < cap) {
-            const uint64_t e = (uint64_t)b * cap + slot;
+            const uint64_t e = (uint64_t)lo * cap + slot;
             a.bucket_key[e] = key;
             a.bucket_slot[e] = a.uniq_slot[pos];
             a.bucket_rep[e] = a.uniq_item[pos];

@@ -7,29 +7,32 @@
 // Bricks are split into partitions by the top bits of a hash of the brick, so
 // that one partition's distinct bricks fit a table in shared memory:
 //
-//   group_sketch     one read of the fragments: range check, a HyperLogLog
-//                    sketch (4096 registers) of the distinct bricks, and the
-//                    fragment count of each of 2048 fine partitions;
-//   group_plan       one CTA: estimates the distinct bricks B from the sketch
-//                    and picks the path: grouping when the fragments hold at
-//                    least kGroupMinRedundancy per brick and B fits the
-//                    partition tables, else the sort path (every kernel of the
-//                    other path reads the decision and does nothing). Picks
-//                    2^k partitions (B / 384 bricks each) and their starts;
-//   group_scatter    the fragments, by partition: one CTA per SM walks its
-//                    chunk of the input in tiles of 8192 (the next tile
-//                    streams into shared memory while one is processed), a
-//                    counting sort per tile in shared memory, one atomic per
-//                    partition and tile reserves the tile's runs;
+//   group_probe      reads one 64-byte line of fragments in 16 (every
+//                    fragment of small inputs) into a HyperLogLog sketch
+//                    (4096 registers) of their bricks;
+//   group_plan       one CTA: grouping when the sample shows few enough
+//                    distinct bricks for the redundancy the grouping needs
+//                    (the limit comes from the sampling model, group_shape),
+//                    else the sort path (every kernel of the other path reads
+//                    the decision and does nothing); picks 2^k partitions
+//                    from the estimated bricks and n, and their slabs;
+//   group_scatter    the fragments, by partition, into the partitions' slabs:
+//                    one CTA per SM walks its chunk of the input in tiles of
+//                    8192 (the next tile streams into shared memory while one
+//                    is processed), a counting sort per tile in shared memory,
+//                    one atomic per partition and tile reserves the tile's
+//                    runs; fragments past a full slab go to a shared overflow
+//                    area; also the range check;
 //   group_aggregate  one CTA per partition: a table in shared memory of the
-//                    partition's bricks and their masks, then the brick list
-//                    (brick, index) and the masks;
+//                    partition's bricks and their masks (an overfull table is
+//                    redone in halves of the partition's hash range), then the
+//                    brick list (brick, index) and the masks;
 //   (then the brick list is sorted by brick with the radix sort, values =
 //    indices: B items instead of N)
 //   group_gather     parents and masks in sorted brick order.
 //
-// Every pass over the fragments reads or writes them in order (8 bytes per
-// fragment and pass); only the B-sized brick list is sorted.
+// The scatter and the aggregation read or write the fragments in order (8
+// bytes per fragment and pass); only the B-sized brick list is sorted.
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
@@ -52,7 +55,7 @@ __device__ __forceinline__ uint64_t fmix(uint64_t k) {
     return k;
 }
 
-// The sketch's hash: top 12 bits pick the register, the bits below give its
+// The probe's hash: top 12 bits pick the register, the bits below give its
 // rank (they must be close to uniform).
 __device__ __forceinline__ uint64_t brick_hash(uint64_t brick) { return fmix(brick ^ 0x9E3779B97F4A7C15ull); }
 
