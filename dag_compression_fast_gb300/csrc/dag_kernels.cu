@@ -190,11 +190,18 @@ __global__ void leaf_fixup(LeafBuildArgs a) {
 
 // ---------------------------------------------------------------------------
 // Extract one level + node hash. Child codes are unique and sorted, so a
-// parent owns at most 8 consecutive children; the head child builds the node.
+// parent owns at most 8 consecutive children. Each step is one round trip
+// for the whole tile rather than a chain per thread: the tile's child codes
+// and ids, then all their hashes (gathered at once into shared memory); the
+// nodes' first children are compacted in shared memory and the CTA's threads
+// take the nodes in turn, so a sparse level (one child per node) costs what a
+// dense one does.
 // ---------------------------------------------------------------------------
 struct ExtractSmem {
-    uint64_t codes[kPadded];
-    uint32_t map[kTile];
+    uint64_t codes[kPadded];   // the tile's child codes (blocked reads padded)
+    uint64_t hash[kTile];      // the tile's child hashes
+    uint32_t map[kTile];       // the tile's child ids
+    uint16_t head[kTile + 1];  // first child of each node in the tile, in order; then tile_n
     uint32_t scan[34];
     uint32_t slot;
     uint64_t p_base;
@@ -227,16 +234,29 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
     }
     const bool read_first = n > kDedupClaimFirstMax;
     uint32_t* aux = reinterpret_cast<uint32_t*>(dd.table_aux);  // [2s] representative, [2s+1] unique id
-    bool bad = false, full = false;
+    bool bad = false, full = false, overflow = false;
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
         const uint64_t base = (uint64_t)tile * kTile;
         const uint32_t tile_n = (uint32_t)(n - base < (uint64_t)kTile ? n - base : (uint64_t)kTile);
-        for (int i = tid; i < (int)tile_n; i += kT) {
-            S.codes[pad8(i)] = a.child_codes[base + i];
-            S.map[i] = a.child_map[base + i];
+        {
+            uint32_t m[kI];
+#pragma unroll
+            for (int k = 0; k < kI; ++k) {
+                const int i = tid + k * kT;
+                if (i < (int)tile_n) {
+                    S.codes[pad8(i)] = a.child_codes[base + i];
+                    m[k] = a.child_map[base + i];
+                    S.map[i] = m[k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kI; ++k) {
+                const int i = tid + k * kT;
+                if (i < (int)tile_n) S.hash[i] = __ldg(a.child_hashes + m[k]);
+            }
         }
         __syncthreads();
         const int i0 = tid * kI;
@@ -259,44 +279,58 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
         }
         uint32_t total_heads;
         const uint32_t excl = block_exclusive_sum<uint32_t>(heads, S.scan, &total_heads);
+        {
+            uint32_t r = excl;
+#pragma unroll
+            for (int j = 0; j < kI; ++j)
+                if (head_bits & (1u << j)) S.head[r++] = (uint16_t)(i0 + j);
+            if (tid == 0) S.head[total_heads] = (uint16_t)tile_n;
+        }
         if (warp == 0) {
             const uint64_t pb = sv_lookback(a.status, tile, total_heads, a.err);
             if (lane == 0) S.p_base = pb;
         }
         __syncthreads();
-        uint64_t p = S.p_base + excl;
-        bool overflow = false;
-        for (int j = 0; j < kI; ++j) {
-            if (!(head_bits & (1u << j))) continue;
+        const uint64_t p_base = S.p_base;
+        for (uint32_t h = tid; h < total_heads; h += kT) {
+            const uint64_t p = p_base + h;
             if (p >= a.out_capacity) { overflow = true; break; }
-            const int i = i0 + j;
-            const uint64_t code0 = S.codes[pad8(i)];
-            const uint64_t par = code0 >> 3;
+            const int i = S.head[h], e = S.head[h + 1];
+            const uint64_t par = S.codes[pad8(i)] >> 3;
             uint32_t ch[8];
+            uint64_t hc[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) ch[c] = kEmptyChild;
+            for (int c = 0; c < 8; ++c) { ch[c] = kEmptyChild; hc[c] = 0; }
             uint32_t mask = 0;
+#pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const uint64_t gi = base + i + k;
-                if (gi >= n) break;
-                uint64_t code;
-                uint32_t m;
-                if (i + k < (int)tile_n) { code = S.codes[pad8(i + k)]; m = S.map[i + k]; }
-                else { code = a.child_codes[gi]; m = a.child_map[gi]; }
-                if ((code >> 3) != par) break;
+                uint64_t code, hk;
+                uint32_t id;
+                if (i + k < e) {
+                    code = S.codes[pad8(i + k)];
+                    id = S.map[i + k];
+                    hk = S.hash[i + k];
+                } else if (e == (int)tile_n && base + i + k < n) {
+                    // The tile's last node may go on into the next tile.
+                    code = a.child_codes[base + i + k];
+                    if ((code >> 3) != par) break;
+                    id = a.child_map[base + i + k];
+                    hk = __ldg(a.child_hashes + id);
+                } else {
+                    break;
+                }
                 const uint32_t slot = (uint32_t)(code & 7);
-                ch[slot] = m;
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (slot == (uint32_t)c) { ch[c] = id; hc[c] = hk; }
                 mask |= 1u << slot;
             }
-            uint64_t h[8];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) h[c] = ch[c] == kEmptyChild ? 0 : __ldg(a.child_hashes + ch[c]);
+            const uint64_t hv = hash_children(hc);
             a.node_codes[p] = par;
             a.node_masks[p] = (uint8_t)mask;
             uint4* dst = reinterpret_cast<uint4*>(a.node_children + p * 8);
             dst[0] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
             dst[1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
-            const uint64_t hv = hash_children(h);
             a.node_hashes[p] = hv;
             if (fuse) {
                 // The node's hash into the dedup table; the first inserter of
@@ -321,24 +355,23 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
                     const uint32_t b = shift >= 64 ? 0u : (uint32_t)(hv >> shift);
                     const uint32_t bs = atomicAdd(dd.bucket_count + b, 1u);
                     if (bs < kDedupTopBitCap) {
-                        const uint64_t e = (uint64_t)b * kDedupTopBitCap + bs;
-                        dd.bucket_key[e] = hv;
-                        dd.bucket_slot[e] = (uint32_t)sl;
-                        dd.bucket_rep[e] = (uint32_t)p;
+                        const uint64_t be = (uint64_t)b * kDedupTopBitCap + bs;
+                        dd.bucket_key[be] = hv;
+                        dd.bucket_slot[be] = (uint32_t)sl;
+                        dd.bucket_rep[be] = (uint32_t)p;
                     } else {
                         full = true;
                     }
                 }
             }
-            ++p;
         }
-        if (overflow) atomicOr(a.err, kErrCapacity);
         if (tid == 0 && base + tile_n == n) {
-            const uint64_t cnt = S.p_base + total_heads;
+            const uint64_t cnt = p_base + total_heads;
             *a.d_out_n = cnt < a.out_capacity ? cnt : a.out_capacity;
         }
         __syncthreads();
     }
+    if (overflow) atomicOr(a.err, kErrCapacity);
     if (bad) atomicOr(a.err, kErrBadInput);
     if (full) atomicOr(a.err, kErrFallback);
 }
