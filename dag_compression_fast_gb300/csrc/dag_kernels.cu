@@ -493,70 +493,23 @@ __global__ void __launch_bounds__(kT) unique_runs(UniqueArgs a) {
 // ---------------------------------------------------------------------------
 struct TailSmem {
     uint64_t code[2][kTailCap];   // node codes of the level being built / its children
-    uint64_t key[kTailCap];       // node hashes, sorted with idx
-    uint32_t idx[kTailCap];
+    uint64_t key[kTailCap];       // node hashes, by node
+    uint32_t idx[kTailCap];       // sorted position -> node (by hash, then node)
     uint32_t map[2][kTailCap];    // node -> unique id, per level (ping-pong)
     uint64_t uhash[kTailCap];     // the level's unique hashes: the next level's child hashes
+    uint32_t first[kTailCap];     // node -> index of its first child (its children follow it)
     uint8_t mask[kTailCap];
     uint32_t scan[34];
     uint32_t flags;
 };
-
-__device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb, uint32_t ib) {
-    return ka < kb || (ka == kb && ia < ib);
-}
-
-// Bitonic compare-exchange stages of strides `from` down to 1 (all < 32) on
-// the 32-element chunks a warp holds in registers: element e = 32*chunk +
-// lane, partner e ^ stride, through shuffles. `size` is the merge size
-// (0: the first sizes 2..32, whose direction varies within a chunk).
-__device__ __forceinline__ void tail_warp_stages(TailSmem& S, uint32_t P, uint32_t size, uint32_t from) {
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t c = warp; c < P / 32; c += kTailThreads / 32) {
-        const uint32_t e = c * 32 + lane;
-        uint64_t k = S.key[e];
-        uint32_t i = S.idx[e];
-        const uint32_t s0 = size ? size : 2, s1 = size ? size : 32;
-        for (uint32_t sz = s0; sz <= s1; sz <<= 1) {
-            const bool up = (e & sz) == 0;
-            for (uint32_t st = size ? from : sz >> 1; st > 0; st >>= 1) {
-                const uint64_t ko = __shfl_xor_sync(0xFFFFFFFFu, k, st);
-                const uint32_t io = __shfl_xor_sync(0xFFFFFFFFu, i, st);
-                const bool lower = (lane & st) == 0;
-                const bool other_less = pair_less(ko, io, k, i);
-                if (lower == up ? other_less : !other_less) { k = ko; i = io; }
-            }
-        }
-        S.key[e] = k;
-        S.idx[e] = i;
-    }
-}
-
-// Bitonic sort of S.key/S.idx[0, P), P a power of two >= 32: strides of 32
-// and more through shared memory, smaller ones within warps.
-__device__ void tail_sort(TailSmem& S, uint32_t P) {
-    const uint32_t tid = threadIdx.x;
-    tail_warp_stages(S, P, 0, 0);  // sizes 2..32
-    __syncthreads();
-    for (uint32_t size = 64; size <= P; size <<= 1) {
-        for (uint32_t stride = size >> 1; stride >= 32; stride >>= 1) {
-            for (uint32_t t = tid; t < P / 2; t += kTailThreads) {
-                const uint32_t lo = 2 * t - (t & (stride - 1));
-                const uint32_t hi = lo + stride;
-                const bool up = (lo & size) == 0;
-                const uint64_t ka = S.key[lo], kb = S.key[hi];
-                const uint32_t ia = S.idx[lo], ib = S.idx[hi];
-                if (pair_less(kb, ib, ka, ia) == up) {
-                    S.key[lo] = kb; S.key[hi] = ka;
-                    S.idx[lo] = ib; S.idx[hi] = ia;
-                }
-            }
-            __syncthreads();
-        }
-        tail_warp_stages(S, P, size, 16);
-        __syncthreads();
-    }
-}
+static_assert(sizeof(TailSmem) <= 227 * 1024, "tail state fits one CTA's shared memory");
+// The sort's buckets: at most 2^kTailBucketLog, one per thread for the scan;
+// node ids in bucket order + count, start and fill cursor per bucket, in the
+// room of uhash.
+constexpr int kTailBucketLog = 10;
+constexpr uint32_t kTailBuckets = 1u << kTailBucketLog;
+static_assert(kTailBuckets <= (uint32_t)kTailThreads && (4u << kTailBucketLog) >= (uint32_t)kTailCap, "tail buckets");
+static_assert((kTailCap + 3 * kTailBuckets) * 4 <= sizeof(uint64_t) * kTailCap, "tail buckets fit uhash");
 
 __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
     pdl_prologue();
@@ -568,6 +521,27 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
     const uint32_t* cm = a.child_map;
     const uint64_t* ch = a.child_hashes;
     uint64_t nc = *a.d_child_n;
+    if (nc <= (uint64_t)kTailCap) {
+        // The first level's children (codes, ids, and the hashes their ids
+        // index, all below nc) into shared memory, every load in flight at
+        // once; each level then reads only shared memory.
+        constexpr int kPer = kTailCap / kTailThreads;
+        uint64_t c[kPer], h[kPer];
+        uint32_t m[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const uint32_t i = tid + k * kTailThreads;
+            if (i < nc) { c[k] = cc[i]; m[k] = cm[i]; h[k] = ch[i]; }
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const uint32_t i = tid + k * kTailThreads;
+            if (i < nc) { S.code[1][i] = c[k]; S.map[1][i] = m[k]; S.uhash[i] = h[k]; }
+        }
+        cc = S.code[1];
+        cm = S.map[1];
+        ch = S.uhash;
+    }
     int ping = 0;
     __syncthreads();
     for (int l = a.first_level; l >= 0; --l) {
@@ -575,8 +549,8 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
         const uint64_t cap = out.capacity < (uint64_t)kTailCap ? out.capacity : (uint64_t)kTailCap;
         uint64_t* node_code = S.code[ping];
         uint32_t* node_map = S.map[ping];
-        // Extract + hash: one node per distinct child code >> 3, built by the
-        // first child of its run.
+        // Extract: one node per distinct child code >> 3; its first child
+        // (the head of the run) is recorded in node order.
         uint64_t nn = 0;
         for (uint64_t c0 = 0; c0 < nc; c0 += kTailThreads) {
             const uint64_t i = c0 + tid;
@@ -591,26 +565,8 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
             if (head) {
                 const uint64_t p = nn + excl;
                 if (p < cap) {
-                    uint32_t chd[8];
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) chd[c] = kEmptyChild;
-                    uint32_t m = 0;
-                    for (int k = 0; k < 8 && i + k < nc; ++k) {
-                        const uint64_t code = cc[i + k];
-                        if ((code >> 3) != par) break;
-                        chd[code & 7] = cm[i + k];
-                        m |= 1u << (code & 7);
-                    }
-                    uint64_t h[8];
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) h[c] = chd[c] == kEmptyChild ? 0 : ch[chd[c]];
                     node_code[p] = par;
-                    S.key[p] = hash_children(h);
-                    S.idx[p] = (uint32_t)p;
-                    S.mask[p] = (uint8_t)m;
-                    uint4* dst = reinterpret_cast<uint4*>(a.scratch_children + p * 8);
-                    dst[0] = make_uint4(chd[0], chd[1], chd[2], chd[3]);
-                    dst[1] = make_uint4(chd[4], chd[5], chd[6], chd[7]);
+                    S.first[p] = (uint32_t)i;
                 } else {
                     atomicOr(&S.flags, kErrCapacity);
                 }
@@ -619,27 +575,97 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
             __syncthreads();
         }
         const uint32_t n = (uint32_t)(nn < cap ? nn : cap);
-        // Bitonic sort of (hash, node) pairs, padded to a power of two with
-        // (max, max) which sorts after every real pair.
-        uint32_t P = 32;
-        while (P < n) P <<= 1;
-        for (uint32_t i = n + tid; i < P; i += kTailThreads) { S.key[i] = ~0ull; S.idx[i] = 0xFFFFFFFFu; }
+        // Hash: one node per thread (dense warps); a node's children run from
+        // its first child to the next node's.
+        for (uint32_t p = tid; p < n; p += kTailThreads) {
+            const uint32_t f = S.first[p];
+            const uint64_t e = p + 1 < n ? (uint64_t)S.first[p + 1] : nc;
+            const uint32_t cnt = (uint32_t)(e - f < 8 ? e - f : 8);
+            uint64_t code[8], h[8];
+            uint32_t id[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                code[k] = 0;
+                id[k] = 0;
+                h[k] = 0;
+                if ((uint32_t)k < cnt) { code[k] = cc[f + k]; id[k] = cm[f + k]; }
+            }
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if ((uint32_t)k >= cnt) continue;
+                const uint32_t slot = (uint32_t)(code[k] & 7);
+                const uint64_t hk = ch[id[k]];
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (slot == (uint32_t)c) h[c] = hk;
+                m |= 1u << slot;
+            }
+            S.key[p] = hash_children(h);
+            S.mask[p] = (uint8_t)m;
+        }
         __syncthreads();
-        tail_sort(S, P);
-        // Unique with the full compare; node -> unique id into node_map.
+        // Sort of the nodes by (hash, node): counting sort on the hash's top
+        // bits (the hashes are uniform: ~4 nodes per bucket), then each node's
+        // rank among its bucket's. The order goes to idx (sorted position ->
+        // node); the hashes stay by node. The buckets use uhash's room, free
+        // from the hashing to the unique pass.
+        {
+            uint32_t* border = reinterpret_cast<uint32_t*>(S.uhash);
+            uint32_t* bcnt = border + kTailCap;
+            uint32_t* bstart = bcnt + kTailBuckets;
+            uint32_t* bfill = bstart + kTailBuckets;
+            int lb = 0;
+            while (lb < kTailBucketLog && (4u << lb) < n) ++lb;
+            const uint32_t nb = 1u << lb;
+            for (uint32_t b = tid; b < nb; b += kTailThreads) bcnt[b] = 0;
+            __syncthreads();
+            for (uint32_t p = tid; p < n; p += kTailThreads)
+                atomicAdd(&bcnt[lb ? (uint32_t)(S.key[p] >> (64 - lb)) : 0u], 1u);
+            __syncthreads();
+            uint32_t total;
+            const uint32_t ex = block_exclusive_sum<uint32_t>(tid < nb ? bcnt[tid] : 0u, S.scan, &total);
+            if (tid < nb) {
+                bstart[tid] = ex;
+                bfill[tid] = ex;
+            }
+            __syncthreads();
+            for (uint32_t p = tid; p < n; p += kTailThreads) {
+                const uint32_t b = lb ? (uint32_t)(S.key[p] >> (64 - lb)) : 0u;
+                border[atomicAdd(&bfill[b], 1u)] = p;
+            }
+            __syncthreads();
+            for (uint32_t p = tid; p < n; p += kTailThreads) {
+                const uint64_t k = S.key[p];
+                const uint32_t b = lb ? (uint32_t)(k >> (64 - lb)) : 0u;
+                const uint32_t s0 = bstart[b], s1 = s0 + bcnt[b];
+                uint32_t rank = 0;
+                for (uint32_t j = s0; j < s1; ++j) {
+                    const uint32_t q = border[j];
+                    const uint64_t kq = S.key[q];
+                    rank += kq < k || (kq == k && q < p);
+                }
+                S.idx[s0 + rank] = p;
+            }
+            __syncthreads();
+        }
+        // Unique with the full compare; node -> unique id into node_map. A
+        // node's children are the popc(mask) children from its first one on,
+        // in slot order.
         uint64_t uid_base = 0;
         for (uint32_t c0 = 0; c0 < n; c0 += kTailThreads) {
             const uint32_t i = c0 + tid;
             bool head = false;
             if (i < n) {
-                head = i == 0 || S.key[i] != S.key[i - 1];
+                const uint32_t x = S.idx[i];
+                head = i == 0 || S.key[x] != S.key[S.idx[i - 1]];
                 if (!head) {
-                    const uint32_t x = S.idx[i], y = S.idx[i - 1];
-                    const uint4* cx = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)x * 8);
-                    const uint4* cy = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)y * 8);
-                    const uint4 x0 = cx[0], x1 = cx[1], y0 = cy[0], y1 = cy[1];
-                    const bool same = S.mask[x] == S.mask[y] && x0.x == y0.x && x0.y == y0.y && x0.z == y0.z &&
-                                      x0.w == y0.w && x1.x == y1.x && x1.y == y1.y && x1.z == y1.z && x1.w == y1.w;
+                    const uint32_t y = S.idx[i - 1];
+                    bool same = S.mask[x] == S.mask[y];
+                    const uint32_t fx = S.first[x], fy = S.first[y], cnt = __popc((uint32_t)S.mask[x]);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if ((uint32_t)k < cnt) same &= cm[fx + k] == cm[fy + k];
                     if (!same) atomicOr(&S.flags, kErrCollision);
                 }
             }
@@ -651,13 +677,32 @@ __global__ void __launch_bounds__(kTailThreads) tail_levels(TailArgs a) {
                 const uint32_t x = S.idx[i];
                 node_map[x] = (uint32_t)uid;
                 if (head && uid < out.capacity) {
-                    out.hashes[uid] = S.key[i];
-                    S.uhash[uid] = S.key[i];
-                    out.masks[uid] = S.mask[x];
-                    const uint4* src = reinterpret_cast<const uint4*>(a.scratch_children + (uint64_t)x * 8);
+                    out.hashes[uid] = S.key[x];
+                    S.uhash[uid] = S.key[x];
+                    const uint32_t m = S.mask[x], f = S.first[x], cnt = __popc(m);
+                    out.masks[uid] = (uint8_t)m;
+                    uint32_t chd[8];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) chd[c] = kEmptyChild;
+                    uint64_t code[8];
+                    uint32_t id[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        code[k] = 0;
+                        id[k] = 0;
+                        if ((uint32_t)k < cnt) { code[k] = cc[f + k]; id[k] = cm[f + k]; }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        if ((uint32_t)k >= cnt) continue;
+                        const uint32_t slot = (uint32_t)(code[k] & 7);
+#pragma unroll
+                        for (int c = 0; c < 8; ++c)
+                            if (slot == (uint32_t)c) chd[c] = id[k];
+                    }
                     uint4* dst = reinterpret_cast<uint4*>(out.children + uid * 8);
-                    dst[0] = src[0];
-                    dst[1] = src[1];
+                    dst[0] = make_uint4(chd[0], chd[1], chd[2], chd[3]);
+                    dst[1] = make_uint4(chd[4], chd[5], chd[6], chd[7]);
                 }
             }
             uid_base += total;

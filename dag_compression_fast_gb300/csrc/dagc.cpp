@@ -1011,7 +1011,6 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             ta.child_map = child_map;
             ta.child_hashes = child_hashes;
             ta.d_child_n = d_child_n;
-            ta.scratch_children = P32(Lo.o_NCH);
             for (int l = 0; l <= tail_first; ++l) {
                 ta.lv[l].hashes = P64(Lo.o_ph[l]);
                 ta.lv[l].masks = P8(Lo.o_pm[l]);

@@ -280,7 +280,6 @@ struct TailArgs {
     int first_level;
     const uint64_t* child_codes; const uint32_t* child_map; const uint64_t* child_hashes;
     const uint64_t* d_child_n;
-    uint32_t* scratch_children;  // kTailCap * 8 words
     TailLevelOut lv[kMaxTailLevels];
     uint32_t* err;
 };
