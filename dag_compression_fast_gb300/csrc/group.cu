@@ -59,13 +59,16 @@ __device__ __forceinline__ uint64_t fmix(uint64_t k) {
 // rank (they must be close to uniform).
 __device__ __forceinline__ uint64_t brick_hash(uint64_t brick) { return fmix(brick ^ 0x9E3779B97F4A7C15ull); }
 
+constexpr uint32_t kNarrowMul = 0x9E3779B1u, kNarrowMulInv = 0x0E8B2F51u;
+static_assert(kNarrowMul * kNarrowMulInv == 1u, "inverse mod 2^32");
+
 // The partition's hash, one multiply (Fibonacci hashing): its top
 // kGroupPartLog bits are the fine partition, the bits below them the slot in
 // the partition's table. Narrow form (every brick below 2^31): a 32-bit
 // multiply of the brick, and 32-bit table keys.
 template <bool kNarrow>
 __device__ __forceinline__ uint32_t fine_part(uint64_t brick) {
-    if (kNarrow) return ((uint32_t)brick * 0x9E3779B1u) >> (32 - kGroupPartLog);
+    if (kNarrow) return ((uint32_t)brick * kNarrowMul) >> (32 - kGroupPartLog);
     return (uint32_t)((brick * 0x9E3779B97F4A7C15ull) >> (64 - kGroupPartLog));
 }
 template <bool kNarrow>
@@ -76,13 +79,32 @@ __device__ __forceinline__ uint32_t part_of(uint64_t key, int lp) {
 // product (the partition and the slot take the top ones).
 template <bool kNarrow>
 __device__ __forceinline__ uint32_t sub_of(uint64_t brick) {
-    if (kNarrow) return (uint32_t)brick * 0x9E3779B1u;
+    if (kNarrow) return (uint32_t)brick * kNarrowMul;
     return (uint32_t)(brick * 0x9E3779B97F4A7C15ull);
 }
 template <bool kNarrow>
 __device__ __forceinline__ uint32_t slot_of(uint64_t brick, uint32_t lt) {
-    if (kNarrow) return (((uint32_t)brick * 0x9E3779B1u) >> (32 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+    if (kNarrow) return (((uint32_t)brick * kNarrowMul) >> (32 - kGroupPartLog - lt)) & ((1u << lt) - 1);
     return (uint32_t)((brick * 0x9E3779B97F4A7C15ull) >> (64 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+}
+
+// Narrow form: the 32-bit product is a bijection of the brick (odd
+// multiplier) and a partition's slab implies its top lp bits, so a slab entry
+// is one word: the product's low 32 - lp bits, then the fragment's 6-bit
+// voxel index (lp >= kCompactMinPartLog). The brick comes back as the product
+// times the multiplier's inverse mod 2^32.
+constexpr int kCompactMinPartLog = 6;
+__device__ __forceinline__ uint32_t compact_word(uint64_t key, int lp) {
+    const uint32_t h = (uint32_t)(key >> 6) * kNarrowMul;
+    return ((h << lp) >> (lp - 6)) | (uint32_t)(key & 63);
+}
+// Slot and brick of a compact word's product remainder r = w >> 6 (the slot
+// and sub-range bits lie within the remainder's 32 - lp bits).
+__device__ __forceinline__ uint32_t compact_slot(uint32_t r, uint32_t lt) {
+    return (r >> (32 - kGroupPartLog - lt)) & ((1u << lt) - 1);
+}
+__device__ __forceinline__ uint64_t compact_brick(uint32_t part, int lp, uint32_t r) {
+    return (uint64_t)(((part << (32 - lp)) | r) * kNarrowMulInv);
 }
 
 __device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t count, uint64_t i) {
@@ -225,6 +247,7 @@ __global__ void __launch_bounds__(kPlanThreads) group_plan(GroupArgs a) {
         while (lp < kGroupPartLog && ((float)(1u << lp) * kGroupTargetBricksPerPart < bricks ||
                                       (a.n >> lp) > 65536 || (1ull << lp) < spread))
             ++lp;
+        if (a.narrow && lp < kCompactMinPartLog) lp = kCompactMinPartLog;  // compact slab entries
         const uint64_t mean = (a.n + (1ull << lp) - 1) >> lp;
         shape[0] = (uint32_t)lp;
         shape[1] = (uint32_t)(mean + mean / 4 + 1024);
@@ -253,7 +276,7 @@ static_assert(kScatterTile <= 65536 && kGroupMaxParts <= 65536, "rank and partit
 
 struct ScatterSmem {
     uint64_t in[kScatterTile];       // the next tile's keys, copied in while this tile is processed
-    uint64_t stage[kScatterTile];    // this tile's keys, by partition
+    uint64_t stage[kScatterTile];    // this tile's keys, by partition (narrow: words + partition ids)
     uint32_t cnt[kGroupMaxParts];    // the tile's count per partition, then its offset in the tile
     int64_t delta[kGroupMaxParts];   // output position - tile position, per partition
     uint32_t scan[34];
@@ -270,6 +293,10 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ScatterSmem& sm = *reinterpret_cast<ScatterSmem*>(smem_raw);
+    // Narrow form: compact words (4 bytes) staged with their partition ids.
+    uint32_t* stage_w = reinterpret_cast<uint32_t*>(sm.stage);
+    uint16_t* stage_p = reinterpret_cast<uint16_t*>(stage_w + kScatterTile);
+    uint32_t* parts_w = reinterpret_cast<uint32_t*>(a.parts);
     if (a.path[0] != 1u) return;
     const int lp = (int)a.path[1];
     const int parts = 1 << lp;
@@ -288,13 +315,14 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
         for (int k = 0; k < kScatterPer; ++k) key[k] = sm.in[k * kScatterThreads + threadIdx.x];
         __syncthreads();  // `in` is free for the next tile
         if (base + kScatterTile < hi) scatter_prefetch(sm, a.frags, base + kScatterTile, hi);
-        uint32_t pr[kScatterPer];
+        uint32_t pr[kScatterPer], w[kScatterPer];
 #pragma unroll
         for (int k = 0; k < kScatterPer; ++k) {
             const uint64_t i = base + (uint64_t)k * kScatterThreads + threadIdx.x;
             if (i >= hi) continue;
             key[k] = key_of(a, i, key[k], &bad);
             const uint32_t pid = part_of<kNarrow>(key[k], lp);
+            if (kNarrow) w[k] = compact_word(key[k], lp);
             pr[k] = (pid << 16) | atomicAdd(&sm.cnt[pid], 1u);
         }
         __syncthreads();
@@ -328,24 +356,37 @@ __global__ void __launch_bounds__(kScatterThreads) group_scatter(GroupArgs a) {
         for (int k = 0; k < kScatterPer; ++k) {
             const uint64_t i = base + (uint64_t)k * kScatterThreads + threadIdx.x;
             if (i >= hi) continue;
-            sm.stage[sm.cnt[pr[k] >> 16] + (pr[k] & 0xFFFFu)] = key[k];
+            const uint32_t off = sm.cnt[pr[k] >> 16] + (pr[k] & 0xFFFFu);
+            if (kNarrow) {
+                stage_w[off] = w[k];
+                stage_p[off] = (uint16_t)(pr[k] >> 16);
+            } else {
+                sm.stage[off] = key[k];
+            }
         }
         __syncthreads();
         // Write-out in tile order: runs of one partition are contiguous. The
-        // partition is recomputed from the key (cheaper than storing it).
+        // wide form recomputes the partition from the key.
         const uint32_t m = (uint32_t)(hi - base < (uint64_t)kScatterTile ? hi - base : (uint64_t)kScatterTile);
         const uint32_t lane = threadIdx.x & 31;
 #pragma unroll 4
         for (uint32_t q0 = 0; q0 < m; q0 += kScatterThreads) {  // uniform over the CTA: every lane votes
             const uint32_t q = q0 + threadIdx.x;
-            uint64_t k = 0;
+            uint64_t k = 0;  // wide: the key; narrow: the word, with the partition above it for the overflow area
             bool spill = false;
             if (q < m) {
-                k = sm.stage[q];
-                const uint32_t pid = part_of<kNarrow>(k, lp);
+                uint32_t pid;
+                if (kNarrow) {
+                    pid = stage_p[q];
+                    k = ((uint64_t)pid << 32) | stage_w[q];
+                } else {
+                    k = sm.stage[q];
+                    pid = part_of<kNarrow>(k, lp);
+                }
                 const uint64_t pos = (uint64_t)((int64_t)sm.delta[pid] + q);
                 if (pos < (uint64_t)(pid + 1) * slab_cap) {
-                    a.parts[pos] = k;
+                    if (kNarrow) parts_w[pos] = (uint32_t)k;
+                    else a.parts[pos] = k;
                 } else {
                     // The partition's slab is full (a brick with very many
                     // fragments): to the shared overflow area.
@@ -392,13 +433,12 @@ struct AggSmem {
 };
 
 // One fragment into the partition's table: find or claim its brick's slot
-// (linear probing), OR its bit into the mask. False when the table is full.
+// (linear probing from `s`; the brick's tag is nonzero), OR its bit into the
+// mask. False when the table is full.
 template <bool kNarrow>
-__device__ __forceinline__ bool agg_insert(AggSmem<kNarrow>& sm, uint64_t key, uint32_t lt, uint32_t slots) {
+__device__ __forceinline__ bool agg_insert(AggSmem<kNarrow>& sm, typename AggSmem<kNarrow>::Key tag, uint32_t s,
+                                           uint32_t bit, uint32_t slots) {
     using Key = typename AggSmem<kNarrow>::Key;
-    const uint64_t brick = key >> 6;
-    const Key tag = (Key)brick + 1;
-    uint32_t s = slot_of<kNarrow>(brick, lt);
     Key cur = *reinterpret_cast<volatile Key*>(&sm.key[s]);
     if (cur != tag) {
         // Rare: the brick's first fragment here, or a collision.
@@ -413,9 +453,26 @@ __device__ __forceinline__ bool agg_insert(AggSmem<kNarrow>& sm, uint64_t key, u
             if (cur == tag) break;
         }
     }
-    const uint32_t bit = (uint32_t)(key & 63);
     atomicOr(reinterpret_cast<uint32_t*>(&sm.mask[s]) + (bit >> 5), 1u << (bit & 31));
     return true;
+}
+
+// A slab entry into the table. Wide: the key, tag brick + 1. Narrow: the
+// compact word, tag (product remainder) + 1, unique within the partition.
+template <bool kNarrow>
+__device__ __forceinline__ bool agg_entry(AggSmem<kNarrow>& sm, uint64_t e, uint32_t lt, uint32_t slots) {
+    if constexpr (kNarrow) {
+        const uint32_t r = (uint32_t)e >> 6;
+        return agg_insert<true>(sm, r + 1, compact_slot(r, lt), (uint32_t)e & 63, slots);
+    } else {
+        const uint64_t brick = e >> 6;
+        return agg_insert<false>(sm, brick + 1, slot_of<false>(brick, lt), (uint32_t)(e & 63), slots);
+    }
+}
+// Sub-range bits of a slab entry: the low bits of the partition's product.
+template <bool kNarrow>
+__device__ __forceinline__ uint32_t entry_sub(uint64_t e) {
+    return kNarrow ? (uint32_t)e >> 6 : sub_of<false>(e >> 6);
 }
 
 template <bool kNarrow>
@@ -426,7 +483,9 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
     using Key = typename Smem::Key;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
     if (a.path[0] != 1u) return;
-    const uint32_t parts = 1u << a.path[1], lt = a.path[2], slots = 1u << lt;
+    const int lp = (int)a.path[1];
+    const uint32_t parts = 1u << lp, lt = a.path[2], slots = 1u << lt;
+    const uint32_t* parts_w = reinterpret_cast<const uint32_t*>(a.parts);  // narrow: compact words
     const uint64_t slab_cap = a.path[3];
     bool full = false;
     for (uint32_t p = blockIdx.x; p < parts; p += gridDim.x) {
@@ -455,13 +514,14 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
 #pragma unroll
                 for (int u = 0; u < kAggIlp; ++u) {
                     const uint64_t i = i0 + (uint64_t)u * kAggThreads;
-                    k[u] = i < hi ? __ldcs(a.parts + i) : 0;
+                    if (kNarrow) k[u] = i < hi ? __ldcs(parts_w + i) : 0u;
+                    else k[u] = i < hi ? __ldcs(a.parts + i) : 0ull;
                 }
 #pragma unroll
                 for (int u = 0; u < kAggIlp; ++u)
                     if (i0 + (uint64_t)u * kAggThreads < hi &&
-                        (level == 0 || (sub_of<kNarrow>(k[u] >> 6) & sub_mask) == sub) &&
-                        !agg_insert<kNarrow>(sm, k[u], lt, slots))
+                        (level == 0 || (entry_sub<kNarrow>(k[u]) & sub_mask) == sub) &&
+                        !agg_entry<kNarrow>(sm, k[u], lt, slots))
                         sm.full = 1;
                 if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;  // fail fast
             }
@@ -470,10 +530,12 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
                 // in the shared overflow area, among other partitions'.
                 const uint64_t no = *a.overflow_count;
                 for (uint64_t i = threadIdx.x; i < no; i += kAggThreads) {
+                    // Narrow entries carry their partition in the high word.
                     const uint64_t k = a.overflow[i];
-                    if (part_of<kNarrow>(k, (int)a.path[1]) == p &&
-                        (level == 0 || (sub_of<kNarrow>(k >> 6) & sub_mask) == sub) &&
-                        !agg_insert<kNarrow>(sm, k, lt, slots))
+                    const uint32_t kp = kNarrow ? (uint32_t)(k >> 32) : part_of<kNarrow>(k, lp);
+                    const uint64_t e = kNarrow ? (uint64_t)(uint32_t)k : k;
+                    if (kp == p && (level == 0 || (entry_sub<kNarrow>(e) & sub_mask) == sub) &&
+                        !agg_entry<kNarrow>(sm, e, lt, slots))
                         sm.full = 1;
                     if (*reinterpret_cast<volatile uint32_t*>(&sm.full)) break;
                 }
@@ -504,7 +566,7 @@ __global__ void __launch_bounds__(kAggThreads) group_aggregate(GroupArgs a) {
                 const uint64_t t = (uint64_t)sm.key[s0 + j];
                 if (t == 0) continue;
                 if (pos < a.cap) {
-                    a.bricks[pos] = t - 1;
+                    a.bricks[pos] = kNarrow ? compact_brick(p, lp, (uint32_t)t - 1) : t - 1;
                     a.idx[pos] = (uint32_t)pos;
                     a.masks[pos] = sm.mask[s0 + j];
                 } else {
