@@ -1049,12 +1049,14 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // Algorithmic bytes: the minimum each stage must read and write.
         const uint64_t p0 = counts[kCntBricks], lv = counts[kCntLeaves];
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 8 * n + 16 * p0);
-        // Grouping: the probe reads a sixteenth of the fragments, the
-        // aggregation 8 bytes per fragment, the scatter reads and writes 8;
-        // the brick sort and the gather move ~60 bytes per brick.
+        // Grouping: the probe reads a sixteenth of the fragments; the scatter
+        // reads 8 bytes per fragment and writes its slab entry (4 bytes in the
+        // narrow form, else 8), which the aggregation reads; the brick sort
+        // and the gather move ~60 bytes per brick.
+        const uint64_t entry = sort_hi <= 37 ? 4 : 8;
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_SKETCH, n / 2);
-        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, 16 * n);
-        set_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, 8 * n + 20 * p0);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, (8 + entry) * n);
+        set_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, entry * n + 20 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP, 60 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
         uint64_t lb = 0;

@@ -31,8 +31,10 @@
 //    indices: B items instead of N)
 //   group_gather     parents and masks in sorted brick order.
 //
-// The scatter and the aggregation read or write the fragments in order (8
-// bytes per fragment and pass); only the B-sized brick list is sorted.
+// The scatter reads the fragments in order and writes one slab entry per
+// fragment (4 bytes in the narrow form: the brick's 32-bit product without
+// the partition bits, and the voxel index; else the 8-byte key), which the
+// aggregation reads in order; only the B-sized brick list is sorted.
 
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
