@@ -202,6 +202,7 @@ struct dagc_context_t {
     bool use_graphs = true;
     cudaStream_t capture_stream = nullptr;
     std::vector<GraphEntry> graphs;
+    std::vector<GraphKey> graph_seen;  // call shapes launched directly once; recorded when seen again
     int shape_keys = 5, shape_pairs = 3;  // digit-pass shapes (see dagc_set_option), tuned on GB300
     int occ_keys[kNumSortShapes] = {}, occ_pairs[kNumSortShapes] = {};
     StageStats stages[DAGC_NUM_STAGES];
@@ -519,12 +520,14 @@ uint64_t level_cap(int level, uint64_t n) {
 void drop_graphs(dagc_context ctx) {
     for (GraphEntry& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
     ctx->graphs.clear();
+    ctx->graph_seen.clear();
 }
 
 // Runs `enqueue` (which puts one call's whole kernel sequence on a stream).
-// With graphs on, the sequence is recorded once on the context's own capture
-// stream and replayed on `s` afterwards, which removes the per-launch host
-// cost; with profiling on (events per stage) it is launched directly.
+// With graphs on, a call shape's second call records the sequence on the
+// context's own capture stream and later calls replay it on `s`, which removes
+// the per-launch host cost (a shape's first call launches directly); with
+// profiling on (events per stage) it is launched directly.
 template <typename F>
 int run_enqueue(dagc_context ctx, const GraphKey& key, cudaStream_t s, F&& enqueue) {
     if (!ctx->use_graphs || ctx->profiling || !ctx->capture_stream) return enqueue(s);
@@ -534,6 +537,23 @@ int run_enqueue(dagc_context ctx, const GraphKey& key, cudaStream_t s, F&& enque
             ctx->launches += g.launches;
             return DAGC_OK;
         }
+    }
+    // A call shape seen for the first time launches directly: recording and
+    // instantiating a graph costs more than one direct launch sequence, and a
+    // stream of requests of ever new sizes would pay that on every call. The
+    // shape's second call records it.
+    bool seen = false;
+    for (size_t i = 0; i < ctx->graph_seen.size(); ++i) {
+        if (ctx->graph_seen[i] == key) {
+            ctx->graph_seen.erase(ctx->graph_seen.begin() + i);
+            seen = true;
+            break;
+        }
+    }
+    if (!seen) {
+        if (ctx->graph_seen.size() >= 16) ctx->graph_seen.erase(ctx->graph_seen.begin());
+        ctx->graph_seen.push_back(key);
+        return enqueue(s);
     }
     // Entries made for an arena block that has since been replaced are dead.
     for (size_t i = 0; i < ctx->graphs.size();) {

@@ -53,6 +53,8 @@ __device__ __forceinline__ uint32_t segment_from(const uint64_t* off, uint32_t c
     return hint;
 }
 
+constexpr uint64_t kHistMinPerThread = 16;
+
 __global__ void __launch_bounds__(kSortThreads)
 radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t n_host, int lo_bit,
                 int hi_bit, int validate_bits, uint32_t* __restrict__ hist, uint32_t* status0,
@@ -70,15 +72,24 @@ radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t
     const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = gtid; i < status_words; i += gstride) status0[i] = 0;
     __syncthreads();
+    // Only the CTAs the keys need (at least kHistMinPerThread keys per
+    // thread) build histograms: the grid is sized by the bound, and for a
+    // small count each CTA's flush of ~1000 bins into the global histogram
+    // would cost more than its keys.
+    const uint64_t per_cta = (uint64_t)blockDim.x * kHistMinPerThread;
+    const uint64_t want = (n + per_cta - 1) / per_cta;
+    const uint32_t active = (uint32_t)(want < gridDim.x ? (want > 0 ? want : 1) : gridDim.x);
+    if (blockIdx.x >= active) return;
+    const uint64_t astride = (uint64_t)active * blockDim.x;
 
     // Four independent loads in flight per thread (grid-stride, unrolled).
     uint64_t bad = 0;
-    for (uint64_t i0 = gtid; i0 < n; i0 += 4 * gstride) {
+    for (uint64_t i0 = gtid; i0 < n; i0 += 4 * astride) {
         uint64_t k[4];
         bool in[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const uint64_t i = i0 + u * gstride;
+            const uint64_t i = i0 + u * astride;
             in[u] = i < n;
             k[u] = in[u] ? __ldg(keys + i) : 0;
         }
@@ -87,7 +98,7 @@ radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t
             if (!in[u]) continue;
             if (validate_bits > 0 && validate_bits < 64) bad |= k[u] >> validate_bits;
             if (seg_offsets)
-                k[u] |= (uint64_t)segment_search(seg_offsets, seg_count, i0 + u * gstride) << seg_shift;
+                k[u] |= (uint64_t)segment_search(seg_offsets, seg_count, i0 + u * astride) << seg_shift;
             for (int p = 0; p < passes; ++p) {
                 const int shift = lo_bit + p * kRadixBits;
                 const int bits = min(kRadixBits, hi_bit - shift);

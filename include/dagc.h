@@ -156,8 +156,10 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * 5 = (16, 3, alternate), 6 = (16, 2, alternate), 7 = (12, 3, alternate). */
 #define DAGC_OPT_SORT_SHAPE_KEYS 1   /* keys-only sorts (the fragment sort) */
 #define DAGC_OPT_SORT_SHAPE_PAIRS 2  /* key/value sorts (leaf and node hashes) */
-/* 1 (default): record each CreateDAG kernel sequence once as a CUDA graph and
- * replay it for later calls with the same input pointer, size and depth;
+/* 1 (default): launch a CreateDAG kernel sequence directly the first time its
+ * input pointer, size and depth are seen, record it as a CUDA graph the second
+ * time and replay the graph for later calls with the same shape (recording
+ * costs more than one direct launch, so one-off shapes never pay it);
  * 0: launch every kernel directly. Profiling always launches directly. */
 #define DAGC_OPT_GRAPHS 3
 /* 1 (default): deduplicate the leaves and each level with a hash set and sort

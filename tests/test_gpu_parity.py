@@ -258,13 +258,15 @@ def test_graph_replay_matches_direct_launches(ctx):
     codes = random_codes(10, 400_000, 21, cluster=True)
     t = torch.from_numpy(codes.view(np.int64)).cuda()
     ref = O.create_dag(codes, 10)
-    for _ in range(3):  # first call records, the next two replay
+    for _ in range(4):  # first call launches directly, the second records, the rest replay
         assert_dag_equal(ctx.create_dag(t, 10).to_host(), ref)
     ctx.set_option(D.OPT_GRAPHS, 0)
     try:
         assert_dag_equal(ctx.create_dag(t, 10).to_host(), ref)
     finally:
         ctx.set_option(D.OPT_GRAPHS, 1)
+    for _ in range(2):  # recorded again
+        assert_dag_equal(ctx.create_dag(t, 10).to_host(), ref)
     # A different input in the same buffer: the replay must see the new data.
     codes2 = random_codes(10, 400_000, 22, cluster=True)
     t.copy_(torch.from_numpy(codes2.view(np.int64)))
