@@ -81,7 +81,13 @@ def main(argv=None) -> int:
     jobs = make_jobs(a.jobs, a.seed)
     gen_s = time.perf_counter() - t0
     srv = D.Server(0, slots=a.slots, hbm_budget_bytes=int(a.budget_gb * (1 << 30)))
-    run_rate(srv, jobs[: min(8, len(jobs))], 1e6, a.seed)  # warm the slots (arenas, graphs)
+    # Warm the slots with every job once, all at once: each slot grows its
+    # arena and sees the call shapes, as a running server has. The rates
+    # below then measure steady state; this pass's latencies are the cold
+    # cost and are printed first.
+    cold = run_rate(srv, jobs, 1e6, a.seed)
+    print(json.dumps({"warmup_pass": True, "jobs": cold["jobs"], "p50_ms": cold["p50_ms"],
+                      "p99_ms": cold["p99_ms"], "wall_s": cold["wall_s"]}), flush=True)
     for r in a.rates:
         res = run_rate(srv, jobs, r, a.seed + int(r))
         st = srv.stats()
