@@ -429,7 +429,7 @@ struct AggSmem {
     using Key = typename std::conditional<kNarrow, uint32_t, unsigned long long>::type;
     uint32_t full;                   // a probe chain ran out: the partition gives up
     uint64_t mask[kGroupPartSlots];  // OR of the fragments' bits
-    Key key[kGroupPartSlots];        // brick + 1, 0 = empty
+    Key key[kGroupPartSlots];        // tag (wide: brick + 1; narrow: product remainder + 1), 0 = empty
     uint32_t scan[34];
     uint64_t base;
 };
