@@ -1,11 +1,18 @@
 #!/usr/bin/env python
 """Benchmark: input voxels/s from Morton fragments to the final DAG on GB300.
 
-Workload: the procedural terrain of a 2048^3 grid (depth 11): 4-octave fBm
-heightfield, 3-voxel-thick surface, every voxel emitted U{1..4} times and
-shuffled -> ~31.5M uint64 fragments (252 MB, larger than the 129 MB L2, so
-every step streams from HBM). Seeded synthetic data stands in for the
+Headline workload (the largest single-GPU configuration): a random triangle
+soup in an 8192^3 grid (depth 13). 2M triangles with seeded uniform vertex
+positions and edge lengths log-uniform in 1-16 voxels, conservatively
+surface-voxelized (triangle/box separating-axis test) to ~65M uint64 Morton
+fragments, shuffled (520 MB, larger than the 129 MB L2, so every step streams
+from HBM). Low redundancy (about 5.8 fragments per 4^3 brick): the device
+takes the radix-sort path. Seeded synthetic data stands in for the
 reference's voxelized glTF scene.
+
+Second workload, reported under "terrain_2048": the fBm terrain heightfield
+of a 2048^3 grid (depth 11), ~31.5M fragments, on which the device takes the
+fragment-grouping path.
 
 One step = DAGCompression::CreateDAG + CreateFinalDAG through the dagc C ABI,
 from device-resident fragments to the device-resident uint32 DAG.
@@ -13,15 +20,18 @@ from device-resident fragments to the device-resident uint32 DAG.
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
 --impl reference times the reference's algorithm on the host cores instead
-(the CPU oracle, all threads), same workload and metric.
+(the CPU restatement of src/DAGCompression.cu, every host thread), on the
+same workload, metric and config.
 Multi-GPU runs (torchrun) are independent replicas: the path has no exchange
 step on one volume, so each rank compresses its own copy ("weak" scaling).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -36,10 +46,10 @@ if REPO not in sys.path:
 
 METRIC = "input voxels/sec to final DAG; % HBM roofline; batched p50/p99 ms per chunk"
 UNIT = "voxels/s"
-DEPTH = 11
-SEED = 0xDA6C0DE + 1
-WORKLOAD = "terrain_fbm_2048^3_depth11"
-L2_NOTE = "inputs (252 MB of fragments per step) larger than the 129 MB L2"
+
+SOUP = {"name": "triangle_soup_8192^3_depth13_2M_triangles", "depth": 13, "seed": 0xDA6C0DE + 3,
+        "triangles": 2_000_000}
+TERRAIN = {"name": "terrain_fbm_2048^3_depth11", "depth": 11, "seed": 0xDA6C0DE + 1}
 
 
 def parse_args():
@@ -49,8 +59,47 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="dagc", choices=["dagc", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    p.add_argument("--soak-seconds", type=float, default=1.0,
+                   help="untimed steps run right before the timed region while the clocks are sampled")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-terrain", action="store_true", help="skip the second (terrain) workload")
     return p.parse_args()
+
+
+def soup_codes() -> np.ndarray:
+    import dag_compression_fast_gb300 as D
+    return D.gen_triangle_soup(SOUP["depth"], SOUP["seed"], SOUP["triangles"])
+
+
+def terrain_codes() -> np.ndarray:
+    import dag_compression_fast_gb300 as D
+    return D.gen_terrain(TERRAIN["depth"], TERRAIN["seed"])
+
+
+def bench_config(n: int, world: int) -> dict:
+    """The config both arms print (identical keys and values)."""
+    return {"workload": SOUP["name"], "fragments": int(n), "depth": SOUP["depth"], "triangles": SOUP["triangles"],
+            "seed": SOUP["seed"], "voxelization": "conservative (triangle/box separating-axis test)",
+            "l2": f"inputs ({8 * n / 1e6:.0f} MB of fragments per step) larger than the 129 MB L2",
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            k = line.split(":")[0].strip().lower()
+            if k in ("model name", "cpu model", "hardware"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return platform.processor() or platform.machine()
 
 
 def dist_setup():
@@ -96,7 +145,7 @@ def stage_roofline(prof, stage, kernel, peak, peak_kind, traffic):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms in the background."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -113,7 +162,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-i", str(self.device), "-lms", "200"],
+                 "-i", str(self.device), "-lms", "100"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -126,7 +175,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
@@ -135,6 +184,7 @@ class ClockSampler:
             try:
                 sm.append(float(f[1]))
                 smax.append(float(f[2]))
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for name, v in zip(names, f[5:9]):
@@ -144,53 +194,82 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def time_oracle(codes: np.ndarray, depth: int, threads: int, budget_s: float, max_reps: int = 50):
+    """CreateDAG + CreateFinalDAG of the CPU restatement, repeated until the budget is spent."""
+    from oracle import oracle as O
+    O.create_dag(codes[:1000], depth, threads)  # load + warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        O.final_dag(O.create_dag(codes, depth, threads))
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or reps >= max_reps:
+            return codes.size * reps / el, reps, el
 
 
 def cpu_baseline(codes: np.ndarray, budget_s: float):
     """The oracle (the reference's algorithm restated on the CPU) on the same
-    fragments with every host thread; repeated until the budget is spent."""
-    from oracle import oracle as O
+    fragments with every host thread, plus one thread on a bounded prefix."""
     threads = os.cpu_count() or 1
-    O.create_dag(codes[:1000], DEPTH, threads)  # load + warm
-    reps, t0 = 0, time.perf_counter()
-    while True:
-        d = O.create_dag(codes, DEPTH, threads)
-        O.final_dag(d)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or reps >= 50:
-            break
-    return {"value": codes.size * reps / el, "unit": UNIT, "cores": threads, "kind": "port",
+    depth = SOUP["depth"]
+    value, reps, el = time_oracle(codes, depth, threads, budget_s)
+    sample = codes[: min(codes.size, 4_000_000)]
+    v1, reps1, el1 = time_oracle(sample, depth, 1, budget_s / 2, max_reps=3)
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
             "sample": f"full workload ({codes.size} fragments) x {reps} runs of CreateDAG+CreateFinalDAG, "
-                      f"{el:.1f} s, oracle threads={threads}"}
+                      f"{el:.1f} s, oracle threads={threads}",
+            "single_thread": {"value": v1, "unit": UNIT, "cores": 1,
+                              "sample": f"first {sample.size} fragments of the shuffled workload x {reps1} runs, "
+                                        f"{el1:.1f} s"}}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    import dag_compression_fast_gb300 as D
-    codes = D.gen_terrain(DEPTH, SEED)
-    from oracle import oracle as O
+    codes = soup_codes()
     threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    depth = SOUP["depth"]
     for _ in range(args.warmup):
-        O.final_dag(O.create_dag(codes, DEPTH, threads))
+        O.final_dag(O.create_dag(codes, depth, threads))
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.final_dag(O.create_dag(codes, DEPTH, threads))
+        O.final_dag(O.create_dag(codes, depth, threads))
     el = time.perf_counter() - t0
     value = codes.size * args.steps / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (seeded fBm terrain)",
-        "config": {"workload": WORKLOAD, "fragments": int(codes.size), "depth": DEPTH},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "data": "synthetic (seeded triangle soup, stands in for the voxelized scene)",
+        "config": bench_config(codes.size, world),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
                          "sample": f"full workload per step, {args.steps} steps, oracle threads={threads}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def group_roofline(prof, peak, peak_kind, n):
+    group_kernels = {
+        "group_sketch": ("group_probe + group_plan (sampled sketch, path choice)", "group_probe_terrain_d11.md"),
+        "group_scatter": ("group_scatter (fragments by partition: one read, one write)",
+                          "group_scatter_terrain_d11.md"),
+        "group_aggregate": ("group_aggregate (per-partition tables in shared memory: one read)",
+                            "group_aggregate_terrain_d11.md"),
+    }
+    top = max(group_kernels, key=lambda k: prof[k][0])
+    label, prof_file = group_kernels[top]
+    return stage_roofline(prof, top, label, peak, peak_kind, profile_figure(prof_file, "dram_bytes_per_fragment", n))
+
+
+def stage_table(prof, steps):
+    return {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps,
+                "gbs": round((v[2] / 1e9) / (v[0] / 1e3), 1) if v[0] > 0 and v[2] else None}
+            for k, v in prof.items() if v[1]}
 
 
 def main():
@@ -204,57 +283,69 @@ def main():
     import dag_compression_fast_gb300 as D
     torch.cuda.set_device(local)
     dev = f"cuda:{local}"
-    codes = D.gen_terrain(DEPTH, SEED)
+    depth = SOUP["depth"]
+    codes = soup_codes()
     n = int(codes.size)
     ctx = D.Context(local)
     d_codes = torch.from_numpy(codes.view(np.int64)).to(dev)
     stream = torch.cuda.current_stream()
-
-    def step():
-        dag = ctx.create_dag(d_codes, DEPTH)
-        words = ctx.create_final_dag(dag)
-        nw = words.n
-        words.free()
-        return nw
-
-    for _ in range(max(args.warmup, 3)):
-        n_words = step()
-    counts = ctx.last_counts()
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
+    def max_over_ranks(x: float) -> float:
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([x], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    def step_on(frags, dp):
+        dag = ctx.create_dag(frags, dp)
+        words = ctx.create_final_dag(dag)
+        nw = words.n
+        words.free()
+        return nw
+
+    for _ in range(max(args.warmup, 3)):
+        n_words = step_on(d_codes, depth)
+    counts = ctx.last_counts()
+
     # ---- timed region: device-resident fragments -> device-resident DAG ----
-    # (the production path: each call's kernel sequence replays as a CUDA graph)
+    # (the production path: each call's kernel sequence replays as a CUDA
+    # graph). The clock sampler runs through an untimed soak of steps right
+    # before the timed K steps and through them, so that it sees the clocks
+    # under this load even when K steps take only a fraction of a second.
     sampler = ClockSampler(local)
     sampler.start()
+    t_soak = time.perf_counter()
+    soak_steps = 0
+    while time.perf_counter() - t_soak < args.soak_seconds:
+        step_on(d_codes, depth)
+        soak_steps += 1
     launches0 = ctx.kernel_launches()
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        step()
+        step_on(d_codes, depth)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1))
     launches = ctx.kernel_launches() - launches0
     clocks = sampler.stop()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     value = n * args.steps * world / (ms / 1e3)
 
     # ---- the same steps with CUDA events around every stage and digit pass ----
     ctx.profile(True)
     ctx.profile_reset()
     for _ in range(args.steps):
-        step()
+        step_on(d_codes, depth)
     torch.cuda.synchronize()
     ctx.profile(False)
     prof = ctx.profile_read()
@@ -263,26 +354,20 @@ def main():
     h_codes = torch.from_numpy(codes.view(np.int64)).pin_memory()
     h_view = h_codes.numpy().view(np.uint64)
     h_words = torch.empty(n_words, dtype=torch.int32).pin_memory()
-    import ctypes
     lib = D.lib()
     sh = stream.cuda_stream
     nw = ctypes.c_uint64(0)
     for _ in range(2):
-        ctx._check(lib.dagc_compress_host(ctx.handle, h_view.ctypes.data, n, DEPTH, sh, h_words.data_ptr(),
+        ctx._check(lib.dagc_compress_host(ctx.handle, h_view.ctypes.data, n, depth, sh, h_words.data_ptr(),
                                           n_words, ctypes.byref(nw)))
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx._check(lib.dagc_compress_host(ctx.handle, h_view.ctypes.data, n, DEPTH, sh, h_words.data_ptr(),
+        ctx._check(lib.dagc_compress_host(ctx.handle, h_view.ctypes.data, n, depth, sh, h_words.data_ptr(),
                                           n_words, ctypes.byref(nw)))
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_sync = {"value": n * args.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 4 * int(nw.value),
                 "mode": "dagc_compress_host, one call per step, each waiting for the previous"}
@@ -290,25 +375,20 @@ def main():
     # ---- end to end through the serving API: the same steps as jobs of a
     # two-slot server (dagc_server_submit / dagc_server_wait). Every step still
     # copies its pinned host fragments in and its words out inside the timed
-    # region; a step's host->device copy overlaps the previous step's kernels,
-    # so the pace is the host link's (252 MB at ~211 GB/s). ----
+    # region; a step's host->device copy overlaps the previous step's kernels. ----
     sv = D.Server(local, slots=2, hbm_budget_bytes=256 << 30)
     for _ in range(max(args.warmup, 2)):
-        sv.wait(sv.submit(h_view, DEPTH))
+        sv.wait(sv.submit(h_view, depth))
     barrier()
     t0 = time.perf_counter()
-    tickets = [sv.submit(h_view, DEPTH) for _ in range(args.steps)]
+    tickets = [sv.submit(h_view, depth) for _ in range(args.steps)]
     pipe_words = 0
     for tk in tickets:
         w_out, _ = sv.wait(tk)
         pipe_words = len(w_out)
-    pipe_s = time.perf_counter() - t0
+    pipe_s = max_over_ranks(time.perf_counter() - t0)
     sv.close()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([pipe_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        pipe_s = float(t.item())
+    del h_codes, h_view, h_words
     if pipe_words != int(nw.value):
         raise RuntimeError("serving path returned a different word count")
     e2e = {"value": n * args.steps * world / pipe_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
@@ -317,64 +397,73 @@ def main():
                    "steps overlapped (wall clock over K steps)"}
 
     # ---- roofline of the dominant kernel of the path the device chose ----
-    # Fragments with many per brick are grouped by hash (partition scatter +
-    # per-partition tables); otherwise they are radix-sorted (the digit pass
-    # dominates).
+    # Fragments with few per brick are radix-sorted (the digit pass
+    # dominates); with many per brick they are grouped by hash.
     peak, peak_kind = measured_peaks()
-    pass_traffic = profile_figure("onesweep_pass_keys_20M_27bit.md", "dram_bytes_per_key_per_pass", n)
-    group_kernels = {
-        "group_sketch": ("group_probe + group_plan (sampled sketch, path choice)",
-                         "group_probe_terrain_d11.md"),
-        "group_scatter": ("group_scatter (fragments by partition: one read, one write)",
-                          "group_scatter_terrain_d11.md"),
-        "group_aggregate": ("group_aggregate (per-partition tables in shared memory: one read)",
-                            "group_aggregate_terrain_d11.md"),
-    }
-    top = max(group_kernels, key=lambda k: prof[k][0])
-    if prof[top][0] > prof["fragment_pass"][0]:
-        label, prof_file = group_kernels[top]
-        roofline = stage_roofline(prof, top, label, peak, peak_kind,
-                                  profile_figure(prof_file, "dram_bytes_per_fragment", n))
-        # The radix-sort path's digit pass on the same fragments, for reference
-        # (it serves inputs with few fragments per brick).
-        ctx.set_option(D.OPT_GROUP, 0)
-        ctx.profile(True)
-        ctx.profile_reset()
-        for _ in range(2):
-            step()
-        torch.cuda.synchronize()
-        ctx.profile(False)
-        ctx.set_option(D.OPT_GROUP, 1)
-        sort_prof = ctx.profile_read()
-        roofline_sort = stage_roofline(sort_prof, "fragment_pass", "onesweep_pass (fragment sort, 8-bit digit, "
-                                       "keys only; sort path forced)", peak, peak_kind, pass_traffic)
-    else:
-        roofline = stage_roofline(prof, "fragment_pass", "onesweep_pass (fragment sort, 8-bit digit, keys only)",
+    pass_traffic = profile_figure("onesweep_pass_keys_soup_d13.md", "dram_bytes_per_key_per_pass", n)
+    if prof["fragment_pass"][2] > 0:
+        roofline = stage_roofline(prof, "fragment_pass", "onesweep_pass (fragment sort digit pass, keys only)",
                                   peak, peak_kind, pass_traffic)
-        roofline_sort = None
-    stages = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
-                  "gbs": round((v[2] / 1e9) / (v[0] / 1e3), 1) if v[0] > 0 and v[2] else None}
-              for k, v in prof.items() if v[1]}
+    else:
+        roofline = group_roofline(prof, peak, peak_kind, n)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (seeded fBm terrain, stands in for the voxelized scene)",
-        "config": {"workload": WORKLOAD, "fragments": n, "depth": DEPTH, "bricks": counts[1], "leaves": counts[2], "words": int(n_words),
-                   "l2": L2_NOTE, "parallelism": f"replicas x{world}"},
+        "data": "synthetic (seeded triangle soup, stands in for the voxelized scene)",
+        "config": bench_config(n, world),
+        "counts": {"bricks": counts[1], "leaves": counts[2], "words": int(n_words),
+                   "nodes_per_level": counts[3:]},
         "e2e": e2e,
         "e2e_sync": e2e_sync,
         "roofline": roofline,
         "gpu_launches": int(launches),
-        "stages": stages,
+        "stages": stage_table(prof, args.steps),
+        "timed_region_s": ms / 1e3,
+        "soak": {"steps": soak_steps, "seconds": args.soak_seconds},
     }
-    if roofline_sort:
-        line["roofline_sort_pass"] = roofline_sort
     if clocks:
+        clocks["window"] = "untimed soak right before the timed region, then the timed region"
+        clocks["ms_per_step_x_sm_mhz"] = round(ms / args.steps * clocks["sm_mhz"], 1)
         line["clocks"] = clocks
+    del d_codes
+    torch.cuda.empty_cache()
+
+    # ---- second workload: the fBm terrain (grouping path) ----
+    if not args.no_terrain:
+        t_codes = terrain_codes()
+        tn = int(t_codes.size)
+        td = torch.from_numpy(t_codes.view(np.int64)).to(dev)
+        tdepth = TERRAIN["depth"]
+        for _ in range(max(args.warmup, 3)):
+            step_on(td, tdepth)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_on(td, tdepth)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tms = max_over_ranks(e0.elapsed_time(e1))
+        ctx.profile(True)
+        ctx.profile_reset()
+        for _ in range(args.steps):
+            step_on(td, tdepth)
+        torch.cuda.synchronize()
+        ctx.profile(False)
+        tprof = ctx.profile_read()
+        line["terrain_2048"] = {
+            "workload": TERRAIN["name"], "fragments": tn, "depth": tdepth, "seed": TERRAIN["seed"],
+            "value": tn * args.steps * world / (tms / 1e3), "unit": UNIT, "ms_per_step": tms / args.steps,
+            "roofline": group_roofline(tprof, peak, peak_kind, tn) if tprof["group_scatter"][2] > 0 else
+            stage_roofline(tprof, "fragment_pass", "onesweep_pass", peak, peak_kind, None),
+            "stages": stage_table(tprof, args.steps),
+        }
+        del td
+
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(codes, args.cpu_seconds)
+    ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -67,8 +67,12 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // allocation retried once (the OOM fallback of src/Memory.cpp:56-70).
 class DevicePool {
 public:
-    ~DevicePool() { trim(); }
+    ~DevicePool() {
+        trim();
+        for (cudaEvent_t e : spare_events_) cudaEventDestroy(e);
+    }
     cudaError_t alloc(void** p, size_t bytes) {
+        reclaim();
         bytes = align_up(std::max<size_t>(bytes, 1), 512);
         auto it = free_.lower_bound(bytes);
         if (it != free_.end() && it->first <= 2 * bytes + (4u << 20)) {
@@ -101,7 +105,53 @@ public:
         in_use_ -= it->second;
         live_.erase(it);
     }
+    // Returns a block once the work queued on `s` so far has completed (work
+    // that may still read it): an event is recorded on `s` and the block is
+    // handed out again only after the event has completed.
+    void release_after(void* p, cudaStream_t s) {
+        if (!p || live_.find(p) == live_.end()) return;
+        cudaEvent_t e = nullptr;
+        if (!spare_events_.empty()) {
+            e = spare_events_.back();
+            spare_events_.pop_back();
+        } else if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            e = nullptr;
+        }
+        if (!e || cudaEventRecord(e, s) != cudaSuccess) {
+            cudaGetLastError();
+            if (e) spare_events_.push_back(e);
+            cudaStreamSynchronize(s);
+            cudaGetLastError();
+            release(p);
+            return;
+        }
+        deferred_.push_back({p, e});
+    }
+    // Moves deferred blocks whose event has completed to the free cache.
+    void reclaim() {
+        for (size_t i = 0; i < deferred_.size();) {
+            const cudaError_t q = cudaEventQuery(deferred_[i].e);
+            if (q == cudaErrorNotReady) {
+                cudaGetLastError();
+                ++i;
+                continue;
+            }
+            if (q != cudaSuccess) cudaGetLastError();
+            release(deferred_[i].p);
+            spare_events_.push_back(deferred_[i].e);
+            deferred_[i] = deferred_.back();
+            deferred_.pop_back();
+        }
+    }
     void trim() {
+        for (const Deferred& d : deferred_) {
+            cudaEventSynchronize(d.e);
+            release(d.p);
+            spare_events_.push_back(d.e);
+        }
+        cudaGetLastError();
+        deferred_.clear();
         for (auto& kv : free_) cudaFree(kv.second);
         free_.clear();
         cached_ = 0;
@@ -111,8 +161,14 @@ public:
     size_t cached() const { return cached_; }
 
 private:
+    struct Deferred {
+        void* p;
+        cudaEvent_t e;
+    };
     std::multimap<size_t, void*> free_;
     std::unordered_map<void*, size_t> live_;
+    std::vector<Deferred> deferred_;
+    std::vector<cudaEvent_t> spare_events_;
     size_t in_use_ = 0, cached_ = 0, peak_ = 0;
 };
 
@@ -180,13 +236,14 @@ struct GraphKey {
     uint64_t n;
     int depth;
     void* arena;
-    uint32_t chunks;  // batched calls: number of chunks (0 otherwise)
-    bool dedup;       // hash-set dedup (else radix sort + unique) for the leaves and levels
-    void* table;      // the dedup table block
-    int group;        // fragment grouping mode
+    uint32_t chunks;   // batched calls: number of chunks (0 otherwise)
+    int chunk_depth;   // batched calls: chunk depth, which sets the composite key split (0 otherwise)
+    bool dedup;        // hash-set dedup (else radix sort + unique) for the leaves and levels
+    void* table;       // the dedup table block
+    int group;         // fragment grouping mode
     bool operator==(const GraphKey& o) const {
         return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks &&
-               dedup == o.dedup && table == o.table && group == o.group;
+               chunk_depth == o.chunk_depth && dedup == o.dedup && table == o.table && group == o.group;
     }
 };
 struct GraphEntry {
@@ -344,6 +401,14 @@ struct StageTimer {
 void set_pending_bytes(dagc_context ctx, int stage, uint64_t bytes) {
     for (PendingTiming& p : ctx->pending)
         if (p.stage == stage && p.bytes == 0) p.bytes = bytes;
+}
+
+// Sets the algorithmic bytes of every pending timing of `stage` (used for the
+// kernels of the path the device did not take: they ran and returned at once,
+// so they moved nothing).
+void override_pending_bytes(dagc_context ctx, int stage, uint64_t bytes) {
+    for (PendingTiming& p : ctx->pending)
+        if (p.stage == stage) p.bytes = bytes;
 }
 
 // Called after a stream synchronisation: folds the finished event pairs into
@@ -1049,7 +1114,8 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         if (cs.sv_next > cs.sv_end) return set_error(ctx, DAGC_ERR_CUDA, "look-back status regions miscounted");
     return DAGC_OK;
     };
-    int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u, use_dedup,
+    int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u,
+                                       batch ? batch->chunk_depth : 0, use_dedup,
                                        use_dedup ? ctx->table : nullptr, use_dedup ? group_mode : 0},
                          s, enqueue);
     if (st) { ctx->table_dirty = true; return st; }
@@ -1085,6 +1151,20 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             lb += 20 * child + 293 * counts[kCntNodes + l] + 41 * counts[kCntUnique + l];
         }
         set_pending_bytes(ctx, DAGC_STAGE_LEVELS, lb);
+        // The kernels of the path the device did not take returned at once.
+        if (group_mode != 0 && use_dedup && ctx->gtable) {
+            uint32_t path = 0;
+            DAGC_CUDA(ctx, cudaMemcpy(&path, &hdr->path[0], 4, cudaMemcpyDeviceToHost));
+            if (path == 1) {
+                override_pending_bytes(ctx, DAGC_STAGE_FRAGMENT_HIST, 0);
+                override_pending_bytes(ctx, DAGC_STAGE_FRAGMENT_PASS, 0);
+                override_pending_bytes(ctx, DAGC_STAGE_LEAF_BUILD, 0);
+            } else {
+                override_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, 0);
+                override_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, 0);
+                override_pending_bytes(ctx, DAGC_STAGE_GROUP, 0);
+            }
+        }
         settle_profile(ctx);
     }
     if (e32) ctx->table_dirty = true;  // a level may have stopped before clearing its slots
@@ -1834,10 +1914,13 @@ int dagc_final(dagc_context ctx, dagc_dag dag, void* stream, uint32_t** d_words,
 }
 
 int dagc_free_words(dagc_context ctx, uint32_t* d_words, void* stream) {
-    (void)stream;
     if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lock(ctx->mu);
-    ctx->pool.release(d_words);
+    if (!d_words) return DAGC_OK;
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    // Work already queued on `stream` (a copy of the words, a kernel reading
+    // them) finishes before the block can be handed out again.
+    ctx->pool.release_after(d_words, static_cast<cudaStream_t>(stream));
     return DAGC_OK;
 }
 

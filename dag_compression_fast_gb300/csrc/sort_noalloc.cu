@@ -16,7 +16,9 @@
 //     library, for the lifetime of the process;
 //   * the first call on a device resolves the array's device address
 //     (cudaGetSymbolAddress) and configures the kernels; make that first call
-//     outside any stream capture;
+//     before any stream capture;
+//   * every call reads its error word back and synchronises its stream
+//     before it returns;
 //   * all calls share the one array: calls whose work overlaps on the GPU
 //     (different streams, or host threads without ordering) race and give
 //     wrong results. Each call clears the parts that must start at zero.
@@ -24,6 +26,7 @@
 #include "../../include/dagc.h"
 #include "dagc_device.cuh"
 #include "dagc_kernels.h"
+#include "dagc_launch.h"
 
 #include <cstddef>
 #include <mutex>
@@ -101,6 +104,9 @@ extern "C" int dagc_sort_keys_noalloc(const uint64_t* d_in, uint64_t* d_out, uin
     int st = setup_current_device(&dev);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Plain stream order for these launches, whatever a context call made
+    // earlier on this thread asked for.
+    t_pdl = false;
     char* base = static_cast<char*>(dev.scratch);
     NoAllocScratch* S = reinterpret_cast<NoAllocScratch*>(base);  // device address: offsets only on the host
     if (cudaMemsetAsync(base, 0, offsetof(NoAllocScratch, status), s) != cudaSuccess) {

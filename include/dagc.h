@@ -119,6 +119,10 @@ int dagc_merge(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_
  * released with dagc_free_words. An empty DAG gives 0 words and NULL. */
 int dagc_final(dagc_context ctx, dagc_dag dag, void* stream, uint32_t** d_words,
                uint64_t* n_words);
+/* Returns a word array to the context's pool. Work already queued on `stream`
+ * that reads the words (a copy out, a tracer launch) completes before the
+ * memory is handed out again: an event recorded on `stream` guards it. Work on
+ * other streams must be ordered before this call by the caller. */
 int dagc_free_words(dagc_context ctx, uint32_t* d_words, void* stream);
 /* Copies n words of a final DAG to host memory (synchronous). */
 int dagc_words_download(dagc_context ctx, const uint32_t* d_words, uint64_t n, uint32_t* h_words);
@@ -328,9 +332,10 @@ void dagc_server_destroy(dagc_server server);
  * fixed ~9.1 MB device array inside the library, present on every GPU that
  * loads it until the process exits. n <= 1048576 keys (else
  * DAGC_ERR_TOO_LARGE, nothing touched); d_in is left intact; no context. The
- * first call on a device sets the array up: make it before any stream
- * capture. Calls share the array, so calls whose GPU work overlaps race.
- * Synchronous on return; returns a dagc status. */
+ * first call on a device sets the array up: make that first call before any
+ * stream capture. Calls share the array, so calls whose GPU work overlaps
+ * race. Every call reads its error word back from the device and
+ * synchronises `stream` before it returns; returns a dagc status. */
 int dagc_sort_keys_noalloc(const uint64_t* d_in, uint64_t* d_out, uint64_t n, int lo_bit,
                            int hi_bit, void* stream);
 

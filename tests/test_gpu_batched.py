@@ -82,3 +82,24 @@ def test_batched_rejects_unordered_chunks(ctx):
     with pytest.raises(D.DagcError) as e:
         ctx.create_dag_batched(np.array([1, 2], np.uint64), [1, 1], [5, 3], 5, 1)
     assert e.value.status == D.ERR_INVALID_ARGUMENT
+
+
+def test_batched_graph_key_includes_chunk_split(ctx):
+    """Two batched calls on one fragment buffer with the same fragment count,
+    chunk count and total depth but a different chunk/top split: a call shape
+    is recorded as a CUDA graph on its second call and replayed after that, so
+    each split is called three times in turn; every result must equal the
+    oracle's for its own split."""
+    import torch
+    k = 8
+    rng = np.random.default_rng(21)
+    local = rng.integers(0, 8 ** 5, 4000, dtype=np.uint64)  # valid for chunk depth 5 and 6
+    counts = np.full(k, local.size // k, np.uint64)
+    d_frag = torch.from_numpy(local.view(np.int64)).cuda()
+    chunks = np.split(local, k)
+    splits = [(5, 2, np.arange(0, 64, 8, dtype=np.uint64)), (6, 1, np.arange(8, dtype=np.uint64))]
+    expect = {cd: O.create_dag(global_codes(chunks, morton, cd), cd + top) for cd, top, morton in splits}
+    for _ in range(3):
+        for cd, top, morton in splits:
+            got = ctx.create_dag_batched(d_frag, counts, morton, cd, top).to_host()
+            assert_dag_equal(got, expect[cd])

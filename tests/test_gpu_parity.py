@@ -340,3 +340,30 @@ def test_terrain_2048_full_size_bit_exact(ctx):
     w = ctx.create_final_dag(dag).to_numpy()
     assert np.array_equal(w, O.final_dag(ref))
     assert np.array_equal(decode_final(w, 11), np.unique(codes))
+
+
+@pytest.fixture(scope="module")
+def soup_8192():
+    """The triangle-soup workload at full size: 2M triangles in an 8192^3 grid
+    (depth 13), ~65M shuffled fragments, and the multi-threaded oracle's DAG."""
+    codes = D.gen_triangle_soup(13, 0xDA6C0DE + 3, 2_000_000)
+    assert codes.size > 60_000_000
+    ref = O.create_dag(codes, 13, threads=16)
+    return codes, ref, O.final_dag(ref)
+
+
+@pytest.mark.parametrize("group", [1, 2, 0])
+def test_soup_8192_full_size_bit_exact(soup_8192, group):
+    """Triangle soup, 8192^3, ~65M fragments (low redundancy: the device's
+    own choice is the sort path), bit-exact against the oracle on the
+    device-chosen path (1), with fragment grouping forced (2) and with the
+    sort path forced (0); decoded back to the input voxel set."""
+    codes, ref, ref_words = soup_8192
+    with D.Context(0) as c:
+        c.set_option(D.OPT_GROUP, group)
+        dag = c.create_dag(codes, 13)
+        assert_dag_equal(dag.to_host(), ref)
+        w = c.create_final_dag(dag).to_numpy()
+    assert np.array_equal(w, ref_words)
+    if group == 1:
+        assert np.array_equal(decode_final(w, 13), np.unique(codes))

@@ -8,10 +8,11 @@ device synchronisation. dagc_sort_keys_noalloc serves them with a fixed
 scratch array compiled into the library.
 
 The test calls it through the C ABI twice in a row (the second call reuses the
-scratch the first one left behind) and checks each result against the
-allocating entry point dagc_sort_keys, bit for bit. It also checks that a
-request above the fixed limit is refused before any memory is touched. This
-file is collected last so that a failure here comes after every other test.
+scratch the first one left behind) and checks each result bit for bit against
+numpy's stable sort on the same bit range and against the allocating entry
+point dagc_sort_keys. It also checks that a request above the fixed limit is
+refused before any memory is touched. This file is collected last so that a
+failure here comes after every other test.
 """
 import ctypes
 
@@ -23,6 +24,15 @@ import dag_compression_fast_gb300 as D
 pytestmark = pytest.mark.gpu
 
 MAX_KEYS = 1 << 20
+
+
+def stable_sorted(keys: np.ndarray, lo: int, hi: int) -> np.ndarray:
+    """Keys in the order of a stable sort on bits [lo, hi)."""
+    u = keys.view(np.uint64)
+    digit = u >> np.uint64(lo)
+    if hi - lo < 64:
+        digit = digit & np.uint64((1 << (hi - lo)) - 1)
+    return keys[np.argsort(digit, kind="stable")]
 
 
 def test_noalloc_sort_matches_allocating_sort_twice():
@@ -43,6 +53,7 @@ def test_noalloc_sort_matches_allocating_sort_twice():
         st = lib.dagc_sort_keys_noalloc(keys.data_ptr(), out.data_ptr(), n, lo, hi, stream)
         assert st == D.OK, lib.dagc_status_string(st)
         torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), stable_sorted(keys_np, lo, hi))
         assert torch.equal(out, expected)
         assert torch.equal(keys, torch.from_numpy(keys_np).cuda())  # input left intact
     ctx.close()
