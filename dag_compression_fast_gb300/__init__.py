@@ -34,9 +34,13 @@ OPT_DEDUP = 4
 OPT_DEDUP_UNIQUE_LIMIT = 5
 OPT_GROUP = 6
 OPT_PDL = 7
+OPT_SORT_RADIX_BITS = 8
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
-NUM_SORT_SHAPES = 8
+NUM_KEY_SHAPES = 6
+NUM_PAIR_SHAPES = 8
+NUM_SORT_SHAPES = NUM_PAIR_SHAPES
+RADIX_BITS = (8, 9, 10, 11)
 
 OK = 0
 ERR_INVALID_ARGUMENT = 1
@@ -59,6 +63,7 @@ DAGC_SYMBOLS = [
     "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
     "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_voxelize", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
+    "dagc_tune_sort", "dagc_tune_save", "dagc_tune_load", "dagc_tune_clear", "dagc_sort_plan",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
 ]
@@ -151,6 +156,13 @@ def lib() -> ctypes.CDLL:
         L.dagc_sort_keys.argtypes = [vp, vp, vp, u64, i32, i32, vp]
         L.dagc_sort_pairs.argtypes = [vp, vp, vp, vp, vp, u64, i32, i32, vp]
         L.dagc_sort_keys_noalloc.argtypes = [vp, vp, u64, i32, i32, vp]
+        pi32 = ctypes.POINTER(i32)
+        pdbl = ctypes.POINTER(ctypes.c_double)
+        L.dagc_tune_sort.argtypes = [vp, u64, i32, i32, i32, i32, pi32, pi32, pdbl, pdbl]
+        L.dagc_tune_save.argtypes = [vp, ctypes.c_char_p]
+        L.dagc_tune_load.argtypes = [vp, ctypes.c_char_p]
+        L.dagc_tune_clear.argtypes = [vp]
+        L.dagc_sort_plan.argtypes = [vp, u64, i32, i32, i32, pi32, pi32]
         _lib = L
     return _lib
 
@@ -559,6 +571,33 @@ class Context:
         out = torch.empty_like(t)
         self._check(lib().dagc_sort_keys(self.handle, ptr, out.data_ptr(), n, lo_bit, hi_bit, _stream_handle(stream)))
         return out
+
+    # ------------------------------------------------------- autotuner ----
+    def tune_sort(self, n: int, lo_bit: int, hi_bit: int, with_values: bool = False, reps: int = 5):
+        """Times every valid digit-pass plan of one sort class on the device
+        and keeps the fastest in the context's tuning table (dagc_tune_sort).
+        Returns {"shape", "radix_bits", "ms", "default_ms"}."""
+        sh, rb = ctypes.c_int(0), ctypes.c_int(0)
+        ms, dms = ctypes.c_double(0), ctypes.c_double(0)
+        self._check(lib().dagc_tune_sort(self.handle, n, lo_bit, hi_bit, int(with_values), reps, ctypes.byref(sh),
+                                         ctypes.byref(rb), ctypes.byref(ms), ctypes.byref(dms)))
+        return {"shape": sh.value, "radix_bits": rb.value, "ms": ms.value, "default_ms": dms.value}
+
+    def sort_plan(self, n: int, lo_bit: int, hi_bit: int, with_values: bool = False):
+        """(shape, radix_bits) a sort of this class would take."""
+        sh, rb = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(lib().dagc_sort_plan(self.handle, n, lo_bit, hi_bit, int(with_values), ctypes.byref(sh),
+                                         ctypes.byref(rb)))
+        return sh.value, rb.value
+
+    def tune_save(self, path: str):
+        self._check(lib().dagc_tune_save(self.handle, os.fsencode(path)))
+
+    def tune_load(self, path: str):
+        self._check(lib().dagc_tune_load(self.handle, os.fsencode(path)))
+
+    def tune_clear(self):
+        self._check(lib().dagc_tune_clear(self.handle))
 
     def sort_pairs(self, keys, values=None, lo_bit: int = 0, hi_bit: int = 64, stream=None):
         import torch

@@ -88,7 +88,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             if o.strip():
                 print(o)
     if force or jobs or not os.path.exists(LIBDAGC):
-        _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIBDAGC] + objs)
+        _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIBDAGC] + objs + ["-ldl"])
     gen_srcs = [os.path.join(CSRC, f) for f in GEN_SOURCES]
     if force or not _newer(LIBGEN, gen_srcs + headers):
         _run([CXX] + CXX_FLAGS + ["-shared", "-o", LIBGEN] + gen_srcs)

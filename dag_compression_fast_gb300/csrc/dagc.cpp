@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <dlfcn.h>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -51,7 +52,7 @@ struct CallHeader {
     uint32_t pad;
     uint64_t counts[64];
     uint32_t tile_counters[kMaxTileCounters];
-    uint32_t hist[kMaxSorts][kMaxPasses * 256];
+    uint32_t hist[kMaxSorts][kSortHistWords];
     DedupState dedup[kMaxDepth + 1];  // leaves + one per level
     uint32_t sketch[kGroupSketchRegs];  // distinct-brick sketch of the fragment grouping's probe
     uint32_t gover[kGroupMaxParts];     // its partitions that spilled past their slabs
@@ -229,6 +230,20 @@ struct PendingTiming {
     uint64_t bytes;
 };
 
+// A digit-pass plan: kernel shape and widest digit.
+struct SortChoice {
+    int shape;
+    int radix_bits;
+};
+// Class of a sort for the tuning table: keys-only or pairs, number of sorted
+// bits, and the key count's power of two (counts within a factor of two
+// share a plan).
+inline uint32_t sort_class(bool with_values, int bits, uint64_t n) {
+    int lg = 0;
+    while (lg < 40 && (1ull << (lg + 1)) <= n) ++lg;
+    return (with_values ? 1u << 24 : 0u) | (uint32_t)bits << 8 | (uint32_t)lg;
+}
+
 // A recorded CreateDAG pipeline: valid for one input pointer, size, depth,
 // arena block and pass shapes.
 struct GraphKey {
@@ -248,7 +263,7 @@ struct GraphKey {
 };
 struct GraphEntry {
     GraphKey key;
-    int shape_keys, shape_pairs;
+    uint32_t tune_version;
     cudaGraphExec_t exec;
     uint64_t launches;
 };
@@ -260,8 +275,17 @@ struct dagc_context_t {
     cudaStream_t capture_stream = nullptr;
     std::vector<GraphEntry> graphs;
     std::vector<GraphKey> graph_seen;  // call shapes launched directly once; recorded when seen again
-    int shape_keys = 5, shape_pairs = 3;  // digit-pass shapes (see dagc_set_option), tuned on GB300
-    int occ_keys[kNumSortShapes] = {}, occ_pairs[kNumSortShapes] = {};
+    // Digit-pass plans. A forced shape / width (dagc_set_option, >= 0)
+    // applies to every sort of its kind; otherwise the tuning table picks per
+    // sort class (SortClass), falling back to the defaults.
+    int shape_keys = -1, shape_pairs = -1, radix_keys = -1;
+    std::map<uint32_t, SortChoice> tune;  // sort_class key -> measured best plan
+    std::map<uint32_t, std::pair<double, double>> tune_ms;  // its time and the default plan's (ms)
+    const SortChoice* plan_override = nullptr;  // the autotuner's candidate while it is timed
+    uint32_t* sort_err = nullptr;               // error word of the last standalone sort
+    std::string tune_file;                      // the file the table was loaded from at creation
+    uint32_t tune_version = 0;            // bumped on every change of the table or a forced plan
+    int occ_keys[kNumKeyShapes][kMaxRadixBits - kRadixBits + 1] = {}, occ_pairs[kNumPairShapes] = {};
     StageStats stages[DAGC_NUM_STAGES];
     std::vector<cudaEvent_t> free_events;
     std::vector<PendingTiming> pending;
@@ -476,6 +500,27 @@ struct SegmentSpec {
     int shift;
 };
 
+// Default plans, measured on GB300: keys-only sorts take 16 keys per thread,
+// 3 CTAs per SM, alternating matchers; key/value sorts 8 items, 4 CTAs, ballots.
+constexpr SortChoice kDefaultKeys{0, kRadixBits};
+constexpr SortChoice kDefaultPairs{3, kRadixBits};
+
+// The plan of one sort: forced options first, then the tuning table, then
+// the defaults; a plan that cannot take the bit range falls back to 8-bit
+// digits.
+SortChoice sort_plan_for(dagc_context ctx, bool with_values, int lo, int hi, uint64_t n) {
+    if (ctx->plan_override) return *ctx->plan_override;
+    SortChoice c = with_values ? kDefaultPairs : kDefaultKeys;
+    auto it = ctx->tune.find(sort_class(with_values, hi - lo, n));
+    if (it != ctx->tune.end()) c = it->second;
+    const int forced_shape = with_values ? ctx->shape_pairs : ctx->shape_keys;
+    if (forced_shape >= 0) c.shape = forced_shape;
+    if (!with_values && ctx->radix_keys >= 0) c.radix_bits = ctx->radix_keys;
+    if (!sort_plan_valid(c.shape, with_values, c.radix_bits, lo, hi)) c.radix_bits = kRadixBits;
+    if (!sort_plan_valid(c.shape, with_values, c.radix_bits, lo, hi)) c = with_values ? kDefaultPairs : kDefaultKeys;
+    return c;
+}
+
 // pass_stage >= 0: time the histogram under hist_stage and every digit pass
 // separately under pass_stage (host-known n only, for the byte counts).
 int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint64_t* keys_in,
@@ -506,7 +551,9 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     a.err = &cs.h->err;
     const uint64_t tiles = sort_tiles(n_bound);
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
-    a.shape = with_values ? ctx->shape_pairs : ctx->shape_keys;
+    const SortChoice plan = sort_plan_for(ctx, with_values, lo, hi, n_bound);
+    a.shape = plan.shape;
+    a.radix_bits = plan.radix_bits;
     a.gate = gate;
     a.gate_run = gate_run;
     if (seg && seg->d_offsets) {
@@ -514,10 +561,13 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
         a.seg_count = seg->count;
         a.seg_shift = seg->shift;
     }
-    const int occ = with_values ? ctx->occ_pairs[a.shape] : ctx->occ_keys[a.shape];
-    const uint64_t shape_tiles = (n_bound + 256ull * sort_shape_items(a.shape) - 1) / (256ull * sort_shape_items(a.shape));
+    // Grid: resident CTAs of the widest pass kernel (the narrower ones of
+    // the same shape fit at least as many).
+    const int occ = with_values ? ctx->occ_pairs[a.shape] : ctx->occ_keys[a.shape][a.radix_bits - kRadixBits];
+    const uint64_t tile = 256ull * sort_shape_items(a.shape, with_values);
+    const uint64_t shape_tiles = (n_bound + tile - 1) / tile;
     a.grid_pass = grid_for(occ, ctx->sms, std::min<uint64_t>(tiles, shape_tiles));
-    const int passes = sort_passes(lo, hi);
+    const int passes = sort_plan_passes(a);
     const uint64_t kv = with_values ? 12 : 8;
     {
         StageTimer t(ctx, hist_stage, s);
@@ -597,7 +647,7 @@ template <typename F>
 int run_enqueue(dagc_context ctx, const GraphKey& key, cudaStream_t s, F&& enqueue) {
     if (!ctx->use_graphs || ctx->profiling || !ctx->capture_stream) return enqueue(s);
     for (GraphEntry& g : ctx->graphs) {
-        if (g.key == key && g.shape_keys == ctx->shape_keys && g.shape_pairs == ctx->shape_pairs) {
+        if (g.key == key && g.tune_version == ctx->tune_version) {
             DAGC_CUDA(ctx, cudaGraphLaunch(g.exec, s));
             ctx->launches += g.launches;
             return DAGC_OK;
@@ -653,7 +703,7 @@ int run_enqueue(dagc_context ctx, const GraphKey& key, cudaStream_t s, F&& enque
         cudaGraphExecDestroy(ctx->graphs.front().exec);
         ctx->graphs.erase(ctx->graphs.begin());
     }
-    ctx->graphs.push_back({key, ctx->shape_keys, ctx->shape_pairs, exec, recorded});
+    ctx->graphs.push_back({key, ctx->tune_version, exec, recorded});
     DAGC_CUDA(ctx, cudaGraphLaunch(exec, s));
     ctx->launches += recorded;
     return DAGC_OK;
@@ -714,8 +764,8 @@ struct CreateLayout {
         o_hdr = L.take<CallHeader>(1);
         o_sv = L.take<uint64_t>(sv_total);
         zero_bytes = L.off;
-        o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
-        o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
+        o_ss0 = L.take<uint32_t>(sort_status_words(n));
+        o_ss1 = L.take<uint32_t>(sort_status_words(n));
         o_A = L.take<uint64_t>(n);
         o_B = L.take<uint64_t>(n);
         if (grouping) {
@@ -788,6 +838,8 @@ int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
     if (!ctx->gtable && ctx->group_mode != 0) DAGC_CUDA(ctx, cudaMalloc(&ctx->gtable, kGroupScratchBytes));
     return DAGC_OK;
 }
+
+int load_tune_file(dagc_context ctx, const char* path);
 
 // Internal status: the hash-set dedup could not hold this input; the caller
 // reruns the call with the radix form.
@@ -1019,6 +1071,11 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         int tail_first = -1;
         while (tail_first + 1 < nl && tail_first + 1 < kMaxTailLevels && cap[tail_first + 1] <= (uint64_t)kTailCap)
             ++tail_first;
+        // The tail's first level reads all of its children in one CTA: a level
+        // that may have many (8^5 bound at depth >= 8 with dense top levels)
+        // goes to the multi-CTA path instead.
+        while (tail_first >= 0 && (tail_first + 1 < nl ? cap[tail_first + 1] : p0cap) > (uint64_t)kTailChildCap)
+            --tail_first;
         for (int l = nl - 1, it = 0; l > tail_first; --l, ++it) {
             ExtractArgs e{};
             e.child_codes = child_codes;
@@ -1353,8 +1410,8 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
     for (int l = 0; l < nl; ++l) sv_total += sv_words(level_total[l]);
     const size_t o_sv = L.take<uint64_t>(sv_total);
     const size_t zero_bytes = L.off;
-    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(capmax) * 256);
-    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(capmax) * 256);
+    const size_t o_ss0 = L.take<uint32_t>(sort_status_words(capmax));
+    const size_t o_ss1 = L.take<uint32_t>(sort_status_words(capmax));
     const size_t o_KC = L.take<uint64_t>(capmax);
     const size_t o_MC = L.take<uint8_t>(capmax);
     const size_t o_CC = L.take<uint32_t>(capmax * 8);
@@ -1620,20 +1677,36 @@ int dagc_context_create(int device, dagc_context* out) {
     if (const char* gm = std::getenv("DAGC_GROUP")) c->group_mode = std::min(2, std::max(0, std::atoi(gm)));
     if (const char* pd = std::getenv("DAGC_PDL")) c->pdl = std::atoi(pd) != 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
-    for (int sh = 0; sh < kNumSortShapes; ++sh) {
-        c->occ_keys[sh] = std::max(1, occupancy_sort_shape(sh, false));
-        c->occ_pairs[sh] = std::max(1, occupancy_sort_shape(sh, true));
+    for (int sh = 0; sh < kNumKeyShapes; ++sh)
+        for (int b = kRadixBits; b <= kMaxRadixBits; ++b)
+            c->occ_keys[sh][b - kRadixBits] = std::max(1, occupancy_sort_shape(sh, false, b));
+    for (int sh = 0; sh < kNumPairShapes; ++sh) c->occ_pairs[sh] = std::max(1, occupancy_sort_shape(sh, true));
+    if (const char* e = std::getenv("DAGC_SORT_SHAPE_KEYS")) c->shape_keys = std::atoi(e) % kNumKeyShapes;
+    if (const char* e = std::getenv("DAGC_SORT_SHAPE_PAIRS")) c->shape_pairs = std::atoi(e) % kNumPairShapes;
+    if (const char* e = std::getenv("DAGC_SORT_RADIX_BITS")) {
+        const int r = std::atoi(e);
+        if (r >= kRadixBits && r <= kMaxRadixBits) c->radix_keys = r;
     }
-    // Resident-CTA caps for the persistent grids (tuning experiments).
-    if (const char* e = std::getenv("DAGC_PASS_CTAS_PER_SM")) {
-        const int cap = std::max(1, std::atoi(e));
-        for (int sh = 0; sh < kNumSortShapes; ++sh) {
-            c->occ_keys[sh] = std::min(c->occ_keys[sh], cap);
-            c->occ_pairs[sh] = std::min(c->occ_pairs[sh], cap);
+    // The tuning table: the file DAGC_TUNE_FILE names (empty: none), else
+    // sort_plans.json of the package (one directory above this library); a
+    // missing file leaves the defaults.
+    std::string tune_path;
+    if (const char* t = std::getenv("DAGC_TUNE_FILE")) {
+        tune_path = t;
+    } else {
+        Dl_info info{};
+        if (dladdr(reinterpret_cast<void*>(&dagc_context_create), &info) && info.dli_fname) {
+            const std::string lib = info.dli_fname;
+            const size_t slash = lib.rfind('/');
+            if (slash != std::string::npos) tune_path = lib.substr(0, slash) + "/../sort_plans.json";
         }
     }
-    if (const char* e = std::getenv("DAGC_SORT_SHAPE_KEYS")) c->shape_keys = std::atoi(e) % kNumSortShapes;
-    if (const char* e = std::getenv("DAGC_SORT_SHAPE_PAIRS")) c->shape_pairs = std::atoi(e) % kNumSortShapes;
+    if (!tune_path.empty()) {
+        if (FILE* f = std::fopen(tune_path.c_str(), "r")) {
+            std::fclose(f);
+            if (load_tune_file(c.get(), tune_path.c_str()) == DAGC_OK) c->tune_file = tune_path;
+        }
+    }
     c->grid_hist = 8 * c->sms;
     c->grid_leaf = std::max(1, occupancy_kernel(0)) * c->sms;
     if (const char* e = std::getenv("DAGC_SCAN_CTAS_PER_SM"))
@@ -1997,12 +2070,20 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
     std::lock_guard<std::mutex> lock(ctx->mu);
     switch (option) {
         case DAGC_OPT_SORT_SHAPE_KEYS:
-            if (value < 0 || value >= kNumSortShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
+            if (value < -1 || value >= kNumKeyShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
             ctx->shape_keys = value;
+            ++ctx->tune_version;
             return DAGC_OK;
         case DAGC_OPT_SORT_SHAPE_PAIRS:
-            if (value < 0 || value >= kNumSortShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
+            if (value < -1 || value >= kNumPairShapes) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad shape");
             ctx->shape_pairs = value;
+            ++ctx->tune_version;
+            return DAGC_OK;
+        case DAGC_OPT_SORT_RADIX_BITS:
+            if (value != -1 && (value < kRadixBits || value > kMaxRadixBits))
+                return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "digit width must be -1 or 8..11");
+            ctx->radix_keys = value;
+            ++ctx->tune_version;
             return DAGC_OK;
         case DAGC_OPT_GRAPHS:
             ctx->use_graphs = value != 0;
@@ -2211,6 +2292,117 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap) {
     return k;
 }
 
+}  // extern "C"
+
+namespace {
+
+// One standalone sort enqueued on `s` through the context's arena (no wait).
+int enqueue_sort(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out, const uint32_t* d_vals_in,
+                 uint32_t* d_vals_out, uint64_t n, int lo, int hi, cudaStream_t s) {
+    const bool with_values = d_vals_out != nullptr;
+    Layout L;
+    const size_t o_hdr = L.take<CallHeader>(1);
+    const size_t zero_bytes = L.off;
+    const size_t o_ss0 = L.take<uint32_t>(sort_status_words(n));
+    const size_t o_ss1 = L.take<uint32_t>(sort_status_words(n));
+    const size_t o_ka = L.take<uint64_t>(n);
+    const size_t o_va = L.take<uint32_t>(with_values ? n : 0);
+    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
+    arena_wait(ctx, s);
+    char* b = static_cast<char*>(ctx->arena.base);
+    CallSlots cs;
+    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
+    SortBuffers sb{{reinterpret_cast<uint32_t*>(b + o_ss0), reinterpret_cast<uint32_t*>(b + o_ss1)}};
+    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
+    ctx->sort_err = &cs.h->err;
+    return run_sort(ctx, cs, sb, d_keys_in, d_keys_out, reinterpret_cast<uint64_t*>(b + o_ka), d_vals_in, d_vals_out,
+                    with_values ? reinterpret_cast<uint32_t*>(b + o_va) : nullptr, with_values, n, nullptr, lo, hi, 0,
+                    s);
+}
+
+// Waits for the sorts enqueued on `s` and maps their error word to a status.
+int finish_sort(dagc_context ctx, cudaStream_t s) {
+    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, ctx->sort_err, 8, cudaMemcpyDeviceToHost, s));
+    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
+    std::string msg;
+    const int st = device_error_status((uint32_t)ctx->h_stage[0], msg);
+    return st ? set_error(ctx, st, msg) : DAGC_OK;
+}
+
+// Tuning table file: JSON, one object per sort class.
+int save_tune_file(dagc_context ctx, const char* path) {
+    FILE* f = std::fopen(path, "w");
+    if (!f) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, ctx->device);
+    cudaGetLastError();
+    std::fprintf(f, "{\n  \"format\": \"dagc digit-pass plans\",\n  \"version\": 1,\n  \"device\": \"%s\",\n"
+                    "  \"sm\": %d,\n  \"entries\": [",
+                 prop.name, prop.major * 10 + prop.minor);
+    bool first = true;
+    for (const auto& kv : ctx->tune) {
+        const uint32_t cls = kv.first;
+        auto m = ctx->tune_ms.find(cls);
+        const double ms = m == ctx->tune_ms.end() ? 0.0 : m->second.first;
+        const double dms = m == ctx->tune_ms.end() ? 0.0 : m->second.second;
+        std::fprintf(f,
+                     "%s\n    {\"values\": %u, \"bits\": %u, \"log2n\": %u, \"shape\": %d, \"radix_bits\": %d, "
+                     "\"ms\": %.6f, \"default_ms\": %.6f}",
+                     first ? "" : ",", cls >> 24, (cls >> 8) & 0xFFu, cls & 0xFFu, kv.second.shape,
+                     kv.second.radix_bits, ms, dms);
+        first = false;
+    }
+    std::fprintf(f, "\n  ]\n}\n");
+    const bool ok = std::fclose(f) == 0;
+    return ok ? DAGC_OK : set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+}
+
+// Number after `"key":` inside [b, e), or `fallback`.
+double json_number(const char* b, const char* e, const char* key, double fallback) {
+    const std::string pat = std::string("\"") + key + "\":";
+    const char* p = std::search(b, e, pat.begin(), pat.end());
+    if (p == e) return fallback;
+    return std::strtod(p + pat.size(), nullptr);
+}
+
+int load_tune_file(dagc_context ctx, const char* path) {
+    FILE* f = std::fopen(path, "r");
+    if (!f) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+    std::string text;
+    char buf[4096];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
+    std::fclose(f);
+    const size_t ent = text.find("\"entries\"");
+    if (ent == std::string::npos) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "no entries in tuning file");
+    std::map<uint32_t, SortChoice> table;
+    std::map<uint32_t, std::pair<double, double>> times;
+    size_t pos = ent;
+    while ((pos = text.find('{', pos)) != std::string::npos) {
+        const size_t close = text.find('}', pos);
+        if (close == std::string::npos) break;
+        const char* b = text.data() + pos;
+        const char* e = text.data() + close;
+        const int values = (int)json_number(b, e, "values", -1), bits = (int)json_number(b, e, "bits", -1);
+        const int lg = (int)json_number(b, e, "log2n", -1), shape = (int)json_number(b, e, "shape", -1);
+        const int rb = (int)json_number(b, e, "radix_bits", -1);
+        pos = close + 1;
+        if (values < 0 || values > 1 || bits < 1 || bits > 64 || lg < 0 || lg > 40) continue;
+        if (!sort_plan_valid(shape, values != 0, rb, 0, bits)) continue;  // not a plan of this build: skipped
+        const uint32_t cls = (values ? 1u << 24 : 0u) | (uint32_t)bits << 8 | (uint32_t)lg;
+        table[cls] = SortChoice{shape, rb};
+        times[cls] = {json_number(b, e, "ms", 0), json_number(b, e, "default_ms", 0)};
+    }
+    ctx->tune.swap(table);
+    ctx->tune_ms.swap(times);
+    ++ctx->tune_version;
+    return DAGC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint64_t n, int lo, int hi, void* stream) {
     return dagc_sort_pairs(ctx, d_in, d_out, nullptr, nullptr, n, lo, hi, stream);
 }
@@ -2221,32 +2413,121 @@ int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_key
     if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 keys");
     if (n == 0) return DAGC_OK;
     if (!d_keys_in || !d_keys_out || d_keys_in == d_keys_out) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad key buffers");
-    const bool with_values = d_vals_out != nullptr;
     std::lock_guard<std::mutex> lock(ctx->mu);
     DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    Layout L;
-    const size_t o_hdr = L.take<CallHeader>(1);
-    const size_t zero_bytes = L.off;
-    const size_t o_ss0 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
-    const size_t o_ss1 = L.take<uint32_t>((uint64_t)sort_tiles(n) * 256);
-    const size_t o_ka = L.take<uint64_t>(n);
-    const size_t o_va = L.take<uint32_t>(with_values ? n : 0);
-    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
-    arena_wait(ctx, s);
-    char* b = static_cast<char*>(ctx->arena.base);
-    CallSlots cs;
-    cs.h = reinterpret_cast<CallHeader*>(b + o_hdr);
-    SortBuffers sb{{reinterpret_cast<uint32_t*>(b + o_ss0), reinterpret_cast<uint32_t*>(b + o_ss1)}};
-    DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
-    int st = run_sort(ctx, cs, sb, d_keys_in, d_keys_out, reinterpret_cast<uint64_t*>(b + o_ka), d_vals_in, d_vals_out,
-                      with_values ? reinterpret_cast<uint32_t*>(b + o_va) : nullptr, with_values, n, nullptr, lo, hi, 0, s);
+    int st = enqueue_sort(ctx, d_keys_in, d_keys_out, d_vals_in, d_vals_out, n, lo, hi, s);
     if (st) return st;
-    DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, cs.h, 8, cudaMemcpyDeviceToHost, s));
-    DAGC_CUDA(ctx, cudaStreamSynchronize(s));
-    std::string msg;
-    st = device_error_status((uint32_t)ctx->h_stage[0], msg);
-    return st ? set_error(ctx, st, msg) : DAGC_OK;
+    return finish_sort(ctx, s);
+}
+
+int dagc_sort_plan(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int with_values, int* shape,
+                   int* radix_bits) {
+    if (!valid_ctx(ctx) || lo_bit < 0 || hi_bit > 64 || lo_bit > hi_bit || !shape || !radix_bits)
+        return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const SortChoice c = sort_plan_for(ctx, with_values != 0, lo_bit, hi_bit, n);
+    *shape = c.shape;
+    *radix_bits = c.radix_bits;
+    return DAGC_OK;
+}
+
+int dagc_tune_sort(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int with_values, int reps, int* best_shape,
+                   int* best_radix_bits, double* best_ms, double* default_ms) {
+    if (!valid_ctx(ctx) || lo_bit < 0 || hi_bit > 64 || lo_bit >= hi_bit || n == 0 || reps < 1)
+        return DAGC_ERR_INVALID_ARGUMENT;
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 keys");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const bool values = with_values != 0;
+    cudaStream_t s = ctx->capture_stream;  // a stream of the context's own, idle between calls
+    void *kin = nullptr, *kout = nullptr, *vout = nullptr;
+    DAGC_CUDA(ctx, ctx->pool.alloc(&kin, n * 8));
+    int st = DAGC_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(s);
+        ctx->pool.release(kin);
+        ctx->pool.release(kout);
+        ctx->pool.release(vout);
+        ctx->plan_override = nullptr;
+    };
+    if (ctx->pool.alloc(&kout, n * 8) != cudaSuccess || (values && ctx->pool.alloc(&vout, n * 4) != cudaSuccess)) {
+        cudaGetLastError();
+        cleanup();
+        return set_error(ctx, DAGC_ERR_OUT_OF_MEMORY, "tuning buffers");
+    }
+    launch_fill_tune_keys(static_cast<uint64_t*>(kin), n, lo_bit, hi_bit, 0x7E57C0DEull + n, s);
+    cudaEvent_t e0 = take_event(ctx), e1 = take_event(ctx);
+    if (!e0 || !e1) { cleanup(); return set_error(ctx, DAGC_ERR_CUDA, "events"); }
+    // Times one plan: one untimed sort, then `reps` sorts between two events.
+    auto time_plan = [&](SortChoice c, double* ms) -> int {
+        ctx->plan_override = &c;
+        for (int r = 0; r <= reps; ++r) {
+            if (r == 1) cudaEventRecord(e0, s);
+            const int e = enqueue_sort(ctx, static_cast<uint64_t*>(kin), static_cast<uint64_t*>(kout), nullptr,
+                                       static_cast<uint32_t*>(vout), n, lo_bit, hi_bit, s);
+            if (e) { ctx->plan_override = nullptr; return e; }
+        }
+        cudaEventRecord(e1, s);
+        ctx->plan_override = nullptr;
+        const int e = finish_sort(ctx, s);
+        if (e) return e;
+        float f = 0;
+        DAGC_CUDA(ctx, cudaEventElapsedTime(&f, e0, e1));
+        *ms = f / reps;
+        return DAGC_OK;
+    };
+    const SortChoice def = values ? kDefaultPairs : kDefaultKeys;
+    double dms = 0;
+    st = time_plan(def, &dms);
+    SortChoice best = def;
+    double bms = dms;
+    const int shapes = values ? kNumPairShapes : kNumKeyShapes;
+    const int max_bits = values ? kRadixBits : kMaxRadixBits;
+    for (int sh = 0; sh < shapes && !st; ++sh) {
+        for (int b = kRadixBits; b <= max_bits && !st; ++b) {
+            if (!sort_plan_valid(sh, values, b, lo_bit, hi_bit)) continue;
+            // Wider digits only where they save a pass.
+            if (b > kRadixBits && sort_passes_r(lo_bit, hi_bit, b) == sort_passes_r(lo_bit, hi_bit, b - 1)) continue;
+            double ms = 0;
+            st = time_plan(SortChoice{sh, b}, &ms);
+            if (!st && ms < bms) { bms = ms; best = SortChoice{sh, b}; }
+        }
+    }
+    ctx->free_events.push_back(e0);
+    ctx->free_events.push_back(e1);
+    cleanup();
+    if (st) return st;
+    const uint32_t cls = sort_class(values, hi_bit - lo_bit, n);
+    ctx->tune[cls] = best;
+    ctx->tune_ms[cls] = {bms, dms};
+    ++ctx->tune_version;
+    if (best_shape) *best_shape = best.shape;
+    if (best_radix_bits) *best_radix_bits = best.radix_bits;
+    if (best_ms) *best_ms = bms;
+    if (default_ms) *default_ms = dms;
+    return DAGC_OK;
+}
+
+int dagc_tune_save(dagc_context ctx, const char* path) {
+    if (!valid_ctx(ctx) || !path) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return save_tune_file(ctx, path);
+}
+
+int dagc_tune_load(dagc_context ctx, const char* path) {
+    if (!valid_ctx(ctx) || !path) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return load_tune_file(ctx, path);
+}
+
+int dagc_tune_clear(dagc_context ctx) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->tune.clear();
+    ctx->tune_ms.clear();
+    ++ctx->tune_version;
+    return DAGC_OK;
 }
 
 }  // extern "C"

@@ -27,13 +27,36 @@ constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;
 
 // ---------------------------------------------------------------- sort ----
 constexpr int kSortThreads = 256;
-// Digit-pass tiles hold 256 threads x (8..16) keys; status arrays are sized
-// for the smallest tile so that every pass shape fits.
+// Digit-pass tiles hold 256 threads x (8..16) keys.
 constexpr int kSortTile = 2048;
-constexpr int kRadixBits = 8;
+constexpr int kRadixBits = 8;       // default digit width
+constexpr int kMaxRadixBits = 11;   // widest digit a keys-only pass takes
 constexpr int kMaxPasses = 8;
+constexpr int kSortHistWords = 8192;  // one sort's histograms: passes x 2^(widest digit)
 
 DAGC_HD uint32_t sort_tiles(uint64_t n) { return (uint32_t)((n + kSortTile - 1) / kSortTile); }
+// Look-back status words of one digit pass for n keys, enough for every pass
+// shape: tiles of at least 2048 keys with 256 digits, or of at least 4096
+// keys with up to 2048 digits.
+DAGC_HD uint64_t sort_status_words(uint64_t n) { return ((n + 4095) / 4096 + 1) * 2048; }
+
+// Digits of a sort over bits [lo, hi) in `passes` passes: widths differ by at
+// most one, the wider ones first; pass i covers bits [shift, shift + bits).
+DAGC_HD int sort_passes_r(int lo_bit, int hi_bit, int radix_bits) {
+    return hi_bit > lo_bit ? (hi_bit - lo_bit + radix_bits - 1) / radix_bits : 0;
+}
+DAGC_HD void pass_digit(int lo_bit, int hi_bit, int passes, int i, int* shift, int* bits) {
+    const int b = hi_bit - lo_bit, w = b / passes, extra = b % passes;
+    *bits = w + (i < extra ? 1 : 0);
+    *shift = lo_bit + i * w + (i < extra ? i : extra);
+}
+// Histogram words between consecutive passes: 2^(widest digit).
+DAGC_HD int pass_hist_stride(int lo_bit, int hi_bit, int passes) {
+    const int b = hi_bit - lo_bit;
+    return passes > 0 ? 1 << ((b + passes - 1) / passes) : 0;
+}
+// Number of digit passes for a bit range at the default width.
+DAGC_HD int sort_passes(int lo_bit, int hi_bit) { return sort_passes_r(lo_bit, hi_bit, kRadixBits); }
 
 // Device count pointer convention: when d_n is non-null the kernels read the
 // element count from device memory (written by an earlier kernel) and n is an
@@ -49,13 +72,14 @@ struct SortArgs {
     uint64_t n;               // count or upper bound (see d_n)
     const uint64_t* d_n;
     int lo_bit, hi_bit;
+    int radix_bits;           // widest digit (8..11; keys only above 8); 0 = 8
     int validate_bits;        // > 0: flag keys with bits >= validate_bits set
-    uint32_t* hist;           // kMaxPasses * 256 words, zeroed
-    uint32_t* status[2];      // 2 x sort_tiles(n) * 256 words; status[0] zeroed on entry
+    uint32_t* hist;           // kSortHistWords words, zeroed
+    uint32_t* status[2];      // 2 x sort_status_words(n) words; status[0] zeroed on entry
     uint32_t* tile_counters;  // kMaxPasses words, zeroed
     uint32_t* err;
     int grid_hist, grid_pass; // persistent grid sizes
-    int shape;                // digit-pass kernel shape, see sort_shape_*
+    int shape;                // digit-pass kernel shape (a key shape or a pair shape)
     // Gate: when non-null, every kernel of the sort does nothing unless
     // *gate == gate_run (a path chosen on the device, see GroupArgs).
     const uint32_t* gate; uint32_t gate_run;
@@ -69,26 +93,30 @@ struct SortArgs {
     int seg_shift;
 };
 
-// Digit-pass kernel shapes (items per thread x minimum resident CTAs per SM,
-// which caps registers); the autotuner and dagc options pick one per sort.
-constexpr int kNumSortShapes = 8;
-int sort_shape_items(int shape);
-int sort_shape_min_ctas(int shape);
-// Resident CTAs per SM of a shape (occupancy query) for grid sizing.
-int occupancy_sort_shape(int shape, bool with_values);
+// Digit-pass kernel shapes. Keys-only sorts: (items per thread, minimum
+// resident CTAs per SM, which caps registers, equal-digit matching); each is
+// built for every digit width 8..kMaxRadixBits. Key/value sorts: 8-bit
+// digits. The autotuner and dagc options pick a shape and a width per sort.
+constexpr int kNumKeyShapes = 6;
+constexpr int kNumPairShapes = 8;
+constexpr int kNumSortShapes = kNumPairShapes;
+int sort_shape_items(int shape, bool with_values);
+// Resident CTAs per SM of a shape at a digit width (occupancy query) for grid sizing.
+int occupancy_sort_shape(int shape, bool with_values, int radix_bits = kRadixBits);
+// Whether a (shape, width) plan can sort bits [lo, hi): histogram room and
+// look-back status room.
+bool sort_plan_valid(int shape, bool with_values, int radix_bits, int lo_bit, int hi_bit);
 
-// Number of digit passes for a bit range.
-DAGC_HD int sort_passes(int lo_bit, int hi_bit) {
-    return hi_bit > lo_bit ? (hi_bit - lo_bit + kRadixBits - 1) / kRadixBits : 0;
-}
 // Where the result lands: keys_out always (the pass sequence is arranged so).
 void launch_sort(const SortArgs& a, cudaStream_t s);
 // The same, one launch at a time: histogram (+ copy when there is no digit),
-// then digit pass i for i in [0, sort_passes).
+// then digit pass i for i in [0, sort_plan_passes(a)).
+int sort_plan_passes(const SortArgs& a);
 void launch_sort_histogram(const SortArgs& a, cudaStream_t s);
 void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s);
-size_t sort_pass_smem(bool with_values);
 void sort_configure();  // sets shared-memory attributes once per device
+// Autotuner input: n pseudo-random keys with bits only in [lo_bit, hi_bit).
+void launch_fill_tune_keys(uint64_t* out, uint64_t n, int lo_bit, int hi_bit, uint64_t seed, cudaStream_t s);
 
 // ---------------------------------------------------------- DAG kernels ----
 constexpr int kScanThreads = 256;
@@ -272,6 +300,7 @@ uint64_t voxelize_tiles(uint64_t n_tri);
 constexpr int kTailThreads = 1024;
 constexpr int kTailCap = 4096;
 constexpr int kMaxTailLevels = 8;
+constexpr int kTailChildCap = 8192;  // most children of the tail's first level
 struct TailLevelOut {
     uint64_t* hashes; uint8_t* masks; uint32_t* children; uint64_t capacity;
     uint64_t* d_nodes; uint64_t* d_unique;
@@ -327,7 +356,6 @@ void launch_copy_segments(const CopyTable& t, cudaStream_t s);
 void kernels_configure();
 
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
-int occupancy_sort_pass(bool with_values);
 enum KernelId { kKernelLeafBuild = 0, kKernelExtract = 1, kKernelUnique = 2, kKernelFinalScan = 3 };
 int occupancy_kernel(int which);
 

@@ -28,8 +28,9 @@
 //                  representative's payload; the unique id goes to the slot;
 //   dedup_map      every item reads its unique id and representative through
 //                  its slot, duplicates are compared in full with their
-//                  representative (collision check), the slots' keys are
-//                  cleared (items sharing a slot still read its aux word).
+//                  representative (collision check). dedup_sort cleared the
+//                  slots' keys, once per distinct key (items sharing a slot
+//                  only read its aux word).
 //
 // What the fixed sizes cannot hold (table, unique list, a bucket) sets
 // kErrFallback, and the caller reruns the call with the radix-sort form.
@@ -360,6 +361,7 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
             if (uid < a.out_capacity && s < a.table_cap) {
                 a.out_keys[uid] = k;
                 aux[2 * (uint64_t)s + 1] = (uint32_t)uid;
+                a.table_key[s] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
                 if (a.out_masks) {
                     a.out_masks[uid] = m;
                     uint4* d4 = reinterpret_cast<uint4*>(a.out_children + uid * 8);
@@ -411,7 +413,6 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
                     collision |= a.masks[i] != a.masks[rep] || x0.x != y0.x || x0.y != y0.y || x0.z != y0.z ||
                                  x0.w != y0.w || x1.x != y1.x || x1.y != y1.y || x1.z != y1.z || x1.w != y1.w;
                 }
-                a.table_key[s[k]] = 0;  // leave the table empty for the next level
             }
             // Ids stay inside the next level's arrays even when a fallback or
             // an error discards this call.

@@ -3,15 +3,20 @@
 // (src/DAGCompression.cu:336-394) and thrust::sequence (:743-750).
 //
 // Structure (one-sweep style):
-//   1. radix_histogram: one read of the keys builds the 256-bin histogram of
-//      every digit pass at once (shared-memory counters, then global atomics),
+//   1. radix_histogram: one read of the keys builds the histogram of every
+//      digit pass at once (shared-memory counters, then global atomics),
 //      validates the key range and clears the first pass's look-back status.
-//   2. onesweep_pass, once per 8-bit digit: a persistent grid takes 4096-key
-//      tiles in order from an atomic counter, ranks keys inside each warp with
-//      __match_any_sync, publishes per-digit tile counts, finds the tile's
-//      global digit offsets by decoupled look-back (bounded waits), stages the
-//      tile in shared memory in digit order and writes it out so that equal
-//      digits land in contiguous runs.
+//   2. onesweep_pass, once per digit: a persistent grid takes tiles of keys in
+//      order from an atomic counter, ranks keys inside each warp with
+//      __match_any_sync or per-bit ballots, publishes per-digit tile counts,
+//      finds the tile's global digit offsets by decoupled look-back (bounded
+//      waits), stages the tile in shared memory in digit order and writes it
+//      out so that equal digits land in contiguous runs.
+// Digits are 8 bits wide for key/value sorts and 8 to 11 bits for keys-only
+// sorts (fewer passes over the keys; the digit width and the pass shape are
+// chosen per sort, see sort_plan_valid and the context's tuning table). The
+// digits of a sort are balanced: a 33-bit range in four passes takes widths
+// 9, 8, 8, 8.
 // All counts can be device-resident (d_n), so a whole pipeline runs without a
 // host round trip.
 
@@ -27,9 +32,8 @@ namespace {
 constexpr uint32_t kSAgg = 1u << 30;
 constexpr uint32_t kSInc = 2u << 30;
 constexpr uint32_t kSVal = (1u << 30) - 1;
-constexpr int kRadix = 1 << kRadixBits;
 
-constexpr int kPassThreads = 256;  // one thread per digit
+constexpr int kPassThreads = 256;
 
 // A device-resident count never exceeds the bound its buffers were sized for.
 __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
@@ -55,22 +59,45 @@ __device__ __forceinline__ uint32_t segment_from(const uint64_t* off, uint32_t c
 
 constexpr uint64_t kHistMinPerThread = 16;
 
-__global__ void __launch_bounds__(kSortThreads)
-radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t n_host, int lo_bit,
-                int hi_bit, int validate_bits, uint32_t* __restrict__ hist, uint32_t* status0,
-                uint32_t* err, const uint64_t* seg_offsets, uint32_t seg_count, int seg_shift,
-                const uint32_t* gate, uint32_t gate_run) {
+struct HistParams {
+    const uint64_t* keys;
+    const uint64_t* d_n;
+    uint64_t n_host;
+    int lo_bit, hi_bit, passes, stride;  // digit layout (pass_digit), words between passes
+    int validate_bits;
+    uint32_t* hist;
+    uint32_t* status0;                   // first pass's look-back status, cleared here
+    uint32_t first_tile, first_radix;    // its tile size and digit count
+    uint32_t* err;
+    const uint64_t* seg_offsets;
+    uint32_t seg_count;
+    int seg_shift;
+    const uint32_t* gate;
+    uint32_t gate_run;
+};
+
+__global__ void __launch_bounds__(kSortThreads) radix_histogram(HistParams h) {
     pdl_prologue();
-    __shared__ uint32_t s_hist[kMaxPasses][kRadix];
-    if (gate && *gate != gate_run) return;
-    const uint64_t n = load_n(d_n, n_host);
-    const int passes = sort_passes(lo_bit, hi_bit);
-    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+    __shared__ uint32_t s_hist[kSortHistWords];
+    if (h.gate && *h.gate != h.gate_run) return;
+    const uint64_t n = load_n(h.d_n, h.n_host);
+    const int passes = h.passes;
+    const int words = passes * h.stride;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) s_hist[i] = 0;
     // Clear the first pass's look-back status for this n.
-    const uint64_t status_words = (uint64_t)sort_tiles(n) * kRadix;
+    const uint64_t status_words = (n + h.first_tile - 1) / h.first_tile * h.first_radix;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = gtid; i < status_words; i += gstride) status0[i] = 0;
+    for (uint64_t i = gtid; i < status_words; i += gstride) h.status0[i] = 0;
+    int shift[kMaxPasses];
+    uint32_t mask[kMaxPasses];
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p) {
+        int b = 0;
+        shift[p] = 0;
+        if (p < passes) pass_digit(h.lo_bit, h.hi_bit, passes, p, &shift[p], &b);
+        mask[p] = (1u << b) - 1u;
+    }
     __syncthreads();
     // Only the CTAs the keys need (at least kHistMinPerThread keys per
     // thread) build histograms: the grid is sized by the bound, and for a
@@ -91,27 +118,27 @@ radix_histogram(const uint64_t* __restrict__ keys, const uint64_t* d_n, uint64_t
         for (int u = 0; u < 4; ++u) {
             const uint64_t i = i0 + u * astride;
             in[u] = i < n;
-            k[u] = in[u] ? __ldg(keys + i) : 0;
+            k[u] = in[u] ? __ldg(h.keys + i) : 0;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (!in[u]) continue;
-            if (validate_bits > 0 && validate_bits < 64) bad |= k[u] >> validate_bits;
-            if (seg_offsets)
-                k[u] |= (uint64_t)segment_search(seg_offsets, seg_count, i0 + u * astride) << seg_shift;
-            for (int p = 0; p < passes; ++p) {
-                const int shift = lo_bit + p * kRadixBits;
-                const int bits = min(kRadixBits, hi_bit - shift);
-                const uint32_t d = (uint32_t)(k[u] >> shift) & ((1u << bits) - 1u);
-                atomicAdd(&s_hist[p][d], 1u);
+            if (h.validate_bits > 0 && h.validate_bits < 64) bad |= k[u] >> h.validate_bits;
+            if (h.seg_offsets)
+                k[u] |= (uint64_t)segment_search(h.seg_offsets, h.seg_count, i0 + u * astride) << h.seg_shift;
+#pragma unroll
+            for (int p = 0; p < kMaxPasses; ++p) {
+                if (p >= passes) break;
+                const uint32_t d = (uint32_t)(k[u] >> shift[p]) & mask[p];
+                atomicAdd(&s_hist[p * h.stride + d], 1u);
             }
         }
     }
-    if (__any_sync(0xFFFFFFFFu, bad != 0) && (threadIdx.x & 31) == 0) atomicOr(err, kErrBadInput);
+    if (__any_sync(0xFFFFFFFFu, bad != 0) && (threadIdx.x & 31) == 0) atomicOr(h.err, kErrBadInput);
     __syncthreads();
-    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
-        const uint32_t c = (&s_hist[0][0])[i];
-        if (c) atomicAdd(hist + i, c);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) {
+        const uint32_t c = s_hist[i];
+        if (c) atomicAdd(h.hist + i, c);
     }
 }
 
@@ -122,9 +149,10 @@ struct PassParams {
     uint32_t* vals_out;
     const uint64_t* d_n;
     uint64_t n_host;
-    const uint32_t* hist;     // 256 digit counts of this pass
+    const uint32_t* hist;     // this pass's digit counts (2^bits of them)
     uint32_t* status;         // this pass
     uint32_t* status_clear;   // next pass's status (null for the last pass)
+    uint32_t clear_radix;     // digits of the next pass (its tiles are this pass's)
     uint32_t* tile_counter;
     uint32_t* err;
     int shift, bits;
@@ -135,50 +163,130 @@ struct PassParams {
     uint32_t gate_run;
 };
 
-// Exclusive prefix of one digit over the tiles before `tile`: walks back over
-// their published counts 16 tiles per round trip, stopping at the first
-// inclusive prefix; waits (bounded) on tiles that have published nothing yet.
-// (When every tile of a small sort runs at once, inclusive prefixes spread
-// about one window per round trip, so the window width sets the latency.)
-__device__ __forceinline__ uint32_t lookback_digit(const uint32_t* status, uint32_t tile, uint32_t d,
-                                                   uint32_t* err) {
-    constexpr int kLB = 16;
-    uint32_t excl = 0, iter = 0;
-    int64_t t = (int64_t)tile - 1;
-    while (true) {
-        uint32_t st[kLB];
+// Loads / stores kN consecutive shared (or global) words as vectors.
+template <int kN>
+__device__ __forceinline__ void load_words(const uint32_t* p, uint32_t (&v)[kN]) {
+    if constexpr (kN % 4 == 0) {
 #pragma unroll
-        for (int k = 0; k < kLB; ++k)
-            st[k] = t - k >= 0 ? ld_relaxed(status + (uint64_t)(t - k) * kRadix + d) : kSInc;
-        int consumed = kLB;
-        bool done = false;
+        for (int q = 0; q < kN; q += 4) {
+            const uint4 x = *reinterpret_cast<const uint4*>(p + q);
+            v[q] = x.x; v[q + 1] = x.y; v[q + 2] = x.z; v[q + 3] = x.w;
+        }
+    } else if constexpr (kN == 2) {
+        const uint2 x = *reinterpret_cast<const uint2*>(p);
+        v[0] = x.x; v[1] = x.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < kN; ++q) v[q] = p[q];
+    }
+}
+template <int kN>
+__device__ __forceinline__ void store_words(uint32_t* p, const uint32_t (&v)[kN]) {
+    if constexpr (kN % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < kN; q += 4) *reinterpret_cast<uint4*>(p + q) = make_uint4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+    } else if constexpr (kN == 2) {
+        *reinterpret_cast<uint2*>(p) = make_uint2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < kN; ++q) p[q] = v[q];
+    }
+}
+// Relaxed (look-back) loads and stores of kN consecutive status words.
+template <int kN>
+__device__ __forceinline__ void ld_status(const uint32_t* p, uint32_t (&v)[kN]) {
+    if constexpr (kN % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < kN; q += 4)
+            asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(v[q]), "=r"(v[q + 1]), "=r"(v[q + 2]), "=r"(v[q + 3])
+                         : "l"(p + q)
+                         : "memory");
+    } else if constexpr (kN == 2) {
+        asm volatile("ld.relaxed.gpu.global.v2.u32 {%0, %1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "l"(p) : "memory");
+    } else {
+        v[0] = ld_relaxed(p);
+    }
+}
+template <int kN>
+__device__ __forceinline__ void st_status(uint32_t* p, const uint32_t (&v)[kN]) {
+    if constexpr (kN % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < kN; q += 4)
+            asm volatile("st.relaxed.gpu.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p + q), "r"(v[q]),
+                         "r"(v[q + 1]), "r"(v[q + 2]), "r"(v[q + 3])
+                         : "memory");
+    } else if constexpr (kN == 2) {
+        asm volatile("st.relaxed.gpu.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v[0]), "r"(v[1]) : "memory");
+    } else {
+        st_relaxed(p, v[0]);
+    }
+}
+
+// Exclusive prefixes of a thread's kDPT consecutive digits (starting at d0)
+// over the tiles before `tile`: walks back over their published counts
+// several tiles per round trip, each digit stopping at its first inclusive
+// prefix; waits (bounded) on tiles that have published nothing yet. All
+// digits advance over the same tiles: a round consumes the tiles up to the
+// first one some unfinished digit still waits for.
+template <int kDPT>
+__device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t radix, uint32_t tile, uint32_t d0,
+                                                uint32_t (&excl)[kDPT], uint32_t* err) {
+    constexpr int kLB = kDPT >= 4 ? 4 : 16 / kDPT;  // tiles per round trip
+    uint32_t done = 0, iter = 0;
+    constexpr uint32_t kAll = (1u << kDPT) - 1u;
+#pragma unroll
+    for (int q = 0; q < kDPT; ++q) excl[q] = 0;
+    int64_t t = (int64_t)tile - 1;
+    while (done != kAll) {
+        uint32_t st[kLB][kDPT];
 #pragma unroll
         for (int k = 0; k < kLB; ++k) {
-            if (done || k >= consumed) continue;
-            const uint32_t f = st[k] >> 30;
-            if (f == 0) {
-                consumed = k;  // not published yet: resume here
+            if (t - k >= 0) {
+                ld_status<kDPT>(status + (uint64_t)(t - k) * radix + d0, st[k]);
             } else {
-                excl += st[k] & kSVal;
-                done = f == 2;
+#pragma unroll
+                for (int q = 0; q < kDPT; ++q) st[k][q] = kSInc;
             }
         }
-        if (done) break;
+        // Tiles every unfinished digit can take: up to the first unpublished
+        // one before that digit's inclusive prefix.
+        int consumed = kLB;
+#pragma unroll
+        for (int q = 0; q < kDPT; ++q) {
+            if (done >> q & 1u) continue;
+#pragma unroll
+            for (int k = 0; k < kLB; ++k) {
+                const uint32_t f = st[k][q] >> 30;
+                if (f == 2) break;
+                if (f == 0) { consumed = min(consumed, k); break; }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kDPT; ++q) {
+            if (done >> q & 1u) continue;
+#pragma unroll
+            for (int k = 0; k < kLB; ++k) {
+                if (k >= consumed) break;
+                excl[q] += st[k][q] & kSVal;
+                if ((st[k][q] >> 30) == 2) { done |= 1u << q; break; }
+            }
+        }
         t -= consumed;
         if (consumed == 0) {
             if (++iter > kSpinLimit) { atomicOr(err, kErrTimeout); break; }
             backoff(iter);
         }
     }
-    return excl;
 }
 
 // Shared memory of one onesweep CTA: the staging tile, per-warp digit
 // counters (turned into per-warp output offsets) and per-digit offsets.
-template <int kThreads, int kItems, bool kValues>
+template <int kBits, int kItems, bool kValues>
 struct PassSmem {
-    static constexpr int kTile = kThreads * kItems;
-    static constexpr int kWarpsPerCta = kThreads / 32;
+    static constexpr int kRadix = 1 << kBits;
+    static constexpr int kTile = kPassThreads * kItems;
+    static constexpr int kWarpsPerCta = kPassThreads / 32;
     uint64_t keys[kTile];
     uint32_t vals[kValues ? kTile : 4];
     uint32_t whist[kWarpsPerCta][kRadix];
@@ -188,34 +296,77 @@ struct PassSmem {
     uint32_t tile_id;
 };
 
-// One 8-bit digit pass. Tiles of kTile keys are taken in increasing order from
-// an atomic counter by a persistent grid. Per tile:
-//   1. each thread loads its keys straight into registers (warp-striped,
-//      coalesced), so shared memory only carries the counters and the
-//      staged output;
-//   2. each warp ranks its 32*kItems keys stably with __match_any_sync and a
+// Ranks one warp's kItems rows of 32 keys stably: per row, the lanes holding
+// the same digit are found (match.any on the ADU pipe, or one ballot per
+// digit bit on the ALU pipe, or both alternating), the highest of them adds
+// the group's size to the warp's counter for that digit and the count before
+// it is broadcast. dr[j] holds the digit in its high half and receives the
+// rank (< 2^16) in its low half. kFull: every lane of every row is valid.
+template <int kBits, int kItems, int kMatch, bool kFull>
+__device__ __forceinline__ void rank_warp(uint32_t (&dr)[kItems], uint32_t* wh, uint32_t wofs, uint32_t tile_n,
+                                          uint32_t lane) {
+#pragma unroll
+    for (int j = 0; j < kItems; ++j) {
+        const bool valid = kFull || wofs + j * 32 + lane < tile_n;
+        const uint32_t d = dr[j] >> 16;
+        // Every warp collective below is executed by all 32 lanes (valid or
+        // not); only the results are masked, never the calls.
+        uint32_t peers;
+        if (kMatch == 1 || (kMatch == 2 && (j & 1))) {
+            peers = __match_any_sync(0xFFFFFFFFu, valid ? d : 0xFFFFFFFFu);
+        } else {
+            // Bits above the pass's width are zero in every lane's digit, so
+            // their ballots leave `peers` unchanged.
+            const uint32_t vmask = kFull ? 0xFFFFFFFFu : __ballot_sync(0xFFFFFFFFu, valid);
+            peers = vmask;
+#pragma unroll
+            for (int b = 0; b < kBits; ++b) {
+                const bool bit = (d >> b) & 1u;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+                peers &= bit ? m : ~m;
+            }
+            if (!kFull && !valid) peers = ~vmask;  // invalid lanes: a group of their own, unused
+        }
+        const uint32_t upto = __popc(peers & lanemask_le());
+        const uint32_t leader = 31 - __clz(peers);
+        uint32_t prior = 0;
+        if (valid && lane == leader) prior = atomicAdd(&wh[d], upto);
+        prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
+        dr[j] |= prior + upto - 1;
+    }
+}
+
+// One digit pass (digits of at most kBits bits). Tiles of kTile keys are
+// taken in increasing order from an atomic counter by a persistent grid. Per
+// tile:
+//   1. each thread loads its keys (warp-striped, coalesced) and keeps only
+//      their digits in registers;
+//   2. each warp ranks its 32*kItems keys stably (rank_warp) with a
 //      warp-private counter per digit;
-//   3. thread d sums digit d over the warps, publishes the tile count for the
-//      decoupled look-back, and a block scan gives the tile-local offsets;
-//      the per-warp counters become per-warp output offsets in place;
-//   4. thread d looks back over earlier tiles (8 per round trip, bounded
-//      waits) for digit d's global offset and publishes the inclusive prefix;
-//   5. keys are staged in digit order and written out so that equal digits
-//      form contiguous runs.
-// kMatch: how lanes with equal digits are found. 0: one ballot per digit bit
-// (ALU pipe), 1: match.any (ADU pipe), 2: alternate per item, which spreads
-// the work over both pipes.
-template <int kThreads, int kItems, bool kValues, int kMinCtas, int kMatch>
-__global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p) {
+//   3. each thread sums its kRadix/256 digits over the warps, publishes the
+//      tile counts for the decoupled look-back, and a block scan gives the
+//      tile-local offsets; the per-warp counters become per-warp output
+//      offsets in place;
+//   4. keys are fetched again (the tile was just read: cache hits) and staged
+//      in digit order in shared memory; values, if any, are fetched here;
+//   5. each thread looks back over earlier tiles for its digits' global
+//      offsets and publishes the inclusive prefixes;
+//   6. the staged tile is written out so that equal digits form contiguous
+//      runs.
+template <int kBits, int kItems, bool kValues, int kMinCtas, int kMatch>
+__global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassParams p) {
     pdl_prologue();
-    using Smem = PassSmem<kThreads, kItems, kValues>;
+    using Smem = PassSmem<kBits, kItems, kValues>;
     constexpr int kTile = Smem::kTile;
     constexpr int kW = Smem::kWarpsPerCta;
-    static_assert(kThreads == kRadix, "one thread per digit");
+    constexpr int kRadix = Smem::kRadix;
+    constexpr int kDPT = kRadix / kPassThreads;  // digits per thread: 1, 2, 4 or 8
+    static_assert(kDPT >= 1 && kRadix % kPassThreads == 0, "digits per thread");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t d0 = tid * kDPT;
     if (p.gate && *p.gate != p.gate_run) return;
     const uint64_t n64 = load_n(p.d_n, p.n_host);
     const uint32_t n = (uint32_t)n64;
@@ -227,18 +378,29 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
     const uint32_t dmask = (1u << p.bits) - 1u;
 
     if (p.status_clear) {
-        const uint64_t words = (uint64_t)ntiles * kRadix;
-        for (uint64_t i = (uint64_t)blockIdx.x * kThreads + tid; i < words; i += (uint64_t)active * kThreads)
+        const uint64_t words = (uint64_t)ntiles * p.clear_radix;
+        for (uint64_t i = (uint64_t)blockIdx.x * kPassThreads + tid; i < words; i += (uint64_t)active * kPassThreads)
             p.status_clear[i] = 0;
     }
     {
-        uint32_t total;
-        S.gbase[tid] = block_exclusive_sum<uint32_t>(p.hist[tid], S.scan, &total);
+        // Global digit starts: exclusive scan of the pass histogram.
+        uint32_t h[kDPT], sum = 0, total;
+#pragma unroll
+        for (int q = 0; q < kDPT; ++q) {
+            h[q] = d0 + q < (1u << p.bits) ? p.hist[d0 + q] : 0u;
+            sum += h[q];
+        }
+        uint32_t run = block_exclusive_sum<uint32_t>(sum, S.scan, &total);
+#pragma unroll
+        for (int q = 0; q < kDPT; ++q) {
+            S.gbase[d0 + q] = run;
+            run += h[q];
+        }
     }
     uint32_t* wh = S.whist[warp];
     while (true) {
         if (tid == 0) S.tile_id = atomicAdd(p.tile_counter, 1u);
-        for (int i = tid; i < kW * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0;
+        for (int i = tid; i < kW * kRadix; i += kPassThreads) (&S.whist[0][0])[i] = 0;
         __syncthreads();
         const uint32_t tile = S.tile_id;
         if (tile >= ntiles) break;
@@ -246,102 +408,121 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) onesweep_pass(PassParams p
         const uint32_t tile_n = min((uint32_t)kTile, n - base);
         const uint32_t wofs = warp * (kItems * 32);
 
-        uint64_t k[kItems];
+        // 1. Digits of this thread's keys (composite keys on the first pass
+        //    of a segmented sort).
+        uint32_t dr[kItems];
+        {
+            uint64_t k[kItems];
 #pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const uint32_t i = wofs + j * 32 + lane;
-            if (i < tile_n) k[j] = p.keys_in[base + i];
+            for (int j = 0; j < kItems; ++j) {
+                const uint32_t i = wofs + j * 32 + lane;
+                k[j] = i < tile_n ? __ldg(p.keys_in + base + i) : 0ull;
+            }
+            if (p.seg_offsets) {
+                uint32_t sg = segment_search(p.seg_offsets, p.seg_count, base + wofs + lane);
+#pragma unroll
+                for (int j = 0; j < kItems; ++j) {
+                    const uint32_t i = wofs + j * 32 + lane;
+                    if (i < tile_n) {
+                        sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
+                        k[j] |= (uint64_t)sg << p.seg_shift;
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kItems; ++j) dr[j] = ((uint32_t)(k[j] >> p.shift) & dmask) << 16;
         }
-        if (p.seg_offsets) {  // first pass of a segmented sort: build composite keys
-            uint32_t sg = segment_search(p.seg_offsets, p.seg_count, base + wofs + lane);
+        // 2. Ranks within the warp.
+        if (tile_n == (uint32_t)kTile) rank_warp<kBits, kItems, kMatch, true>(dr, wh, wofs, tile_n, lane);
+        else rank_warp<kBits, kItems, kMatch, false>(dr, wh, wofs, tile_n, lane);
+        __syncthreads();
+
+        // 3. This thread's digits: count over the warps, publish the tile
+        //    counts, block scan for the tile-local offsets; the per-warp
+        //    counters become per-warp output offsets in place.
+        uint32_t cnt[kDPT], local[kDPT];
+        {
+            uint32_t acc[kDPT];
+#pragma unroll
+            for (int q = 0; q < kDPT; ++q) acc[q] = 0;
+#pragma unroll
+            for (int w = 0; w < kW; ++w) {
+                uint32_t c[kDPT];
+                load_words<kDPT>(&S.whist[w][d0], c);
+                store_words<kDPT>(&S.whist[w][d0], acc);
+#pragma unroll
+                for (int q = 0; q < kDPT; ++q) acc[q] += c[q];
+            }
+            uint32_t pub[kDPT], sum = 0;
+#pragma unroll
+            for (int q = 0; q < kDPT; ++q) {
+                cnt[q] = acc[q];
+                pub[q] = (tile == 0 ? kSInc : kSAgg) | cnt[q];
+                sum += cnt[q];
+            }
+            st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
+            uint32_t total;
+            uint32_t run = block_exclusive_sum<uint32_t>(sum, S.scan, &total);
+#pragma unroll
+            for (int q = 0; q < kDPT; ++q) {
+                local[q] = run;
+                run += cnt[q];
+            }
+#pragma unroll
+            for (int w = 0; w < kW; ++w) {
+                uint32_t c[kDPT];
+                load_words<kDPT>(&S.whist[w][d0], c);
+#pragma unroll
+                for (int q = 0; q < kDPT; ++q) c[q] += local[q];
+                store_words<kDPT>(&S.whist[w][d0], c);
+            }
+        }
+        __syncthreads();
+        // 4. Stage in tile-local digit order: the keys are fetched again
+        //    (cache hits), values (if any) here for the first time.
+        {
+            uint32_t sg = 0;
+            if (p.seg_offsets) sg = segment_search(p.seg_offsets, p.seg_count, base + wofs + lane);
 #pragma unroll
             for (int j = 0; j < kItems; ++j) {
                 const uint32_t i = wofs + j * 32 + lane;
                 if (i < tile_n) {
-                    sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
-                    k[j] |= (uint64_t)sg << p.seg_shift;
+                    uint64_t key = __ldg(p.keys_in + base + i);
+                    if (p.seg_offsets) {
+                        sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
+                        key |= (uint64_t)sg << p.seg_shift;
+                    }
+                    const uint32_t pos = wh[dr[j] >> 16] + (dr[j] & 0xFFFFu);
+                    S.keys[pos] = key;
+                    if (kValues) S.vals[pos] = p.vals_in ? p.vals_in[base + i] : base + i;
                 }
             }
         }
-        // Ranks within the warp fit 16 bits: two per register.
-        uint32_t rank2[kItems / 2];
+        // 5. Look back for this thread's digits' offsets among earlier
+        //    tiles, publish the inclusive prefixes.
+        {
+            uint32_t excl[kDPT];
+            if (tile > 0) {
+                lookback_digits<kDPT>(p.status, kRadix, tile, d0, excl, p.err);
+                uint32_t pub[kDPT];
 #pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const bool valid = wofs + j * 32 + lane < tile_n;
-            const uint32_t d = (uint32_t)(k[j] >> p.shift) & dmask;
-            // Lanes holding the same digit. Every warp collective below is
-            // executed by all 32 lanes (valid or not); only the results are
-            // masked, never the calls.
-            uint32_t peers;
-            if (kMatch == 1 || (kMatch == 2 && (j & 1))) {
-                peers = __match_any_sync(0xFFFFFFFFu, valid ? d : 0xFFFFFFFFu);
+                for (int q = 0; q < kDPT; ++q) pub[q] = kSInc | (excl[q] + cnt[q]);
+                st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
             } else {
-                // One ballot per digit bit; bits above p.bits are zero in every
-                // lane's digit, so their ballot leaves `peers` unchanged.
-                const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
-                peers = vmask;
 #pragma unroll
-                for (int b = 0; b < kRadixBits; ++b) {
-                    const bool bit = (d >> b) & 1u;
-                    const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
-                    peers &= bit ? m : ~m;
-                }
-                if (!valid) peers = ~vmask;  // invalid lanes: a group of their own, unused
+                for (int q = 0; q < kDPT; ++q) excl[q] = 0;
             }
-            // The highest peer adds the group's size to the warp's digit
-            // counter and broadcasts the count before it.
-            const uint32_t upto = __popc(peers & lanemask_le());
-            const uint32_t leader = 31 - __clz(peers);
-            uint32_t prior = 0;
-            if (valid && lane == leader) prior = atomicAdd(&wh[d], upto);
-            prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
-            const uint32_t r = prior + upto - 1;
-            if (j & 1) rank2[j / 2] |= r << 16;
-            else rank2[j / 2] = r;
+            uint32_t adj[kDPT], gb[kDPT];
+            load_words<kDPT>(&S.gbase[d0], gb);
+#pragma unroll
+            for (int q = 0; q < kDPT; ++q) adj[q] = gb[q] + excl[q] - local[q];
+            store_words<kDPT>(&S.adj[d0], adj);
         }
         __syncthreads();
-
-        // Digit d = tid: count over the warps, publish the tile count, block
-        // scan for the tile-local offsets; the per-warp counters become
-        // per-warp output offsets in place.
-        uint32_t cnt = 0;
-#pragma unroll
-        for (int w = 0; w < kW; ++w) {
-            const uint32_t c = S.whist[w][tid];
-            S.whist[w][tid] = cnt;
-            cnt += c;
-        }
-        uint32_t* my = p.status + (uint64_t)tile * kRadix + tid;
-        st_relaxed(my, (tile == 0 ? kSInc : kSAgg) | cnt);
-        uint32_t total;
-        const uint32_t local = block_exclusive_sum<uint32_t>(cnt, S.scan, &total);
-#pragma unroll
-        for (int w = 0; w < kW; ++w) S.whist[w][tid] += local;
-        __syncthreads();
-        // Stage in tile-local digit order; values (if any) are fetched here,
-        // they play no part in the ranking.
-#pragma unroll
-        for (int j = 0; j < kItems; ++j) {
-            const uint32_t i = wofs + j * 32 + lane;
-            if (i < tile_n) {
-                const uint32_t r = (rank2[j / 2] >> ((j & 1) * 16)) & 0xFFFFu;
-                const uint32_t pos = wh[(uint32_t)(k[j] >> p.shift) & dmask] + r;
-                S.keys[pos] = k[j];
-                if (kValues) S.vals[pos] = p.vals_in ? p.vals_in[base + i] : base + i;
-            }
-        }
-        // Look back for digit d's offset among earlier tiles, publish the
-        // inclusive prefix.
-        uint32_t excl = 0;
-        if (tile > 0) {
-            excl = lookback_digit(p.status, tile, tid, p.err);
-            st_relaxed(my, kSInc | (excl + cnt));
-        }
-        S.adj[tid] = S.gbase[tid] + excl - local;
-        __syncthreads();
+        // 6. Write-out.
         bool oob = false;
 #pragma unroll 4
-        for (uint32_t i = tid; i < tile_n; i += kThreads) {
+        for (uint32_t i = tid; i < tile_n; i += kPassThreads) {
             const uint64_t key = S.keys[i];
             const uint32_t dst = S.adj[(uint32_t)(key >> p.shift) & dmask] + i;
             if (dst < n) {
@@ -368,57 +549,113 @@ __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin
     }
 }
 
-}  // namespace
-
-// Shape table: (items per thread, minimum CTAs per SM, match mode).
-#define DAGC_SORT_SHAPES(X) \
-    X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2)
-
-namespace {
-struct ShapeEntry {
-    int items, min_ctas;
-    void (*keys)(PassParams);
-    void (*pairs)(PassParams);
-    size_t smem_keys, smem_pairs;
-};
-#define DAGC_SHAPE_ENTRY(id, items, ctas, match)                                                     \
-    {items, ctas, onesweep_pass<kPassThreads, items, false, ctas, match>,                             \
-     onesweep_pass<kPassThreads, items, true, ctas, match>, sizeof(PassSmem<kPassThreads, items, false>), \
-     sizeof(PassSmem<kPassThreads, items, true>)},
-const ShapeEntry kShapes[kNumSortShapes] = {DAGC_SORT_SHAPES(DAGC_SHAPE_ENTRY)};
-#undef DAGC_SHAPE_ENTRY
-}  // namespace
-
-int sort_shape_items(int shape) { return kShapes[shape].items; }
-int sort_shape_min_ctas(int shape) { return kShapes[shape].min_ctas; }
-
-size_t sort_pass_smem(bool with_values) {
-    size_t m = 0;
-    for (const ShapeEntry& e : kShapes) m = std::max(m, with_values ? e.smem_pairs : e.smem_keys);
-    return m;
-}
-
-void sort_configure() {
-    for (const ShapeEntry& e : kShapes) {
-        cudaFuncSetAttribute(e.keys, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem_keys);
-        cudaFuncSetAttribute(e.pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem_pairs);
+// Synthetic keys for the autotuner: a SplitMix64 sequence (Steele, Lea and
+// Flood, 2014) of the index, placed in bits [lo, hi).
+__global__ void fill_tune_keys(uint64_t* out, uint64_t n, int lo, int hi, uint64_t seed) {
+    const uint64_t mask = hi - lo >= 64 ? ~0ull : ((1ull << (hi - lo)) - 1ull) << lo;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        out[i] = (z << lo) & mask;
     }
 }
 
-int occupancy_sort_shape(int shape, bool with_values) {
-    const ShapeEntry& e = kShapes[shape];
+}  // namespace
+
+void launch_fill_tune_keys(uint64_t* out, uint64_t n, int lo_bit, int hi_bit, uint64_t seed, cudaStream_t s) {
+    const uint64_t blocks = (n + 255) / 256;
+    fill_tune_keys<<<(unsigned)(blocks < 4096 ? (blocks ? blocks : 1) : 4096), 256, 0, s>>>(out, n, lo_bit, hi_bit, seed);
+}
+
+// Keys-only shapes: (items per thread, minimum CTAs per SM, match mode); each
+// is built for digits of 8, 9, 10 and 11 bits.
+#define DAGC_KEY_SHAPES(X) X(0, 16, 3, 2) X(1, 16, 2, 2) X(2, 16, 4, 2) X(3, 12, 4, 2) X(4, 16, 3, 0) X(5, 16, 3, 1)
+// Key/value shapes (8-bit digits).
+#define DAGC_PAIR_SHAPES(X) \
+    X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2)
+
+namespace {
+struct PassKernel {
+    void (*fn)(PassParams);
+    size_t smem;
+};
+struct KeyShape {
+    int items, min_ctas;
+    PassKernel by_bits[kMaxRadixBits - kRadixBits + 1];  // digit widths 8..11
+};
+struct PairShape {
+    int items, min_ctas;
+    PassKernel kernel;
+};
+#define DAGC_KEY_KERNEL(items, ctas, match, bits) \
+    {onesweep_pass<bits, items, false, ctas, match>, sizeof(PassSmem<bits, items, false>)}
+#define DAGC_KEY_SHAPE_ENTRY(id, items, ctas, match)                                                      \
+    {items, ctas, {DAGC_KEY_KERNEL(items, ctas, match, 8), DAGC_KEY_KERNEL(items, ctas, match, 9),      \
+                   DAGC_KEY_KERNEL(items, ctas, match, 10), DAGC_KEY_KERNEL(items, ctas, match, 11)}},
+#define DAGC_PAIR_SHAPE_ENTRY(id, items, ctas, match) \
+    {items, ctas, {onesweep_pass<8, items, true, ctas, match>, sizeof(PassSmem<8, items, true>)}},
+const KeyShape kKeyShapes[kNumKeyShapes] = {DAGC_KEY_SHAPES(DAGC_KEY_SHAPE_ENTRY)};
+const PairShape kPairShapes[kNumPairShapes] = {DAGC_PAIR_SHAPES(DAGC_PAIR_SHAPE_ENTRY)};
+#undef DAGC_KEY_KERNEL
+#undef DAGC_KEY_SHAPE_ENTRY
+#undef DAGC_PAIR_SHAPE_ENTRY
+
+int clamp_shape(int shape, bool with_values) {
+    const int count = with_values ? kNumPairShapes : kNumKeyShapes;
+    return shape < 0 || shape >= count ? 0 : shape;
+}
+int plan_bits(const SortArgs& a) {
+    if (a.with_values || a.radix_bits <= kRadixBits) return kRadixBits;
+    return a.radix_bits > kMaxRadixBits ? kMaxRadixBits : a.radix_bits;
+}
+// The kernel of one pass: the shape's, built for the pass's digit width.
+const PassKernel& pass_kernel(int shape, bool with_values, int bits) {
+    if (with_values) return kPairShapes[clamp_shape(shape, true)].kernel;
+    const int b = bits < kRadixBits ? kRadixBits : (bits > kMaxRadixBits ? kMaxRadixBits : bits);
+    return kKeyShapes[clamp_shape(shape, false)].by_bits[b - kRadixBits];
+}
+uint32_t pass_radix(int bits) { return 1u << (bits < kRadixBits ? kRadixBits : bits); }
+}  // namespace
+
+int sort_shape_items(int shape, bool with_values) {
+    return with_values ? kPairShapes[clamp_shape(shape, true)].items : kKeyShapes[clamp_shape(shape, false)].items;
+}
+
+void sort_configure() {
+    for (const KeyShape& e : kKeyShapes)
+        for (const PassKernel& k : e.by_bits)
+            cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+    for (const PairShape& e : kPairShapes)
+        cudaFuncSetAttribute(e.kernel.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.kernel.smem);
+}
+
+int occupancy_sort_shape(int shape, bool with_values, int radix_bits) {
+    const PassKernel& k = pass_kernel(shape, with_values, with_values ? kRadixBits : radix_bits);
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, with_values ? e.pairs : e.keys, kPassThreads,
-                                                  with_values ? e.smem_pairs : e.smem_keys);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, kPassThreads, k.smem);
     return occ;
 }
 
-int occupancy_sort_pass(bool with_values) { return occupancy_sort_shape(1, with_values); }
+bool sort_plan_valid(int shape, bool with_values, int radix_bits, int lo_bit, int hi_bit) {
+    if (with_values && radix_bits > kRadixBits) return false;
+    if (radix_bits < kRadixBits || radix_bits > kMaxRadixBits) return false;
+    const int passes = sort_passes_r(lo_bit, hi_bit, radix_bits);
+    if (passes > kMaxPasses) return false;
+    if (passes && passes * pass_hist_stride(lo_bit, hi_bit, passes) > kSortHistWords) return false;
+    // Look-back status room (sort_status_words): at most one digit word per
+    // two keys of a tile.
+    const int tile = kPassThreads * sort_shape_items(shape, with_values);
+    return (int)pass_radix(radix_bits) * 2 <= tile;
+}
+
+int sort_plan_passes(const SortArgs& a) { return sort_passes_r(a.lo_bit, a.hi_bit, plan_bits(a)); }
 
 // Launch parameters of digit pass i: the passes ping-pong so that the last
 // one always writes keys_out (pass i writes keys_out when passes-1-i is even).
 static PassParams pass_params(const SortArgs& a, int i) {
-    const int passes = sort_passes(a.lo_bit, a.hi_bit);
+    const int passes = sort_plan_passes(a);
     const bool to_out = ((passes - 1 - i) & 1) == 0;
     PassParams p;
     p.keys_in = i == 0 ? a.keys_in : (to_out ? a.keys_alt : a.keys_out);
@@ -427,13 +664,18 @@ static PassParams pass_params(const SortArgs& a, int i) {
     p.vals_out = to_out ? a.vals_out : a.vals_alt;
     p.d_n = a.d_n;
     p.n_host = a.n;
-    p.hist = a.hist + i * 256;
+    p.hist = a.hist + i * pass_hist_stride(a.lo_bit, a.hi_bit, passes);
     p.status = a.status[i & 1];
     p.status_clear = i + 1 < passes ? a.status[(i + 1) & 1] : nullptr;
+    pass_digit(a.lo_bit, a.hi_bit, passes, i, &p.shift, &p.bits);
+    p.clear_radix = 0;
+    if (i + 1 < passes) {
+        int sh, b;
+        pass_digit(a.lo_bit, a.hi_bit, passes, i + 1, &sh, &b);
+        p.clear_radix = pass_radix(b);
+    }
     p.tile_counter = a.tile_counters + i;
     p.err = a.err;
-    p.shift = a.lo_bit + i * kRadixBits;
-    p.bits = a.hi_bit - p.shift < kRadixBits ? a.hi_bit - p.shift : kRadixBits;
     p.seg_offsets = i == 0 ? a.seg_offsets : nullptr;
     p.seg_count = a.seg_count;
     p.seg_shift = a.seg_shift;
@@ -445,26 +687,47 @@ static PassParams pass_params(const SortArgs& a, int i) {
 void launch_sort_histogram(const SortArgs& a, cudaStream_t s) {
     // The histogram pass also validates the key range, so it runs even when
     // there is no digit to sort.
-    launch_pdl(radix_histogram, dim3(a.grid_hist), dim3(kSortThreads), 0, s, a.keys_in, a.d_n, a.n, a.lo_bit, a.hi_bit,
-                                                         a.validate_bits, a.hist, a.status[0], a.err,
-                                                         a.seg_offsets, a.seg_count, a.seg_shift, a.gate,
-                                                         a.gate_run);
-    if (sort_passes(a.lo_bit, a.hi_bit) == 0)
-        launch_pdl(copy_keys, dim3(a.grid_hist), dim3(256), 0, s, a.keys_in, a.keys_out, a.vals_in, a.vals_out, a.with_values,
-                                              a.d_n, a.n, a.gate, a.gate_run);
+    const int passes = sort_plan_passes(a);
+    HistParams h{};
+    h.keys = a.keys_in;
+    h.d_n = a.d_n;
+    h.n_host = a.n;
+    h.lo_bit = a.lo_bit;
+    h.hi_bit = a.hi_bit;
+    h.passes = passes;
+    h.stride = pass_hist_stride(a.lo_bit, a.hi_bit, passes);
+    h.validate_bits = a.validate_bits;
+    h.hist = a.hist;
+    h.status0 = a.status[0];
+    h.first_tile = kPassThreads * sort_shape_items(a.shape, a.with_values);
+    h.first_radix = 0;
+    if (passes) {
+        int sh, b;
+        pass_digit(a.lo_bit, a.hi_bit, passes, 0, &sh, &b);
+        h.first_radix = pass_radix(b);
+    }
+    h.err = a.err;
+    h.seg_offsets = a.seg_offsets;
+    h.seg_count = a.seg_count;
+    h.seg_shift = a.seg_shift;
+    h.gate = a.gate;
+    h.gate_run = a.gate_run;
+    launch_pdl(radix_histogram, dim3(a.grid_hist), dim3(kSortThreads), 0, s, h);
+    if (passes == 0)
+        launch_pdl(copy_keys, dim3(a.grid_hist), dim3(256), 0, s, a.keys_in, a.keys_out, a.vals_in, a.vals_out,
+                   a.with_values, a.d_n, a.n, a.gate, a.gate_run);
 }
 
 void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
     const PassParams p = pass_params(a, i);
-    const ShapeEntry& e = kShapes[a.shape < 0 || a.shape >= kNumSortShapes ? 1 : a.shape];
+    const PassKernel& k = pass_kernel(a.shape, a.with_values, p.bits);
     void* args[] = {const_cast<PassParams*>(&p)};
-    launch_pdl_c(a.with_values ? (const void*)e.pairs : (const void*)e.keys, dim3(a.grid_pass), dim3(kPassThreads),
-                 args, a.with_values ? e.smem_pairs : e.smem_keys, s);
+    launch_pdl_c((const void*)k.fn, dim3(a.grid_pass), dim3(kPassThreads), args, k.smem, s);
 }
 
 void launch_sort(const SortArgs& a, cudaStream_t s) {
     launch_sort_histogram(a, s);
-    for (int i = 0; i < sort_passes(a.lo_bit, a.hi_bit); ++i) launch_sort_pass(a, i, s);
+    for (int i = 0; i < sort_plan_passes(a); ++i) launch_sort_pass(a, i, s);
 }
 
 }  // namespace dagc

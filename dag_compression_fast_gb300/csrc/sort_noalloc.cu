@@ -36,7 +36,7 @@ namespace {
 
 constexpr uint64_t kNoAllocMaxKeys = 1ull << 20;  // 1,048,576 uint64 keys per call
 constexpr uint64_t kNoAllocTiles = (kNoAllocMaxKeys + kSortTile - 1) / kSortTile;
-constexpr int kNoAllocShape = 5;  // digit-pass shape used for these sorts
+constexpr int kNoAllocShape = 0;  // keys-only digit-pass shape used for these sorts (8-bit digits)
 constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch {
@@ -81,7 +81,7 @@ int setup_current_device(DeviceSetup* out) {
             return DAGC_ERR_CUDA;
         }
         d.sms = sms;
-        d.occ_pass = occupancy_sort_shape(kNoAllocShape, false);
+        d.occ_pass = occupancy_sort_shape(kNoAllocShape, false, kRadixBits);
         if (d.occ_pass < 1) d.occ_pass = 1;
         d.scratch = p;
     }
@@ -128,12 +128,14 @@ extern "C" int dagc_sort_keys_noalloc(const uint64_t* d_in, uint64_t* d_out, uin
     a.status[1] = S->status[1];
     a.tile_counters = S->tile_counters;
     a.err = &S->err;
-    const uint64_t tiles = (n + 256ull * sort_shape_items(kNoAllocShape) - 1) / (256ull * sort_shape_items(kNoAllocShape));
+    const uint64_t tile = 256ull * sort_shape_items(kNoAllocShape, false);
+    const uint64_t tiles = (n + tile - 1) / tile;
     const uint64_t resident = (uint64_t)dev.occ_pass * (uint64_t)dev.sms;
     a.grid_pass = (int)(tiles < resident ? tiles : resident);
     const uint64_t hist_blocks = (n + 4095) / 4096, hist_cap = 8ull * (uint64_t)dev.sms;
     a.grid_hist = (int)(hist_blocks < hist_cap ? hist_blocks : hist_cap);
     a.shape = kNoAllocShape;
+    a.radix_bits = kRadixBits;
     launch_sort(a, s);
     if (cudaGetLastError() != cudaSuccess) return DAGC_ERR_CUDA;
     uint32_t err = 0;

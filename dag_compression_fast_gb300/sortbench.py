@@ -45,7 +45,8 @@ def run(ctx, n: int, lo: int, hi: int, reps: int, seed: int = 1, pairs: bool = F
     e1.record(s)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / reps
-    passes = (hi - lo + 7) // 8
+    shape, bits = ctx.sort_plan(n, lo, hi, pairs)
+    passes = (hi - lo + bits - 1) // bits
     kv = 12 if pairs else 8
     bytes_ = 8 * n + passes * 2 * kv * n
     return n / sec / 1e9, bytes_ / sec / 1e9
@@ -57,7 +58,8 @@ def main(argv=None):
     p.add_argument("--lo", type=int, default=6)
     p.add_argument("--hi", type=int, default=33)
     p.add_argument("--reps", type=int, default=5)
-    p.add_argument("--sweep", choices=["none", "bits", "n", "shapes"], default="none")
+    p.add_argument("--sweep", choices=["none", "bits", "n", "shapes", "plans"], default="none")
+    p.add_argument("--radix-bits", type=int, default=-1, help="widest digit of keys-only sorts (8..11)")
     p.add_argument("--pairs", action="store_true", help="key/value pairs (values = input positions)")
     p.add_argument("--shape", type=int, default=-1, help="digit-pass kernel shape (dagc_set_option)")
     a = p.parse_args(argv)
@@ -66,8 +68,21 @@ def main(argv=None):
     opt = D.OPT_SORT_SHAPE_PAIRS if a.pairs else D.OPT_SORT_SHAPE_KEYS
     if a.shape >= 0:
         ctx.set_option(opt, a.shape)
-    if a.sweep == "shapes":
-        for sh in range(D.NUM_SORT_SHAPES):
+    if a.radix_bits >= 0:
+        ctx.set_option(D.OPT_SORT_RADIX_BITS, a.radix_bits)
+    if a.sweep == "plans":
+        # every keys-only shape at every digit width: shape;bits;passes;keys;G keys/s;GB/s
+        for sh in range(D.NUM_KEY_SHAPES):
+            for rb in D.RADIX_BITS:
+                ctx.set_option(D.OPT_SORT_SHAPE_KEYS, sh)
+                ctx.set_option(D.OPT_SORT_RADIX_BITS, rb)
+                if ctx.sort_plan(a.n, a.lo, a.hi) != (sh, rb):
+                    continue  # not a valid plan for this range
+                gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps)
+                print(f"plan shape={sh} bits={rb};passes={(a.hi - a.lo + rb - 1) // rb};{a.n};{gk:.3f};{gb:.1f}",
+                      flush=True)
+    elif a.sweep == "shapes":
+        for sh in range(D.NUM_PAIR_SHAPES if a.pairs else D.NUM_KEY_SHAPES):
             ctx.set_option(opt, sh)
             gk, gb = run(ctx, a.n, a.lo, a.hi, a.reps, pairs=a.pairs)
             print(f"shape={sh};{'pairs' if a.pairs else 'keys'};{a.hi - a.lo};{a.n};{gk:.3f};{gb:.1f}", flush=True)

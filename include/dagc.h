@@ -153,13 +153,21 @@ int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int
 int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
 
 /* ------------------------------------------------------------ options ---- */
-/* Kernel-shape options (the autotuner's knobs). Shapes of the digit-pass
- * kernel, as (keys per thread, resident CTAs per SM, equal-digit matching by
- * ballots / match.any / alternating): 0 = (16, 2, ballot), 1 = (16, 3, ballot),
- * 2 = (12, 3, ballot), 3 = (8, 4, ballot), 4 = (16, 3, match),
- * 5 = (16, 3, alternate), 6 = (16, 2, alternate), 7 = (12, 3, alternate). */
+/* Digit-pass plans (the autotuner's knobs). A plan is a kernel shape, as
+ * (keys per thread, minimum resident CTAs per SM, equal-digit matching by
+ * ballots / match.any / alternating), and the widest digit of the sort.
+ * Keys-only shapes (each built for 8- to 11-bit digits): 0 = (16, 3,
+ * alternate), 1 = (16, 2, alternate), 2 = (16, 4, alternate), 3 = (12, 4,
+ * alternate), 4 = (16, 3, ballot), 5 = (16, 3, match). Key/value shapes
+ * (8-bit digits): 0 = (16, 2, ballot), 1 = (16, 3, ballot), 2 = (12, 3,
+ * ballot), 3 = (8, 4, ballot), 4 = (16, 3, match), 5 = (16, 3, alternate),
+ * 6 = (16, 2, alternate), 7 = (12, 3, alternate). Value -1 (default): each
+ * sort takes the plan of its class from the context's tuning table (see
+ * dagc_tune_sort), else keys (0, 8 bits) and pairs (3, 8 bits). Setting any
+ * of these forces it for every sort of its kind. */
 #define DAGC_OPT_SORT_SHAPE_KEYS 1   /* keys-only sorts (the fragment sort) */
 #define DAGC_OPT_SORT_SHAPE_PAIRS 2  /* key/value sorts (leaf and node hashes) */
+#define DAGC_OPT_SORT_RADIX_BITS 8   /* widest digit of keys-only sorts: 8..11, or -1 */
 /* 1 (default): launch a CreateDAG kernel sequence directly the first time its
  * input pointer, size and depth are seen, record it as a CUDA graph the second
  * time and replay the graph for later calls with the same shape (recording
@@ -230,6 +238,28 @@ int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint
 int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out,
                     const uint32_t* d_vals_in, uint32_t* d_vals_out, uint64_t n, int lo_bit,
                     int hi_bit, void* stream);
+
+/* ----------------------------------------------------------- autotuner ---- */
+/* No counterpart in the reference, whose sort takes CUB's static per-arch
+ * policy (src/cub/device/dispatch/dispatch_radix_sort.cuh:700-724). Sorts are
+ * grouped in classes: keys-only or key/value, number of sorted bits, and the
+ * key count's power of two. dagc_tune_sort times every valid plan (shape x
+ * digit width, wider digits only where they save a pass) of one class on
+ * n pseudo-random keys on this context's device, `reps` sorts each after one
+ * untimed sort, and stores the fastest in the context's tuning table (later
+ * sorts of the class use it); it reports that plan, its time per sort and
+ * the default plan's. dagc_tune_save / dagc_tune_load write / read the table
+ * as JSON. At creation a context loads the file named by the environment
+ * variable DAGC_TUNE_FILE (empty: none), else sort_plans.json one directory
+ * above the library, if it exists. dagc_sort_plan reports the plan a sort of
+ * the given class would take. */
+int dagc_tune_sort(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int with_values, int reps,
+                   int* best_shape, int* best_radix_bits, double* best_ms, double* default_ms);
+int dagc_tune_save(dagc_context ctx, const char* path);
+int dagc_tune_load(dagc_context ctx, const char* path);
+int dagc_tune_clear(dagc_context ctx);
+int dagc_sort_plan(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int with_values, int* shape,
+                   int* radix_bits);
 
 /* ------------------------------------------------------------ .dag.bin ---- */
 /* The reference's final-DAG file (src/Serializer.h:10-100, used at
