@@ -35,6 +35,9 @@ OPT_DEDUP_UNIQUE_LIMIT = 5
 OPT_GROUP = 6
 OPT_PDL = 7
 OPT_SORT_RADIX_BITS = 8
+OPT_TEST_SPIN_LIMIT = 9
+OPT_TEST_STALL_LOOKBACK = 10
+OPT_TEST_FAIL_ALLOCS = 11
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
 NUM_KEY_SHAPES = 6
@@ -60,12 +63,13 @@ DAGC_SYMBOLS = [
     "dagc_dag_free", "dagc_create_footprint",
     "dagc_merge", "dagc_final", "dagc_free_words", "dagc_words_download", "dagc_free_all",
     "dagc_compress_host",
-    "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats",
+    "dagc_compress", "dagc_file_write", "dagc_file_read", "dagc_memory_stats", "dagc_memory_events", "dagc_memory_report",
     "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_voxelize", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_tune_sort", "dagc_tune_save", "dagc_tune_load", "dagc_tune_clear", "dagc_sort_plan",
     "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
-    "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_destroy",
+    "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_folds", "dagc_server_timeline", "dagc_server_set_option",
+    "dagc_server_destroy", "dagc_union", "dagc_dag_lift",
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
@@ -128,6 +132,11 @@ def lib() -> ctypes.CDLL:
         L.dagc_server_wait.argtypes = [vp, u64, vp, u64, pu64, ctypes.POINTER(ctypes.c_double)]
         L.dagc_server_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
         L.dagc_server_shared_dag.argtypes = [vp, i32, pvp, pvp]
+        L.dagc_server_folds.argtypes = [vp, pu64]
+        L.dagc_server_set_option.argtypes = [vp, i32, i32]
+        L.dagc_server_timeline.argtypes = [vp, u64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.dagc_union.argtypes = [vp, vp, u64, vp, pvp, vp]
+        L.dagc_dag_lift.argtypes = [vp, vp, vp, u64, vp, pvp]
         L.dagc_server_destroy.argtypes = [vp]
         L.dagc_server_destroy.restype = None
         L.dagc_dag_free.argtypes = [vp]
@@ -148,6 +157,8 @@ def lib() -> ctypes.CDLL:
         L.dagc_file_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, vp, u64]
         L.dagc_file_read.argtypes = [ctypes.c_char_p, vp, ctypes.POINTER(ctypes.c_uint32), vp, u64, pu64]
         L.dagc_memory_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
+        L.dagc_memory_events.argtypes = [vp, pu64, pu64]
+        L.dagc_memory_report.argtypes = [vp, vp, u64, pu64]
         L.dagc_set_option.argtypes = [vp, i32, i32]
         L.dagc_profile_enable.argtypes = [vp, i32]
         L.dagc_profile_reset.argtypes = [vp]
@@ -469,6 +480,23 @@ class Context:
         self._check(st)
         return Dag(self, out.value)
 
+    def union_dags(self, dags, stream=None):
+        """Per-level union of DAGs of equal depth (dagc_union): (DAG, root hashes)."""
+        arr = (ctypes.c_void_p * len(dags))(*[d._live() for d in dags])
+        roots = np.zeros(len(dags), np.uint64)
+        out = ctypes.c_void_p()
+        self._check(lib().dagc_union(self.handle, arr, len(dags), _stream_handle(stream), ctypes.byref(out),
+                                     roots.ctypes.data))
+        return Dag(self, out.value), roots
+
+    def lift_dag(self, body: "Dag", slot_root_hashes, stream=None) -> Dag:
+        """The DAG over 8^m chunk slots whose roots are in `body` (dagc_dag_lift)."""
+        h = np.ascontiguousarray(slot_root_hashes, np.uint64)
+        out = ctypes.c_void_p()
+        self._check(lib().dagc_dag_lift(self.handle, body._live(), h.ctypes.data, h.size, _stream_handle(stream),
+                                        ctypes.byref(out)))
+        return Dag(self, out.value)
+
     def free_all(self):
         """DAGCompression::FreeAll."""
         self._check(lib().dagc_free_all(self.handle))
@@ -503,6 +531,21 @@ class Context:
         v = [ctypes.c_uint64(0) for _ in range(4)]
         self._check(lib().dagc_memory_stats(self.handle, *[ctypes.byref(x) for x in v]))
         return dict(zip(["in_use", "peak", "cached", "arena"], [x.value for x in v]))
+
+    def memory_report(self) -> str:
+        """The context's device memory by allocation name (dagc_memory_report)."""
+        need = ctypes.c_uint64(0)
+        self._check(lib().dagc_memory_report(self.handle, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self._check(lib().dagc_memory_report(self.handle, buf, need.value, ctypes.byref(need)))
+        return buf.value.decode()
+
+    def memory_events(self):
+        """Failed device allocations (injected or real) and allocations that
+        succeeded on their retry (dagc_memory_events)."""
+        f, r = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._check(lib().dagc_memory_events(self.handle, ctypes.byref(f), ctypes.byref(r)))
+        return {"alloc_failures": f.value, "retries_ok": r.value}
 
     def trace(self, words, depth: int, params: TraceParams, hits: bool = True, stream=None):
         """Headless FDAGTracer::ResolvePaths: traces the final DAG (a Words
@@ -667,6 +710,26 @@ class Server:
         c, f, m, p = (ctypes.c_uint64(0) for _ in range(4))
         lib().dagc_server_stats(self.handle, ctypes.byref(c), ctypes.byref(f), ctypes.byref(m), ctypes.byref(p))
         return {"completed": c.value, "fragments": f.value, "max_concurrent": m.value, "peak_footprint": p.value}
+
+    def set_option(self, option: int, value: int):
+        """dagc_set_option on every worker slot's context."""
+        st = lib().dagc_server_set_option(self.handle, option, value)
+        if st:
+            raise DagcError(st, "dagc_server_set_option failed")
+
+    def folds(self) -> int:
+        """Unions of finished chunks into the resident shared DAG so far."""
+        v = ctypes.c_uint64(0)
+        lib().dagc_server_folds(self.handle, ctypes.byref(v))
+        return v.value
+
+    def timeline(self, ticket: int):
+        """(gpu_start_ms, gpu_end_ms) of a finished job's device work."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        st = lib().dagc_server_timeline(self.handle, ticket, ctypes.byref(a), ctypes.byref(b))
+        if st:
+            raise DagcError(st, "no timeline for this ticket")
+        return a.value, b.value
 
     def shared_dag(self, top_levels: int) -> Dag:
         """Merges every chunk job so far into one device DAG."""

@@ -63,36 +63,58 @@ static_assert(kCntSlots <= kCntOverflow, "count slots");
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Device allocations of a context go through here: a test hook can make the
+// next `inject` of them fail as cudaMalloc does when the device is full
+// (cudaErrorMemoryAllocation), without touching the device.
+struct AllocStats {
+    int inject = 0;             // allocations still to fail (test hook)
+    uint64_t failures = 0;      // failed attempts, injected or real
+    uint64_t retries_ok = 0;    // allocations that succeeded on their retry
+};
+inline cudaError_t dev_malloc(void** p, size_t bytes, AllocStats* st) {
+    if (st && st->inject > 0) {
+        --st->inject;
+        ++st->failures;
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess && st) ++st->failures;
+    return e;
+}
+
 // Best-fit cache of device blocks (the reference's FPool): freed blocks are
 // kept and reused; on cudaMalloc failure the cache is released and the
 // allocation retried once (the OOM fallback of src/Memory.cpp:56-70).
 class DevicePool {
 public:
+    AllocStats* stats = nullptr;
     ~DevicePool() {
         trim();
         for (cudaEvent_t e : spare_events_) cudaEventDestroy(e);
     }
-    cudaError_t alloc(void** p, size_t bytes) {
+    cudaError_t alloc(void** p, size_t bytes, const char* name = "block") {
         reclaim();
         bytes = align_up(std::max<size_t>(bytes, 1), 512);
         auto it = free_.lower_bound(bytes);
         if (it != free_.end() && it->first <= 2 * bytes + (4u << 20)) {
             *p = it->second;
-            live_[*p] = it->first;
+            live_[*p] = {it->first, name};
             cached_ -= it->first;
             in_use_ += it->first;
             free_.erase(it);
             peak_ = std::max(peak_, in_use_);
             return cudaSuccess;
         }
-        cudaError_t e = cudaMalloc(p, bytes);
+        cudaError_t e = dev_malloc(p, bytes, stats);
         if (e == cudaErrorMemoryAllocation) {
             cudaGetLastError();
             trim();
-            e = cudaMalloc(p, bytes);
+            e = dev_malloc(p, bytes, stats);
+            if (e == cudaSuccess && stats) ++stats->retries_ok;
         }
         if (e != cudaSuccess) { cudaGetLastError(); *p = nullptr; return e; }
-        live_[*p] = bytes;
+        live_[*p] = {bytes, name};
         in_use_ += bytes;
         peak_ = std::max(peak_, in_use_);
         return cudaSuccess;
@@ -101,10 +123,23 @@ public:
         if (!p) return;
         auto it = live_.find(p);
         if (it == live_.end()) return;
-        free_.emplace(it->second, p);
-        cached_ += it->second;
-        in_use_ -= it->second;
+        free_.emplace(it->second.first, p);
+        cached_ += it->second.first;
+        in_use_ -= it->second.first;
         live_.erase(it);
+    }
+    // Bytes and block count of the live blocks by name, and of the cache.
+    void tally(std::map<std::string, std::pair<uint64_t, uint64_t>>& m) const {
+        for (const auto& kv : live_) {
+            auto& e = m[kv.second.second];
+            e.first += kv.second.first;
+            ++e.second;
+        }
+        for (const auto& kv : free_) {
+            auto& e = m["cached for reuse"];
+            e.first += kv.first;
+            ++e.second;
+        }
     }
     // Returns a block once the work queued on `s` so far has completed (work
     // that may still read it): an event is recorded on `s` and the block is
@@ -167,7 +202,7 @@ private:
         cudaEvent_t e;
     };
     std::multimap<size_t, void*> free_;
-    std::unordered_map<void*, size_t> live_;
+    std::unordered_map<void*, std::pair<size_t, const char*>> live_;
     std::vector<Deferred> deferred_;
     std::vector<cudaEvent_t> spare_events_;
     size_t in_use_ = 0, cached_ = 0, peak_ = 0;
@@ -177,17 +212,21 @@ private:
 struct Arena {
     void* base = nullptr;
     size_t cap = 0;
+    AllocStats* stats = nullptr;
+    // Grows to at least `bytes` (with 25% headroom; without it when that
+    // does not fit).
     cudaError_t reserve(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
         if (base) cudaFree(base);
         base = nullptr;
         cap = 0;
         const size_t want = align_up(bytes + bytes / 4, 1u << 21);
-        cudaError_t e = cudaMalloc(&base, want);
+        cudaError_t e = dev_malloc(&base, want, stats);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            e = cudaMalloc(&base, align_up(bytes, 1u << 21));
+            e = dev_malloc(&base, align_up(bytes, 1u << 21), stats);
             if (e != cudaSuccess) { cudaGetLastError(); base = nullptr; return e; }
+            if (stats) ++stats->retries_ok;
             cap = align_up(bytes, 1u << 21);
             return cudaSuccess;
         }
@@ -293,8 +332,11 @@ struct dagc_context_t {
     int sms = 152;
     int grid_hist = 0, grid_pass_kv = 0, grid_pass_k = 0;
     int grid_leaf = 0, grid_extract = 0, grid_unique = 0, grid_scan = 0, grid_write = 0;
+    AllocStats alloc_stats;
     DevicePool pool;
     Arena arena;
+    uint32_t test_spin_limit = 0;  // DAGC_OPT_TEST_SPIN_LIMIT (0: kSpinLimit)
+    int test_stall = 0;            // DAGC_OPT_TEST_STALL_LOOKBACK
     // Dedup table: keys (0 = empty), then aux words; every level leaves its
     // keys zero; after a call that stopped early it is cleared. Grouping
     // scratch (kGroupScratchBytes): the brick masks.
@@ -549,6 +591,8 @@ int run_sort(dagc_context ctx, CallSlots& cs, const SortBuffers& sb, const uint6
     a.status[1] = sb.status[1];
     a.tile_counters = cs.counters(kMaxPasses);
     a.err = &cs.h->err;
+    a.spin_limit = ctx->test_spin_limit;
+    a.stall_first_tile = ctx->test_stall;
     const uint64_t tiles = sort_tiles(n_bound);
     a.grid_hist = grid_for(ctx->grid_hist / std::max(ctx->sms, 1), ctx->sms, (n_bound + 4095) / 4096);
     const SortChoice plan = sort_plan_for(ctx, with_values, lo, hi, n_bound);
@@ -602,7 +646,7 @@ int alloc_dag(dagc_context ctx, int num_levels, const std::vector<uint64_t>& lev
     const size_t o_o = L.take<uint64_t>(num_levels + 1);
     const size_t o_m = L.take<uint8_t>(nn);
     void* block = nullptr;
-    DAGC_CUDA(ctx, ctx->pool.alloc(&block, L.off));
+    DAGC_CUDA(ctx, ctx->pool.alloc(&block, L.off, "DAG (levels + leaves)"));
     char* b = static_cast<char*>(block);
     d->block = block;
     d->hashes = reinterpret_cast<uint64_t*>(b + o_h);
@@ -1356,7 +1400,7 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     } else {
         DAGC_CUDA(ctx, cudaMemsetAsync(pos, 0, 4, s));
     }
-    DAGC_CUDA(ctx, ctx->pool.alloc(&w, (by_bound ? bound : node_words + 2 * d->num_leaves) * 4));
+    DAGC_CUDA(ctx, ctx->pool.alloc(&w, (by_bound ? bound : node_words + 2 * d->num_leaves) * 4, "final DAG words"));
     a.words = static_cast<uint32_t*>(w);
     launch_final_write(a, s);
     ++ctx->launches;
@@ -1387,11 +1431,17 @@ struct HostNode {
     uint32_t ch[8];
 };
 
-int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_dag* out) {
+// union_only: the per-level union of any number k >= 1 of DAGs of equal depth
+// (no levels added; the result's top level holds every input's root), and
+// each input's root hash in root_hash_out (0 for an empty input). Otherwise
+// MergeDAGs: k = 8^m inputs in Morton order, m levels built above them.
+int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_dag* out, bool union_only = false,
+               std::vector<uint64_t>* root_hash_out = nullptr) {
     t_pdl = ctx->pdl;
     const int nl = in[0]->num_levels;
     int m = 0;
-    for (uint64_t x = k; x > 1; x /= 8) ++m;
+    if (!union_only)
+        for (uint64_t x = k; x > 1; x /= 8) ++m;
     uint64_t total_leaves = 0;
     std::vector<uint64_t> level_total(nl, 0);
     for (uint64_t i = 0; i < k; ++i) {
@@ -1399,7 +1449,10 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         for (int l = 0; l < nl; ++l) level_total[l] += in[i]->level_offset[l + 1] - in[i]->level_offset[l];
     }
     const int out_levels = nl + m;
-    if (total_leaves == 0) return empty_dag(ctx, out_levels, out);
+    if (total_leaves == 0) {
+        if (root_hash_out) root_hash_out->assign(k, 0);
+        return empty_dag(ctx, out_levels, out);
+    }
     uint64_t capmax = total_leaves;
     for (int l = 0; l < nl; ++l) capmax = std::max(capmax, level_total[l]);
     if (capmax > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "merged level too large");
@@ -1546,11 +1599,12 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
         root_uid[i] = stage_uid[i];
         root_hash[i] = stage_hash[i];
     }
+    if (root_hash_out) *root_hash_out = root_hash;
 
     // Top levels: groups of 8 consecutive roots, built on the host like the
     // reference (src/DAGCompression.cu:1504-1533), deduplicated by hash.
     std::vector<std::vector<HostNode>> top;  // top[0] = just above the inputs
-    uint64_t groups = k;
+    uint64_t groups = union_only ? 1 : k;
     while (groups > 1) {
         const uint64_t ng = groups / 8;
         std::vector<HostNode> cand;
@@ -1631,6 +1685,114 @@ int merge_dags(dagc_context ctx, dagc_dag* in, uint64_t k, cudaStream_t s, dagc_
     return DAGC_OK;
 }
 
+// The DAG of a grid of 8^top chunk slots over a union `body` of chunk DAGs
+// (its top level holds the chunk roots): slot i holds the chunk whose root
+// hash is slot_hash[i] (0: empty). The top levels are built on the host by
+// groups of 8 slots in Morton order, as MergeDAGs does
+// (src/DAGCompression.cu:1504-1533); the body's levels are copied below them.
+int lift_dag(dagc_context ctx, dagc_dag body, const uint64_t* slot_hash, uint64_t slots, cudaStream_t s,
+             dagc_dag* out) {
+    int m = 0;
+    for (uint64_t x = slots; x > 1; x /= 8) ++m;
+    const int nl = body->num_levels;
+    // The roots in the body: their hashes, ascending (level 0 of a union).
+    std::vector<uint64_t> roots;
+    const uint64_t nroot = nl > 0 ? body->level_offset[1] : body->num_leaves;
+    if (nroot) {
+        roots.resize(nroot);
+        dag_ready_sync(body);
+        DAGC_CUDA(ctx, cudaMemcpy(roots.data(), nl > 0 ? body->hashes : body->leaves, nroot * 8, cudaMemcpyDeviceToHost));
+    }
+    std::vector<uint64_t> root_hash(slot_hash, slot_hash + slots);
+    std::vector<uint32_t> root_uid(slots, kEmptyChild);
+    bool any = false;
+    for (uint64_t i = 0; i < slots; ++i) {
+        if (!root_hash[i]) continue;
+        auto it = std::lower_bound(roots.begin(), roots.end(), root_hash[i]);
+        if (it == roots.end() || *it != root_hash[i]) return set_error(ctx, DAGC_ERR_BAD_INPUT, "chunk root missing from the body");
+        root_uid[i] = (uint32_t)(it - roots.begin());
+        any = true;
+    }
+    const int out_levels = nl + m;
+    if (!any) return empty_dag(ctx, out_levels, out);
+    std::vector<std::vector<HostNode>> top;
+    uint64_t groups = slots;
+    while (groups > 1) {
+        const uint64_t ng = groups / 8;
+        std::vector<HostNode> cand;
+        std::vector<int64_t> cand_of(ng, -1);
+        for (uint64_t g = 0; g < ng; ++g) {
+            HostNode nd{};
+            uint64_t hs[8];
+            for (int c = 0; c < 8; ++c) {
+                hs[c] = root_hash[8 * g + c];
+                nd.ch[c] = root_uid[8 * g + c];
+                if (hs[c]) nd.mask |= (uint8_t)(1u << c);
+            }
+            nd.hash = hash_children(hs);
+            if (nd.mask) { cand_of[g] = (int64_t)cand.size(); cand.push_back(nd); }
+        }
+        std::vector<uint32_t> order(cand.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (uint32_t)i;
+        std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return cand[a].hash < cand[c].hash; });
+        std::vector<HostNode> lvl;
+        std::vector<uint32_t> uid_of(cand.size());
+        for (size_t i = 0; i < order.size(); ++i) {
+            const HostNode& nd = cand[order[i]];
+            if (lvl.empty() || lvl.back().hash != nd.hash) lvl.push_back(nd);
+            else if (lvl.back().mask != nd.mask || std::memcmp(lvl.back().ch, nd.ch, 32) != 0)
+                return set_error(ctx, DAGC_ERR_HASH_COLLISION, "64-bit node hash collision between different nodes");
+            uid_of[order[i]] = (uint32_t)(lvl.size() - 1);
+        }
+        std::vector<uint64_t> nh(ng, 0);
+        std::vector<uint32_t> nu(ng, kEmptyChild);
+        for (uint64_t g = 0; g < ng; ++g)
+            if (cand_of[g] >= 0) { nh[g] = cand[cand_of[g]].hash; nu[g] = uid_of[cand_of[g]]; }
+        root_hash = nh;
+        root_uid = nu;
+        top.push_back(std::move(lvl));
+        groups = ng;
+    }
+    // Nodes of the body no slot reaches stay in it (a union of exactly the
+    // slots' chunks has none).
+    std::vector<uint64_t> sizes(out_levels);
+    for (int t = 0; t < m; ++t) sizes[t] = top[m - 1 - t].size();
+    for (int l = 0; l < nl; ++l) sizes[m + l] = body->level_offset[l + 1] - body->level_offset[l];
+    dagc_dag d = nullptr;
+    int st = alloc_dag(ctx, out_levels, sizes, body->num_leaves, &d);
+    if (st) return st;
+    std::vector<uint64_t> th;
+    std::vector<uint8_t> tm;
+    std::vector<uint32_t> tc;
+    for (int t = 0; t < m; ++t) {
+        for (const HostNode& nd : top[m - 1 - t]) {
+            th.push_back(nd.hash);
+            tm.push_back(nd.mask);
+            tc.insert(tc.end(), nd.ch, nd.ch + 8);
+        }
+    }
+    const uint64_t ntop = th.size(), nbody = body->num_nodes();
+    cudaError_t ce = cudaSuccess;
+    if (ntop) {
+        ce = cudaMemcpyAsync(d->hashes, th.data(), ntop * 8, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->children, tc.data(), ntop * 32, cudaMemcpyHostToDevice, s);
+        if (!ce) ce = cudaMemcpyAsync(d->masks, tm.data(), ntop, cudaMemcpyHostToDevice, s);
+    }
+    if (!ce && nbody) ce = cudaMemcpyAsync(d->hashes + ntop, body->hashes, nbody * 8, cudaMemcpyDeviceToDevice, s);
+    if (!ce && nbody) ce = cudaMemcpyAsync(d->children + ntop * 8, body->children, nbody * 32, cudaMemcpyDeviceToDevice, s);
+    if (!ce && nbody) ce = cudaMemcpyAsync(d->masks + ntop, body->masks, nbody, cudaMemcpyDeviceToDevice, s);
+    if (!ce && d->num_leaves) ce = cudaMemcpyAsync(d->leaves, body->leaves, d->num_leaves * 8, cudaMemcpyDeviceToDevice, s);
+    if (!ce) ce = cudaMemcpyAsync(d->d_level_offset, d->level_offset.data(), (out_levels + 1) * 8, cudaMemcpyHostToDevice, s);
+    if (!ce) ce = cudaStreamSynchronize(s);
+    if (ce) {
+        free_dag(d);
+        cudaGetLastError();
+        return set_error(ctx, cuda_status(ce), std::string("lift: ") + cudaGetErrorString(ce));
+    }
+    *out = d;
+    return DAGC_OK;
+}
+
 bool valid_ctx(dagc_context ctx) { return ctx != nullptr; }
 
 }  // namespace
@@ -1663,6 +1825,8 @@ int dagc_context_create(int device, dagc_context* out) {
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
     std::unique_ptr<dagc_context_t> c(new dagc_context_t);
     c->device = device;
+    c->pool.stats = &c->alloc_stats;
+    c->arena.stats = &c->alloc_stats;
     cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     sort_configure();
     kernels_configure();
@@ -1976,6 +2140,38 @@ int dagc_merge(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_
     return DAGC_OK;
 }
 
+int dagc_union(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_dag* out, uint64_t* root_hashes) {
+    if (!valid_ctx(ctx) || !dags || !out || k == 0) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    for (uint64_t i = 0; i < k; ++i) {
+        if (!dags[i]) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null DAG");
+        if (dags[i]->num_levels != dags[0]->num_levels) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depths differ");
+    }
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<uint64_t> rh;
+    const int st = merge_dags(ctx, dags, k, static_cast<cudaStream_t>(stream), out, true, &rh);
+    if (st) return st;
+    if (root_hashes)
+        for (uint64_t i = 0; i < k; ++i) root_hashes[i] = i < rh.size() ? rh[i] : 0;
+    return DAGC_OK;
+}
+
+int dagc_dag_lift(dagc_context ctx, dagc_dag body, const uint64_t* slot_root_hashes, uint64_t slots, void* stream,
+                  dagc_dag* out) {
+    if (!valid_ctx(ctx) || !body || !out || !slot_root_hashes || slots == 0) return DAGC_ERR_INVALID_ARGUMENT;
+    uint64_t x = slots;
+    while (x % 8 == 0) x /= 8;
+    if (x != 1) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "slot count must be a power of 8");
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    *out = nullptr;
+    DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+    int m = 0;
+    for (uint64_t y = slots; y > 1; y /= 8) ++m;
+    if (body->num_levels + m + 2 > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "result deeper than 21");
+    return lift_dag(ctx, body, slot_root_hashes, slots, static_cast<cudaStream_t>(stream), out);
+}
+
 int dagc_final(dagc_context ctx, dagc_dag dag, void* stream, uint32_t** d_words, uint64_t* n_words) {
     if (!valid_ctx(ctx) || !dag || !d_words || !n_words || dag->ctx != ctx) return DAGC_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lock(ctx->mu);
@@ -2040,7 +2236,7 @@ int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n
         std::lock_guard<std::mutex> lock(ctx->mu);
         DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
         if (n) {
-            DAGC_CUDA(ctx, ctx->pool.alloc(&d_in, n * 8));
+            DAGC_CUDA(ctx, ctx->pool.alloc(&d_in, n * 8, "staged fragments"));
             const cudaError_t e = cudaMemcpyAsync(d_in, h_fragments, n * 8, cudaMemcpyHostToDevice, s);
             if (e != cudaSuccess) { ctx->pool.release(d_in); DAGC_CUDA(ctx, e); }
         }
@@ -2100,6 +2296,19 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
             if (value < 0 || value > 2) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "group mode must be 0, 1 or 2");
             ctx->group_mode = value;
             return DAGC_OK;
+        case DAGC_OPT_TEST_SPIN_LIMIT:
+            if (value < 0) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "spin limit must be >= 0");
+            ctx->test_spin_limit = (uint32_t)value;
+            ++ctx->tune_version;  // recorded graphs carry the old value
+            return DAGC_OK;
+        case DAGC_OPT_TEST_STALL_LOOKBACK:
+            ctx->test_stall = value != 0;
+            ++ctx->tune_version;
+            return DAGC_OK;
+        case DAGC_OPT_TEST_FAIL_ALLOCS:
+            if (value < 0) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "count must be >= 0");
+            ctx->alloc_stats.inject = value;
+            return DAGC_OK;
         case DAGC_OPT_DEDUP_UNIQUE_LIMIT:
             if (value < 1) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "limit must be positive");
             ctx->dedup_unique_limit = (uint64_t)value;
@@ -2131,6 +2340,47 @@ int dagc_profile_read(dagc_context ctx, int stage, double* ms, uint64_t* launche
     if (ms) *ms = st.ms;
     if (launches) *launches = st.launches;
     if (bytes) *bytes = st.bytes;
+    return DAGC_OK;
+}
+
+int dagc_memory_report(dagc_context ctx, char* buf, uint64_t capacity, uint64_t* needed) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::string out;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        std::map<std::string, std::pair<uint64_t, uint64_t>> m;
+        ctx->pool.tally(m);
+        if (ctx->arena.cap) m["scratch arena"] = {ctx->arena.cap, 1};
+        if (ctx->table_cap) m["dedup table"] = {ctx->table_cap * 16, 1};
+        if (ctx->gtable) m["grouping table"] = {kGroupScratchBytes, 1};
+        uint64_t total = 0;
+        for (const auto& kv : m) total += kv.second.first;
+        std::vector<std::pair<std::string, std::pair<uint64_t, uint64_t>>> list(m.begin(), m.end());
+        std::sort(list.begin(), list.end(), [](const auto& a, const auto& b) { return a.second.first > b.second.first; });
+        char line[256];
+        std::snprintf(line, sizeof(line), "GPU memory: %.3f MB\nPeak of DAG and word blocks: %.3f MB\n\nAllocations overview:\n",
+                      total / 1048576.0, ctx->pool.peak() / 1048576.0);
+        out += line;
+        for (const auto& kv : list) {
+            std::snprintf(line, sizeof(line), "\t%24s: %12.3f MB (%llu allocs)\n", kv.first.c_str(),
+                          kv.second.first / 1048576.0, (unsigned long long)kv.second.second);
+            out += line;
+        }
+    }
+    if (needed) *needed = out.size() + 1;
+    if (buf && capacity) {
+        const size_t k = std::min<size_t>(capacity - 1, out.size());
+        std::memcpy(buf, out.data(), k);
+        buf[k] = 0;
+    }
+    return DAGC_OK;
+}
+
+int dagc_memory_events(dagc_context ctx, uint64_t* alloc_failures, uint64_t* retries_ok) {
+    if (!valid_ctx(ctx)) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (alloc_failures) *alloc_failures = ctx->alloc_stats.failures;
+    if (retries_ok) *retries_ok = ctx->alloc_stats.retries_ok;
     return DAGC_OK;
 }
 
@@ -2442,7 +2692,7 @@ int dagc_tune_sort(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int wit
     const bool values = with_values != 0;
     cudaStream_t s = ctx->capture_stream;  // a stream of the context's own, idle between calls
     void *kin = nullptr, *kout = nullptr, *vout = nullptr;
-    DAGC_CUDA(ctx, ctx->pool.alloc(&kin, n * 8));
+    DAGC_CUDA(ctx, ctx->pool.alloc(&kin, n * 8, "tuning keys"));
     int st = DAGC_OK;
     auto cleanup = [&]() {
         cudaStreamSynchronize(s);
@@ -2451,7 +2701,8 @@ int dagc_tune_sort(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int wit
         ctx->pool.release(vout);
         ctx->plan_override = nullptr;
     };
-    if (ctx->pool.alloc(&kout, n * 8) != cudaSuccess || (values && ctx->pool.alloc(&vout, n * 4) != cudaSuccess)) {
+    if (ctx->pool.alloc(&kout, n * 8, "tuning keys") != cudaSuccess ||
+        (values && ctx->pool.alloc(&vout, n * 4, "tuning keys") != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
         return set_error(ctx, DAGC_ERR_OUT_OF_MEMORY, "tuning buffers");

@@ -87,51 +87,9 @@ __device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// ------------------------------------------- TMA bulk copies + mbarriers ----
-// One-dimensional bulk copies global -> shared (cp.async.bulk) completing on
-// an mbarrier. Both addresses and the size must be multiples of 16 bytes.
+// Shared-memory address of a generic pointer (for cp.async operands).
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-// Makes barrier initialisation visible to the async (TMA) proxy.
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// Orders this thread's earlier generic-proxy shared accesses before later
-// async-proxy (TMA) accesses of the same shared memory.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst_smem)),
-        "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-// Bounded wait for the phase of `bar` with the given parity to complete.
-// Returns false after kSpinLimit polls (about a second).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    const uint32_t a = smem_addr(bar);
-    for (uint32_t it = 0; it < kSpinLimit; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
 }
 
 __device__ __forceinline__ void backoff(uint32_t iter) {

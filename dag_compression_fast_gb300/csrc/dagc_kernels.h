@@ -91,6 +91,12 @@ struct SortArgs {
     const uint64_t* seg_offsets;
     uint32_t seg_count;
     int seg_shift;
+    // Failure-path test hooks (zero in production): a lower limit on the
+    // look-back waits (0 = kSpinLimit), and a first digit pass whose tile 0
+    // never publishes its counts, so that the waits of the tiles after it run
+    // out and the sort reports kErrTimeout.
+    uint32_t spin_limit;
+    int stall_first_tile;
 };
 
 // Digit-pass kernel shapes. Keys-only sorts: (items per thread, minimum

@@ -8,8 +8,14 @@
 // src/DAG_Compression_Fast.cpp:283-302).
 //
 // Requests that name a chunk (its Morton index in a grid of chunks) keep their
-// intermediate DAG on the device after finishing; dagc_server_shared_dag
-// merges every such chunk into one device DAG (the growing shared DAG).
+// intermediate DAG on the device after finishing, and a merge thread folds
+// each finished chunk into a resident union of all chunks so far (the growing
+// shared DAG, dagc_union); dagc_server_shared_dag builds the levels above the
+// chunks over that union (dagc_dag_lift) instead of merging every chunk again.
+//
+// Every job records CUDA events around its device work on its slot's stream;
+// dagc_server_timeline reports that interval against an event recorded when
+// the server was created, so overlap of jobs on the device can be read off.
 
 #include "../../include/dagc.h"
 
@@ -43,6 +49,7 @@ struct Request {
     std::string error;
     std::vector<uint32_t> words;
     bool done = false;
+    double gpu_start_ms = -1, gpu_end_ms = -1;  // device interval of its work (see dagc_server_timeline)
 };
 
 }  // namespace
@@ -62,6 +69,22 @@ struct dagc_server_t {
     uint64_t next_ticket = 1;
     uint64_t completed = 0, fragments_done = 0, running = 0, max_running = 0;
     bool stop = false;
+    // Growing shared DAG (merge thread; guarded by `mu`): the union of the
+    // folded chunks, their root hashes by slot, chunks waiting to be folded,
+    // DAGs retired while a fold may read them.
+    dagc_dag body = nullptr;
+    std::map<int64_t, uint64_t> slot_root;
+    std::vector<int64_t> fold_queue;
+    bool body_stale = false;  // a folded chunk was replaced: rebuild from chunk_dags
+    bool folding = false;
+    int fold_status = DAGC_OK;
+    uint64_t folds = 0;       // unions made so far
+    std::vector<dagc_dag> retired;
+    std::condition_variable cv_fold, cv_folded;
+    std::thread merger;
+    // Device timeline: reference event and each job's interval, by ticket.
+    cudaEvent_t origin = nullptr;
+    std::map<uint64_t, std::pair<double, double>> timeline;
 };
 
 namespace {
@@ -75,6 +98,9 @@ void worker_loop(dagc_server_t* sv, int slot) {
     // request would synchronise the whole device and serialise the slots.
     void* stage = nullptr;
     uint64_t stage_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
     for (;;) {
         std::shared_ptr<Request> r;
         {
@@ -113,22 +139,33 @@ void worker_loop(dagc_server_t* sv, int slot) {
                 st = DAGC_ERR_CUDA;
             }
             dagc_dag dag = nullptr;
+            if (!st && ev0) cudaEventRecord(ev0, stream);
             if (!st) st = dagc_create(ctx, static_cast<const uint64_t*>(stage), r->n, r->depth, stream, &dag);
             if (!st && r->chunk >= 0) {
-                // Keep a device copy of the chunk's DAG for the shared DAG.
-                std::lock_guard<std::mutex> lock(sv->mu);
+                // Keep a device copy of the chunk's DAG for the shared DAG
+                // (the merge context serialises its own calls).
                 st = dagc_dag_copy(sv->merge_ctx, dag, stream, &keep);
             }
             uint32_t* d_words = nullptr;
             uint64_t nw = 0;
             if (!st) st = dagc_final(ctx, dag, stream, &d_words, &nw);
             else if (dag) dagc_dag_free(dag);
+            if (!st && ev1) cudaEventRecord(ev1, stream);
             if (!st) {
                 words.resize(nw);
                 st = dagc_words_download(ctx, d_words, nw, words.data());
                 dagc_free_words(ctx, d_words, stream);
             }
             if (st) err = dagc_last_error(ctx);
+            if (!st && ev0 && ev1 && sv->origin && cudaEventSynchronize(ev1) == cudaSuccess) {
+                float a = 0, b = 0;
+                if (cudaEventElapsedTime(&a, sv->origin, ev0) == cudaSuccess &&
+                    cudaEventElapsedTime(&b, sv->origin, ev1) == cudaSuccess) {
+                    r->gpu_start_ms = a;
+                    r->gpu_end_ms = b;
+                }
+                cudaGetLastError();
+            }
         }
         {
             std::lock_guard<std::mutex> lock(sv->mu);
@@ -141,16 +178,81 @@ void worker_loop(dagc_server_t* sv, int slot) {
             --sv->running;
             ++sv->completed;
             sv->fragments_done += r->n;
+            sv->timeline[r->ticket] = {r->gpu_start_ms, r->gpu_end_ms};
             if (keep) {
                 auto it = sv->chunk_dags.find(r->chunk);
-                if (it != sv->chunk_dags.end()) dagc_dag_free(it->second);
+                if (it != sv->chunk_dags.end()) {
+                    // A fold may be reading the old DAG: the merge thread frees it.
+                    sv->retired.push_back(it->second);
+                    if (sv->slot_root.count(r->chunk)) sv->body_stale = true;
+                }
                 sv->chunk_dags[r->chunk] = keep;
+                sv->fold_queue.push_back(r->chunk);
+                sv->cv_fold.notify_all();
             }
         }
         sv->cv_done.notify_all();
         sv->cv_work.notify_all();
     }
     if (stage) cudaFree(stage);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    cudaStreamDestroy(stream);
+}
+
+// Folds finished chunks into the resident union, several at a time: one
+// dagc_union of the current body and the waiting chunks (or, after a chunk was
+// replaced, of every kept chunk).
+void merge_loop(dagc_server_t* sv) {
+    cudaSetDevice(sv->device);
+    cudaStream_t stream = nullptr;
+    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    for (;;) {
+        std::vector<int64_t> slots;
+        std::vector<dagc_dag> inputs;
+        dagc_dag old_body = nullptr;
+        bool rebuild = false;
+        {
+            std::unique_lock<std::mutex> lock(sv->mu);
+            sv->cv_fold.wait(lock, [&] { return sv->stop || !sv->fold_queue.empty() || sv->body_stale; });
+            if (sv->fold_queue.empty() && !sv->body_stale) break;  // stopping, nothing left
+            rebuild = sv->body_stale;
+            sv->body_stale = false;
+            sv->fold_queue.clear();
+            sv->folding = true;
+            old_body = sv->body;
+            if (rebuild) {
+                for (auto& kv : sv->chunk_dags) { slots.push_back(kv.first); inputs.push_back(kv.second); }
+            } else {
+                if (old_body) inputs.push_back(old_body);
+                for (auto& kv : sv->chunk_dags)
+                    if (!sv->slot_root.count(kv.first)) { slots.push_back(kv.first); inputs.push_back(kv.second); }
+            }
+        }
+        dagc_dag body = nullptr;
+        std::vector<uint64_t> roots(inputs.size(), 0);
+        int st = inputs.empty() ? DAGC_OK
+                                : dagc_union(sv->merge_ctx, inputs.data(), inputs.size(), stream, &body, roots.data());
+        std::vector<dagc_dag> to_free;
+        {
+            std::lock_guard<std::mutex> lock(sv->mu);
+            const size_t first = rebuild || !old_body ? 0 : 1;
+            if (!st && body) {
+                if (rebuild) sv->slot_root.clear();
+                for (size_t i = 0; i < slots.size(); ++i) sv->slot_root[slots[i]] = roots[first + i];
+                if (old_body) to_free.push_back(old_body);
+                sv->body = body;
+                ++sv->folds;
+            } else if (st) {
+                sv->fold_status = st;
+            }
+            to_free.insert(to_free.end(), sv->retired.begin(), sv->retired.end());
+            sv->retired.clear();
+            sv->folding = false;
+        }
+        for (dagc_dag d : to_free) dagc_dag_free(d);
+        sv->cv_folded.notify_all();
+    }
     cudaStreamDestroy(stream);
 }
 
@@ -175,7 +277,16 @@ int dagc_server_create(int device, int slots, uint64_t hbm_budget_bytes, dagc_se
         if (i < slots) sv->contexts.push_back(c);
         else sv->merge_ctx = c;
     }
+    cudaSetDevice(device);
+    if (cudaEventCreate(&sv->origin) == cudaSuccess) {
+        cudaEventRecord(sv->origin, nullptr);
+        cudaEventSynchronize(sv->origin);
+    } else {
+        cudaGetLastError();
+        sv->origin = nullptr;
+    }
     for (int i = 0; i < slots; ++i) sv->workers.emplace_back(worker_loop, sv.get(), i);
+    sv->merger = std::thread(merge_loop, sv.get());
     *out = sv.release();
     return DAGC_OK;
 }
@@ -244,25 +355,47 @@ int dagc_server_stats(dagc_server sv, uint64_t* completed, uint64_t* fragments, 
 
 int dagc_server_shared_dag(dagc_server sv, int top_levels, dagc_context* ctx_out, dagc_dag* out) {
     if (!sv || !out || !ctx_out || top_levels < 0 || top_levels > 6) return DAGC_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lock(sv->mu);
+    *out = nullptr;
+    std::unique_lock<std::mutex> lock(sv->mu);
     if (sv->chunk_depth < 0 || sv->chunk_depth + top_levels > 21) return DAGC_ERR_INVALID_ARGUMENT;
     const uint64_t slots = 1ull << (3 * top_levels);
-    std::vector<dagc_dag> inputs(slots, nullptr);
-    int st = DAGC_OK;
-    // Copies of the kept chunk DAGs (dagc_merge consumes its inputs) and empty
-    // DAGs for the slots without a chunk.
-    for (uint64_t i = 0; i < slots && !st; ++i) {
-        auto it = sv->chunk_dags.find((int64_t)i);
-        if (it == sv->chunk_dags.end()) {
-            st = dagc_create(sv->merge_ctx, nullptr, 0, sv->chunk_depth, nullptr, &inputs[i]);
-            continue;
-        }
-        st = dagc_dag_copy(sv->merge_ctx, it->second, nullptr, &inputs[i]);  // dagc_merge consumes
-    }
-    if (!st) st = dagc_merge(sv->merge_ctx, inputs.data(), slots, nullptr, out);
-    for (dagc_dag d : inputs) if (d) dagc_dag_free(d);
+    // Every chunk finished so far is folded first.
+    sv->cv_folded.wait(lock, [&] { return sv->fold_queue.empty() && !sv->body_stale && !sv->folding; });
+    if (sv->fold_status) return sv->fold_status;
     *ctx_out = sv->merge_ctx;
-    return st;
+    std::vector<uint64_t> hashes(slots, 0);
+    for (auto& kv : sv->slot_root) {
+        if (kv.first < 0 || (uint64_t)kv.first >= slots) return DAGC_ERR_INVALID_ARGUMENT;
+        hashes[kv.first] = kv.second;
+    }
+    if (!sv->body) return dagc_create(sv->merge_ctx, nullptr, 0, sv->chunk_depth + top_levels, nullptr, out);
+    return dagc_dag_lift(sv->merge_ctx, sv->body, hashes.data(), slots, nullptr, out);
+}
+
+int dagc_server_set_option(dagc_server sv, int option, int value) {
+    if (!sv) return DAGC_ERR_INVALID_ARGUMENT;
+    for (dagc_context c : sv->contexts) {
+        const int st = dagc_set_option(c, option, value);
+        if (st) return st;
+    }
+    return DAGC_OK;
+}
+
+int dagc_server_folds(dagc_server sv, uint64_t* folds) {
+    if (!sv || !folds) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    *folds = sv->folds;
+    return DAGC_OK;
+}
+
+int dagc_server_timeline(dagc_server sv, uint64_t ticket, double* gpu_start_ms, double* gpu_end_ms) {
+    if (!sv || !gpu_start_ms || !gpu_end_ms) return DAGC_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(sv->mu);
+    auto it = sv->timeline.find(ticket);
+    if (it == sv->timeline.end()) return DAGC_ERR_INVALID_ARGUMENT;
+    *gpu_start_ms = it->second.first;
+    *gpu_end_ms = it->second.second;
+    return DAGC_OK;
 }
 
 void dagc_server_destroy(dagc_server sv) {
@@ -273,7 +406,12 @@ void dagc_server_destroy(dagc_server sv) {
     }
     sv->cv_work.notify_all();
     for (auto& t : sv->workers) t.join();
+    sv->cv_fold.notify_all();
+    if (sv->merger.joinable()) sv->merger.join();
     for (auto& kv : sv->chunk_dags) dagc_dag_free(kv.second);
+    for (dagc_dag d : sv->retired) dagc_dag_free(d);
+    if (sv->body) dagc_dag_free(sv->body);
+    if (sv->origin) cudaEventDestroy(sv->origin);
     for (dagc_context c : sv->contexts) dagc_context_destroy(c);
     if (sv->merge_ctx) dagc_context_destroy(sv->merge_ctx);
     delete sv;

@@ -161,6 +161,8 @@ struct PassParams {
     int seg_shift;
     const uint32_t* gate;
     uint32_t gate_run;
+    uint32_t spin_limit;      // polls before a look-back wait gives up (kSpinLimit)
+    int stall_first_tile;     // test hook: tile 0 never publishes (its successors' waits run out)
 };
 
 // Loads / stores kN consecutive shared (or global) words as vectors.
@@ -231,7 +233,7 @@ __device__ __forceinline__ void st_status(uint32_t* p, const uint32_t (&v)[kN]) 
 // first one some unfinished digit still waits for.
 template <int kDPT>
 __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t radix, uint32_t tile, uint32_t d0,
-                                                uint32_t (&excl)[kDPT], uint32_t* err) {
+                                                uint32_t (&excl)[kDPT], uint32_t* err, uint32_t spin_limit) {
     constexpr int kLB = kDPT >= 4 ? 4 : 16 / kDPT;  // tiles per round trip
     uint32_t done = 0, iter = 0;
     constexpr uint32_t kAll = (1u << kDPT) - 1u;
@@ -274,7 +276,7 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
         }
         t -= consumed;
         if (consumed == 0) {
-            if (++iter > kSpinLimit) { atomicOr(err, kErrTimeout); break; }
+            if (++iter > spin_limit) { atomicOr(err, kErrTimeout); break; }
             backoff(iter);
         }
     }
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
                 pub[q] = (tile == 0 ? kSInc : kSAgg) | cnt[q];
                 sum += cnt[q];
             }
-            st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
+            if (!(p.stall_first_tile && tile == 0)) st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
             uint32_t total;
             uint32_t run = block_exclusive_sum<uint32_t>(sum, S.scan, &total);
 #pragma unroll
@@ -503,7 +505,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
         {
             uint32_t excl[kDPT];
             if (tile > 0) {
-                lookback_digits<kDPT>(p.status, kRadix, tile, d0, excl, p.err);
+                lookback_digits<kDPT>(p.status, kRadix, tile, d0, excl, p.err, p.spin_limit);
                 uint32_t pub[kDPT];
 #pragma unroll
                 for (int q = 0; q < kDPT; ++q) pub[q] = kSInc | (excl[q] + cnt[q]);
@@ -681,6 +683,8 @@ static PassParams pass_params(const SortArgs& a, int i) {
     p.seg_shift = a.seg_shift;
     p.gate = a.gate;
     p.gate_run = a.gate_run;
+    p.spin_limit = a.spin_limit ? a.spin_limit : kSpinLimit;
+    p.stall_first_tile = i == 0 ? a.stall_first_tile : 0;
     return p;
 }
 

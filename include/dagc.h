@@ -112,6 +112,22 @@ uint64_t dagc_create_footprint(uint64_t n, int depth);
  * Runs entirely on the device. */
 int dagc_merge(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_dag* out);
 
+/* Per-level union of k >= 1 DAGs of equal depth, the reference's pairwise
+ * MergeDAGs(FPool&, FCpuDag&&, FCpuDag&&) (src/DAGCompression.cu:1165-1320)
+ * for any number of inputs: no level is added, the result's top level holds
+ * every input's root. Does not consume the inputs. root_hashes (k entries,
+ * may be NULL) receives each input's root hash, 0 for an empty input. */
+int dagc_union(dagc_context ctx, dagc_dag* dags, uint64_t k, void* stream, dagc_dag* out,
+               uint64_t* root_hashes);
+/* The DAG over a grid of `slots` = 8^m chunk slots (Morton order) whose chunk
+ * roots are in the top level of `body` (a union of chunk DAGs): slot i holds
+ * the chunk with root hash slot_root_hashes[i] (0: empty). The m top levels
+ * are built as MergeDAGs builds them (src/DAGCompression.cu:1504-1533); the
+ * result equals dagc_merge of the chunk DAGs in their slots when body is their
+ * union. */
+int dagc_dag_lift(dagc_context ctx, dagc_dag body, const uint64_t* slot_root_hashes, uint64_t slots,
+                  void* stream, dagc_dag* out);
+
 /* ------------------------------------------------------- CreateFinalDAG ---- */
 /* Replaces DAGCompression::CreateFinalDAG (src/DAGCompression.h:47,
  * src/DAGCompression.cu:1550-1610). Consumes the DAG. *d_words receives a
@@ -196,6 +212,16 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * every workload here (config 3: 7.1 ms against 8.3 ms). Results are
  * identical. */
 #define DAGC_OPT_PDL 7
+/* Failure-path test hooks (off by default; no counterpart in the reference).
+ * TEST_SPIN_LIMIT: polls before a bounded device wait of the sorts gives up
+ * (0: the production limit, about a second). TEST_STALL_LOOKBACK: 1 makes the
+ * first digit pass of every sort leave its tile 0 unpublished, so the waits of
+ * the tiles after it run out and the call returns DAGC_ERR_DEVICE_TIMEOUT (the
+ * context stays usable). TEST_FAIL_ALLOCS: the context's next `value` device
+ * allocations fail as on a full device (dagc_memory_events counts them). */
+#define DAGC_OPT_TEST_SPIN_LIMIT 9
+#define DAGC_OPT_TEST_STALL_LOOKBACK 10
+#define DAGC_OPT_TEST_FAIL_ALLOCS 11
 int dagc_set_option(dagc_context ctx, int option, int value);
 /* Calls of this context rerun in the radix form so far. */
 int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
@@ -278,6 +304,16 @@ int dagc_file_read(const char* path, double* aabb6, uint32_t* depth, uint32_t* h
  * peak, bytes cached for reuse, and the scratch arena's size. */
 int dagc_memory_stats(dagc_context ctx, uint64_t* in_use, uint64_t* peak, uint64_t* cached,
                       uint64_t* arena);
+/* Text report of a context's device memory, after the reference's
+ * FMemory::GetStatsString (src/Memory.cpp:222-262): total, the peak of DAG
+ * and word blocks, and an overview by allocation name (bytes, count), largest
+ * first. Writes at most `capacity` bytes (NUL-terminated) to buf (may be
+ * NULL); *needed receives the full size including the NUL. */
+int dagc_memory_report(dagc_context ctx, char* buf, uint64_t capacity, uint64_t* needed);
+/* Allocation events of a context: failed device allocations (injected or
+ * real) and allocations that succeeded on their retry after the cache was
+ * released (src/Memory.cpp:56-70 retries once after freeing its pool). */
+int dagc_memory_events(dagc_context ctx, uint64_t* alloc_failures, uint64_t* retries_ok);
 
 /* ------------------------------------------------------------- tracer ---- */
 /* Headless counterpart of the reference's FDAGTracer (src/DAGTracer.h:8-93,
@@ -348,10 +384,21 @@ int dagc_server_wait(dagc_server server, uint64_t ticket, uint32_t* h_words, uin
                      uint64_t* n_words, double* latency_ms);
 int dagc_server_stats(dagc_server server, uint64_t* completed, uint64_t* fragments,
                       uint64_t* max_concurrent, uint64_t* peak_footprint);
-/* Merges every chunk job kept so far into one device DAG over a grid of
- * 2^top_levels chunks per side (missing chunks empty), like dagc_merge; the
- * DAG belongs to *ctx_out (the server's merge context). */
+/* The shared DAG of every chunk job finished so far, over a grid of
+ * 2^top_levels chunks per side (missing chunks empty); equal to dagc_merge of
+ * the chunk DAGs in their slots. A merge thread folds each finished chunk into
+ * a resident union (dagc_union) as it completes; this call waits for the
+ * folds in progress and builds the top levels over the union (dagc_dag_lift).
+ * The DAG belongs to *ctx_out (the server's merge context). */
 int dagc_server_shared_dag(dagc_server server, int top_levels, dagc_context* ctx_out, dagc_dag* out);
+/* dagc_set_option on every worker slot's context. */
+int dagc_server_set_option(dagc_server server, int option, int value);
+/* Unions the merge thread has made so far. */
+int dagc_server_folds(dagc_server server, uint64_t* folds);
+/* Device interval of a finished job's work (CreateDAG to CreateFinalDAG on its
+ * slot's stream), in ms after an event recorded when the server was created;
+ * jobs whose intervals intersect had work in flight on the GPU at the same time. */
+int dagc_server_timeline(dagc_server server, uint64_t ticket, double* gpu_start_ms, double* gpu_end_ms);
 void dagc_server_destroy(dagc_server server);
 
 /* No counterpart in the reference. The key sort of dagc_sort_keys without any

@@ -70,3 +70,58 @@ def test_shared_dag_of_chunk_jobs(ctx):
         assert_dag_equal(shared.to_host(), O.create_dag(codes, 9))
     finally:
         srv.close()
+
+
+def test_shared_dag_grows_as_chunks_finish(ctx):
+    """Each finished chunk is folded into the resident union; after every
+    chunk the shared DAG equals the oracle's DAG of the chunks so far, and a
+    chunk submitted again replaces its earlier version."""
+    codes = random_codes(9, 150_000, 41, cluster=True)
+    chunks, sub = chunks_of(codes, 9, 1)
+    srv = D.Server(0, slots=2)
+    try:
+        so_far = []
+        for i, c in enumerate(chunks):
+            if not c.size:
+                continue
+            srv.wait(srv.submit(c, sub, chunk_morton=i))
+            so_far.append((np.uint64(i) << np.uint64(3 * sub)) | c)
+            shared = srv.shared_dag(1)
+            assert_dag_equal(shared.to_host(), O.create_dag(np.concatenate(so_far), 9))
+        assert srv.folds() >= 2
+        # Chunk 0 again, with other fragments: the shared DAG follows.
+        repl = random_codes(sub, 5_000, 42)
+        srv.wait(srv.submit(repl, sub, chunk_morton=0))
+        rest = [(np.uint64(i) << np.uint64(3 * sub)) | c for i, c in enumerate(chunks) if i and c.size]
+        assert_dag_equal(srv.shared_dag(1).to_host(), O.create_dag(np.concatenate([repl] + rest), 9))
+    finally:
+        srv.close()
+
+
+def test_union_and_lift_equal_merge(ctx):
+    codes = random_codes(8, 80_000, 43)
+    chunks, sub = chunks_of(codes, 8, 1)
+    dags = [ctx.create_dag(c, sub) for c in chunks]
+    body, roots = ctx.union_dags(dags)
+    lifted = ctx.lift_dag(body, roots)
+    assert_dag_equal(lifted.to_host(), O.create_dag(codes, 8))
+
+
+def test_jobs_overlap_on_the_device(ctx):
+    """Device-side evidence of overlap: each job's work is bracketed by CUDA
+    events on its slot's stream; some pair of jobs has intersecting
+    intervals."""
+    jobs = job_mix(91)
+    srv = D.Server(0, slots=4, hbm_budget_bytes=32 << 30)
+    try:
+        for _ in range(2):  # warm: arenas and graphs
+            tickets = [srv.submit(codes, depth) for codes, depth in jobs]
+            for t in tickets:
+                srv.wait(t)
+        iv = [srv.timeline(t) for t in tickets]
+        assert all(0 <= a < b for a, b in iv)
+        overlaps = sum(1 for i in range(len(iv)) for j in range(i + 1, len(iv))
+                       if iv[i][0] < iv[j][1] and iv[j][0] < iv[i][1])
+        assert overlaps >= 1
+    finally:
+        srv.close()
