@@ -43,7 +43,7 @@ __device__ __forceinline__ uint64_t load_n(const uint64_t* d_n, uint64_t n) {
 }
 
 // Segment of position i (seg_offsets ascending, count + 1 entries): binary
-// search for the first position of a block, then `segment_from` walks forward.
+// search for the first position of a block, then `segment_advance` follows it.
 __device__ __forceinline__ uint32_t segment_search(const uint64_t* off, uint32_t count, uint64_t i) {
     uint32_t lo = 0, hi = count;  // invariant: off[lo] <= i < off[hi]
     while (hi - lo > 1) {
@@ -52,9 +52,20 @@ __device__ __forceinline__ uint32_t segment_search(const uint64_t* off, uint32_t
     }
     return lo;
 }
-__device__ __forceinline__ uint32_t segment_from(const uint64_t* off, uint32_t count, uint64_t i, uint32_t hint) {
-    while (hint + 1 < count && __ldg(off + hint + 1) <= i) ++hint;
-    return hint;
+// Segment of a later position from the segment of an earlier one (`hint`):
+// a few steps forward, then a binary search over the rest.
+__device__ __forceinline__ uint32_t segment_advance(const uint64_t* off, uint32_t count, uint64_t i, uint32_t hint) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (hint + 1 >= count || __ldg(off + hint + 1) > i) return hint;
+        ++hint;
+    }
+    uint32_t lo = hint, hi = count;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
 constexpr uint64_t kHistMinPerThread = 16;
@@ -110,7 +121,10 @@ __global__ void __launch_bounds__(kSortThreads) radix_histogram(HistParams h) {
     const uint64_t astride = (uint64_t)active * blockDim.x;
 
     // Four independent loads in flight per thread (grid-stride, unrolled).
+    // A thread's positions only grow, so its segment (batched input) is found
+    // once by binary search and then followed forward.
     uint64_t bad = 0;
+    uint32_t sg = h.seg_offsets && gtid < n ? segment_search(h.seg_offsets, h.seg_count, gtid) : 0u;
     for (uint64_t i0 = gtid; i0 < n; i0 += 4 * astride) {
         uint64_t k[4];
         bool in[4];
@@ -124,8 +138,10 @@ __global__ void __launch_bounds__(kSortThreads) radix_histogram(HistParams h) {
         for (int u = 0; u < 4; ++u) {
             if (!in[u]) continue;
             if (h.validate_bits > 0 && h.validate_bits < 64) bad |= k[u] >> h.validate_bits;
-            if (h.seg_offsets)
-                k[u] |= (uint64_t)segment_search(h.seg_offsets, h.seg_count, i0 + u * astride) << h.seg_shift;
+            if (h.seg_offsets) {
+                sg = segment_advance(h.seg_offsets, h.seg_count, i0 + u * astride, sg);
+                k[u] |= (uint64_t)sg << h.seg_shift;
+            }
 #pragma unroll
             for (int p = 0; p < kMaxPasses; ++p) {
                 if (p >= passes) break;
@@ -426,7 +442,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
                 for (int j = 0; j < kItems; ++j) {
                     const uint32_t i = wofs + j * 32 + lane;
                     if (i < tile_n) {
-                        sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
+                        sg = segment_advance(p.seg_offsets, p.seg_count, base + i, sg);
                         k[j] |= (uint64_t)sg << p.seg_shift;
                     }
                 }
@@ -491,7 +507,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
                 if (i < tile_n) {
                     uint64_t key = __ldg(p.keys_in + base + i);
                     if (p.seg_offsets) {
-                        sg = segment_from(p.seg_offsets, p.seg_count, base + i, sg);
+                        sg = segment_advance(p.seg_offsets, p.seg_count, base + i, sg);
                         key |= (uint64_t)sg << p.seg_shift;
                     }
                     const uint32_t pos = wh[dr[j] >> 16] + (dr[j] & 0xFFFFu);
