@@ -38,6 +38,7 @@ OPT_SORT_RADIX_BITS = 8
 OPT_TEST_SPIN_LIMIT = 9
 OPT_TEST_STALL_LOOKBACK = 10
 OPT_TEST_FAIL_ALLOCS = 11
+OPT_BATCH_PATH = 12
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
 NUM_KEY_SHAPES = 6
@@ -73,7 +74,7 @@ DAGC_SYMBOLS = [
 ]
 
 STAGES = ["fragment_hist", "fragment_pass", "leaf_build", "leaf_dedup", "levels", "materialise",
-          "final", "merge", "group", "group_sketch", "group_aggregate", "group_scatter"]
+          "final", "merge", "group", "group_sketch", "group_aggregate", "group_scatter", "chunk_leaves"]
 GEN_SYMBOLS = ["dagc_gen_free", "dagc_gen_sphere_shell", "dagc_gen_terrain",
                "dagc_gen_triangle_soup", "dagc_gen_soup_triangles", "dagc_gen_batched"]
 

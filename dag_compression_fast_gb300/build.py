@@ -31,7 +31,8 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wextra", "-ffp-contract=off",
              f"-I{CUDA_HOME}/include", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["sort.cu", "dag_kernels.cu", "dedup.cu", "group.cu", "trace.cu", "voxelize.cu", "sort_noalloc.cu"]
+CU_SOURCES = ["sort.cu", "dag_kernels.cu", "dedup.cu", "group.cu", "chunks.cu", "trace.cu", "voxelize.cu",
+              "sort_noalloc.cu"]
 # The tracer's and the voxelizer's float arithmetic must round once per
 # operation (no FMA contraction) so that their results are reproducible on the CPU.
 CU_EXTRA = {"trace.cu": ["--fmad=false"], "voxelize.cu": ["--fmad=false"]}

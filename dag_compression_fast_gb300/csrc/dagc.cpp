@@ -292,12 +292,14 @@ struct GraphKey {
     void* arena;
     uint32_t chunks;   // batched calls: number of chunks (0 otherwise)
     int chunk_depth;   // batched calls: chunk depth, which sets the composite key split (0 otherwise)
+    bool chunk_path;   // batched calls: persistent per-chunk leaves
     bool dedup;        // hash-set dedup (else radix sort + unique) for the leaves and levels
     void* table;       // the dedup table block
     int group;         // fragment grouping mode
     bool operator==(const GraphKey& o) const {
         return frag == o.frag && n == o.n && depth == o.depth && arena == o.arena && chunks == o.chunks &&
-               chunk_depth == o.chunk_depth && dedup == o.dedup && table == o.table && group == o.group;
+               chunk_depth == o.chunk_depth && chunk_path == o.chunk_path && dedup == o.dedup && table == o.table &&
+               group == o.group;
     }
 };
 struct GraphEntry {
@@ -342,6 +344,8 @@ struct dagc_context_t {
     // scratch (kGroupScratchBytes): the brick masks.
     bool use_dedup = true;
     int group_mode = 1;  // DAGC_OPT_GROUP
+    int batch_path = 1;  // DAGC_OPT_BATCH_PATH
+    std::vector<uint32_t> ck_tile_host;  // chunk path: first tile of each chunk (host copy for the upload)
     bool pdl = false;    // DAGC_OPT_PDL
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
@@ -796,8 +800,14 @@ struct CreateLayout {
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
     size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bslot = 0, o_brep = 0;
+    // Persistent per-chunk leaves (batched form): zeroed chunk state
+    // (histograms, cursors, done counters, item counter), tile offsets, the
+    // mask stage and per-item brick counts / offsets.
+    uint32_t ck_bins = 0, ck_groups = 0;
+    size_t o_ck_state = 0, ck_state_bytes = 0, o_ck_hist = 0, o_ck_cursor = 0, o_ck_done = 0, o_ck_work = 0;
+    size_t o_ck_tile = 0, o_ck_mask = 0, o_ck_gb = 0, o_ck_gs = 0, o_ck_gd = 0;
     CreateLayout(uint64_t n, int depth, uint32_t k_batch, bool use_dedup, uint64_t unique_limit = kDedupMaxUnique,
-                 bool grouping = false) {
+                 bool grouping = false, int chunk_depth = 0) {
         const int nl = depth - 2;
         cap.resize(nl);
         for (int l = 0; l < nl; ++l) { cap[l] = level_cap(l, n); capmax = std::max(capmax, cap[l]); }
@@ -860,6 +870,21 @@ struct CreateLayout {
         o_lead_run = L.take<uint64_t>(scan_tiles(n) + 1);
         o_seg_off = L.take<uint64_t>(k_batch ? k_batch + 1 : 0);
         o_seg_code = L.take<uint64_t>(k_batch);
+        if (chunk_depth > 0 && k_batch) {
+            ck_bins = 1u << chunk_bin_bits(chunk_depth);
+            ck_groups = (ck_bins + kChunkGroupBins - 1) / kChunkGroupBins;
+            o_ck_hist = L.take<uint32_t>((uint64_t)k_batch * ck_bins);
+            o_ck_state = o_ck_hist;
+            o_ck_cursor = L.take<uint32_t>((uint64_t)k_batch * ck_bins);
+            o_ck_done = L.take<uint32_t>(2ull * k_batch);
+            o_ck_work = L.take<uint32_t>(1);
+            ck_state_bytes = L.off - o_ck_state;
+            o_ck_tile = L.take<uint32_t>(k_batch + 1ull);
+            o_ck_mask = L.take<uint64_t>(n);
+            o_ck_gb = L.take<uint32_t>((uint64_t)k_batch * ck_groups);
+            o_ck_gs = L.take<uint64_t>((uint64_t)k_batch * ck_groups);
+            o_ck_gd = L.take<uint32_t>((uint64_t)k_batch * ck_groups);
+        }
         total = L.off;
     }
 };
@@ -895,8 +920,11 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     const int group_mode = ctx->group_mode;
     const int nl = depth - 2;
     const int bits = 3 * depth;
+    // Batched calls take the persistent per-chunk leaf build (chunks.cu) when
+    // the chunk's bins fit its limits; otherwise the composite-key path.
+    const bool chunk_path = batch && ctx->batch_path == 1 && chunk_bin_bits(batch->chunk_depth) <= kChunkMaxBinBits;
     const CreateLayout Lo(n, depth, batch ? batch->k : 0u, use_dedup, ctx->dedup_unique_limit,
-                          group_mode != 0 && use_dedup);
+                          group_mode != 0 && use_dedup && !chunk_path, chunk_path ? batch->chunk_depth : 0);
     const std::vector<uint64_t>& cap = Lo.cap;
     const uint64_t capmax = Lo.capmax, p0cap = Lo.p0cap, sv_total = Lo.sv_total;
     const size_t zero_bytes = Lo.zero_bytes;
@@ -923,6 +951,20 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
                                        cudaMemcpyHostToDevice, s));
         DAGC_CUDA(ctx, cudaMemcpyAsync(P64(Lo.o_seg_code), batch->h_morton, batch->k * 8, cudaMemcpyHostToDevice, s));
     }
+    // Chunk path: the first COUNT/SCATTER tile of every chunk (none when a
+    // chunk is a single bin).
+    uint32_t ck_tiles = 0;
+    if (chunk_path) {
+        ctx->ck_tile_host.assign(batch->k + 1, 0);
+        for (uint32_t c = 0; c < batch->k; ++c) {
+            const uint64_t nc = batch->h_offsets[c + 1] - batch->h_offsets[c];
+            const uint64_t t = Lo.ck_bins > 1 ? (nc + kChunkTile - 1) / kChunkTile : 0;
+            ctx->ck_tile_host[c + 1] = ctx->ck_tile_host[c] + (uint32_t)t;
+        }
+        ck_tiles = ctx->ck_tile_host[batch->k];
+        DAGC_CUDA(ctx, cudaMemcpyAsync(P32(Lo.o_ck_tile), ctx->ck_tile_host.data(), (batch->k + 1) * 4,
+                                       cudaMemcpyHostToDevice, s));
+    }
 
     // Everything from here to the last kernel is enqueued by one function, so
     // that it can be recorded once as a CUDA graph and replayed.
@@ -941,7 +983,42 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         //     the kernels of the path not taken do nothing. Either path leaves
         //     the sorted bricks in P, their leaf masks in LM and their count.
         const uint32_t* gate = nullptr;
-        if (group_mode != 0 && use_dedup && ctx->gtable) {
+        if (chunk_path) {
+            // 1. Every chunk's leaves in one persistent launch (+ scan, pack).
+            StageTimer t(ctx, DAGC_STAGE_CHUNK_LEAVES, s);
+            DAGC_CUDA(ctx, cudaMemsetAsync(b + Lo.o_ck_state, 0, Lo.ck_state_bytes, s));
+            ChunkArgs ca{};
+            ca.frags = d_frag;
+            ca.seg_offsets = P64(Lo.o_seg_off);
+            ca.seg_code = P64(Lo.o_seg_code);
+            ca.k = batch->k;
+            ca.chunk_depth = batch->chunk_depth;
+            ca.seg_shift = seg_shift;
+            ca.bin_bits = chunk_bin_bits(batch->chunk_depth);
+            ca.tile_off = P32(Lo.o_ck_tile);
+            ca.tiles = ck_tiles;
+            ca.groups_per_chunk = Lo.ck_groups;
+            ca.hist = P32(Lo.o_ck_hist);
+            ca.cursor = P32(Lo.o_ck_cursor);
+            ca.done = P32(Lo.o_ck_done);
+            ca.work = P32(Lo.o_ck_work);
+            ca.scratch = P64(Lo.o_B);
+            ca.stage_parent = P64(Lo.o_A);
+            ca.stage_mask = P64(Lo.o_ck_mask);
+            ca.group_bricks = P32(Lo.o_ck_gb);
+            ca.group_src = P64(Lo.o_ck_gs);
+            ca.group_dst = P32(Lo.o_ck_gd);
+            ca.parents = P64(Lo.o_P);
+            ca.leaves = P64(Lo.o_LM);
+            ca.out_capacity = p0cap;
+            ca.d_out_n = cs.count(kCntBricks);
+            ca.err = err;
+            launch_chunk_leaves(ca, s);
+            ctx->launches += 3;
+            DAGC_LAUNCHED(ctx);
+            t.stop();
+        }
+        if (!chunk_path && group_mode != 0 && use_dedup && ctx->gtable) {
             GroupArgs g{};
             g.frags = d_frag;
             g.n = n;
@@ -1004,12 +1081,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         // 1b. Fragment sort on the brick key bits [6, 3*depth): only the order of
         //     code >> 6 matters downstream (the leaf mask ORs the low 6 bits).
         const SegmentSpec seg{batch ? P64(Lo.o_seg_off) : nullptr, batch ? batch->k : 0u, seg_shift};
-        st = run_sort(ctx, cs, sb, d_frag, P64(Lo.o_A), P64(Lo.o_B), nullptr, nullptr, nullptr, false, n, nullptr, 6,
-                      sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg, gate, 0u);
+        if (!chunk_path)
+            st = run_sort(ctx, cs, sb, d_frag, P64(Lo.o_A), P64(Lo.o_B), nullptr, nullptr, nullptr, false, n, nullptr, 6,
+                          sort_hi, validate, s, DAGC_STAGE_FRAGMENT_HIST, DAGC_STAGE_FRAGMENT_PASS, &seg, gate, 0u);
         if (st) return st;
 
         // 2. Fused unique + leaf build.
-        {
+        if (!chunk_path) {
             StageTimer t(ctx, DAGC_STAGE_LEAF_BUILD, s);
             LeafBuildArgs a{};
             a.sorted = P64(Lo.o_A);
@@ -1216,7 +1294,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
     return DAGC_OK;
     };
     int st = run_enqueue(ctx, GraphKey{d_frag, n, depth, ctx->arena.base, batch ? batch->k : 0u,
-                                       batch ? batch->chunk_depth : 0, use_dedup,
+                                       batch ? batch->chunk_depth : 0, chunk_path, use_dedup,
                                        use_dedup ? ctx->table : nullptr, use_dedup ? group_mode : 0},
                          s, enqueue);
     if (st) { ctx->table_dirty = true; return st; }
@@ -1245,6 +1323,10 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_SCATTER, (8 + entry) * n);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP_AGGREGATE, entry * n + 20 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_GROUP, 60 * p0);
+        // Chunk leaves: COUNT reads the fragments, SCATTER reads and writes
+        // them, LEAVES reads them and writes 16 bytes per brick, the pack
+        // moves those bricks once more.
+        set_pending_bytes(ctx, DAGC_STAGE_CHUNK_LEAVES, (Lo.ck_bins > 1 ? 32 : 8) * n + 48 * p0);
         set_pending_bytes(ctx, DAGC_STAGE_LEAF_DEDUP, 216 * p0 + 8 * lv);
         uint64_t lb = 0;
         for (int l = 0; l < nl; ++l) {
@@ -1840,6 +1922,7 @@ int dagc_context_create(int device, dagc_context* out) {
     if (const char* d = std::getenv("DAGC_DEDUP")) c->use_dedup = std::atoi(d) != 0;
     if (const char* gm = std::getenv("DAGC_GROUP")) c->group_mode = std::min(2, std::max(0, std::atoi(gm)));
     if (const char* pd = std::getenv("DAGC_PDL")) c->pdl = std::atoi(pd) != 0;
+    if (const char* bp = std::getenv("DAGC_BATCH_PATH")) c->batch_path = std::atoi(bp) != 0;
     // Persistent grid sizes: resident CTAs per SM x SMs.
     for (int sh = 0; sh < kNumKeyShapes; ++sh)
         for (int b = kRadixBits; b <= kMaxRadixBits; ++b)
@@ -1881,6 +1964,7 @@ int dagc_context_create(int device, dagc_context* out) {
     c->grid_write = 8 * c->sms;
     dedup_configure(c->sms);
     group_configure(c->sms);
+    chunk_configure(c->sms);
     *out = c.release();
     return DAGC_OK;
 }
@@ -2295,6 +2379,10 @@ int dagc_set_option(dagc_context ctx, int option, int value) {
         case DAGC_OPT_GROUP:
             if (value < 0 || value > 2) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "group mode must be 0, 1 or 2");
             ctx->group_mode = value;
+            return DAGC_OK;
+        case DAGC_OPT_BATCH_PATH:
+            if (value < 0 || value > 1) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "batch path must be 0 or 1");
+            ctx->batch_path = value;
             return DAGC_OK;
         case DAGC_OPT_TEST_SPIN_LIMIT:
             if (value < 0) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "spin limit must be >= 0");

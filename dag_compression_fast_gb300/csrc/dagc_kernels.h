@@ -195,6 +195,35 @@ void launch_group_scatter(const GroupArgs& a, cudaStream_t s);
 void launch_group_aggregate(const GroupArgs& a, cudaStream_t s);
 void launch_group_gather(const GroupArgs& a, cudaStream_t s);
 
+// Batched form: every chunk's leaves in one persistent launch (chunks.cu).
+// A chunk's local bricks (local code >> 6) fall in 2^bin_bits bins of at most
+// 2^kChunkDirectBits bricks, direct-mapped in shared memory.
+constexpr int kChunkThreads = 512;
+constexpr int kChunkTile = 8192;       // fragments per COUNT / SCATTER item
+constexpr int kChunkDirectBits = 13;   // bricks of one bin
+constexpr int kChunkMaxBinBits = 12;   // bins per chunk (chunk depth <= 10)
+constexpr int kChunkGroupBins = 32;    // bins per LEAVES item
+struct ChunkArgs {
+    const uint64_t* frags;                          // chunk-local codes, chunks back to back
+    const uint64_t* seg_offsets; const uint64_t* seg_code;  // k + 1 offsets, k Morton indices (device)
+    uint32_t k; int chunk_depth; int seg_shift;     // seg_shift = 3 * chunk_depth
+    int bin_bits;                                   // chunk_bin_bits(chunk_depth)
+    const uint32_t* tile_off;                       // k + 1: first COUNT/SCATTER tile of each chunk (device)
+    uint32_t tiles;                                 // tile_off[k] (host copy, for the grid only)
+    uint32_t groups_per_chunk;                      // LEAVES items per chunk
+    uint32_t* hist; uint32_t* cursor;               // k << bin_bits each, zero
+    uint32_t* done;                                 // 2k: COUNT tiles done, SCATTER tiles done (zero)
+    uint32_t* work;                                 // item counter (zero)
+    uint64_t* scratch;                              // fragments by bin (n)
+    uint64_t* stage_parent; uint64_t* stage_mask;   // n each: each item's bricks at its fragment offset
+    uint32_t* group_bricks; uint64_t* group_src; uint32_t* group_dst;  // per LEAVES item
+    uint64_t* parents; uint64_t* leaves; uint64_t out_capacity; uint64_t* d_out_n;
+    uint32_t* err;
+};
+void chunk_configure(int sms);
+int chunk_bin_bits(int chunk_depth);  // -> bins of at most 2^kChunkDirectBits bricks
+void launch_chunk_leaves(const ChunkArgs& a, cudaStream_t s);  // three launches
+
 // Unique over (key, perm) sorted by key: uid = rank of the key among distinct
 // keys; map[perm[i]] = uid; for the first of each run, out_keys[uid] = key and
 // payloads are gathered from perm. With node payloads (masks/children) the

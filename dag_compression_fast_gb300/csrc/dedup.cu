@@ -376,149 +376,6 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     }
 }
 
-// Top-bit form (node hashes, uniform): each warp takes whole buckets. A
-// bucket's keys share their top bits, so the next 8 bits spread them evenly:
-// the warp counts them per 8-bit sub-bucket, scans the counts, lists each
-// sub-bucket's keys together and ranks a key among the few of its own
-// sub-bucket. No block barrier; the CTA's buckets are a contiguous range.
-constexpr int kTopThreads = 128;
-constexpr int kTopWarps = kTopThreads / 32;
-struct TopBitSmem {
-    uint64_t key[kTopWarps][kDedupTopBitCap];
-    uint16_t ord[kTopWarps][kDedupTopBitCap];
-    uint32_t sub[kTopWarps][256];
-    uint32_t red[kTopWarps];
-};
-
-__global__ void __launch_bounds__(kTopThreads) dedup_sort_topbit(DedupArgs a) {
-    pdl_prologue();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TopBitSmem& S = *reinterpret_cast<TopBitSmem*>(smem_raw);
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t nb = a.state->nbuckets;
-    if (blockIdx.x == 0) {
-        // The distinct keys are the bucket entries (the insert appended every
-        // first inserter to its bucket).
-        uint32_t part = 0;
-        for (uint32_t b = tid; b < nb; b += kTopThreads) part += min(a.bucket_count[b], kDedupTopBitCap);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
-        if (lane == 0) S.red[warp] = part;
-        __syncthreads();
-        if (tid == 0) {
-            uint64_t u = 0;
-            for (int w = 0; w < kTopWarps; ++w) u += S.red[w];
-            if (u > a.uniq_cap) atomicOr(a.err, kErrFallback);
-            *a.d_out_n = u < a.uniq_cap ? u : a.uniq_cap;
-        }
-        __syncthreads();
-    }
-    if (nb == 0) return;
-    const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
-    const uint32_t b1 = (uint32_t)((uint64_t)nb * (blockIdx.x + 1) / gridDim.x);
-    if (b0 >= b1) return;
-    // Keys in the buckets before this range (8 independent loads per thread
-    // in flight).
-    uint32_t part = 0;
-    for (uint32_t x0 = 0; x0 < b0; x0 += 8 * kTopThreads) {
-        uint32_t c[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const uint32_t x = x0 + u * kTopThreads + tid;
-            c[u] = x < b0 ? a.bucket_count[x] : 0u;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) part += min(c[u], kDedupTopBitCap);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
-    if (lane == 0) S.red[warp] = part;
-    __syncthreads();
-    uint64_t range_start = 0;
-    for (int w = 0; w < kTopWarps; ++w) range_start += S.red[w];
-    // The inserts' buckets are the top lg bits (nb = 2^lg, from the count the
-    // inserting kernel sized them by); the next 8 bits spread a bucket.
-    const int lg = 31 - __clz(nb);
-    const int sub_shift = 64 - lg - 8;  // lg <= 14: the next 8 bits exist
-    uint64_t* key = S.key[warp];
-    uint16_t* ord = S.ord[warp];
-    uint32_t* sub = S.sub[warp];
-    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
-    for (uint32_t b = b0 + warp; b < b1; b += kTopWarps) {
-        // Start of bucket b: the range start plus the buckets of the range before it.
-        uint32_t before = 0;
-        for (uint32_t x = b0 + lane; x < b; x += 32) before += min(a.bucket_count[x], kDedupTopBitCap);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xFFFFFFFFu, before, o);
-        const uint64_t start = range_start + before;
-        const uint32_t cnt = min(a.bucket_count[b], kDedupTopBitCap);
-        const uint64_t src = (uint64_t)b * kDedupTopBitCap;
-        for (uint32_t i = lane; i < 256; i += 32) sub[i] = 0;
-        __syncwarp();
-        for (uint32_t j = lane; j < cnt; j += 32) {
-            const uint64_t k = a.bucket_key[src + j];
-            key[j] = k;
-            atomicAdd(&sub[(uint32_t)(k >> sub_shift) & 255u], 1u);
-        }
-        __syncwarp();
-        // Exclusive scan of the 256 sub-bucket counts, 8 per lane.
-        {
-            uint32_t c[8], t = 0;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) { c[q] = sub[lane * 8 + q]; t += c[q]; }
-            uint32_t x = t;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                if (lane >= (uint32_t)o) x += y;
-            }
-            uint32_t run = x - t;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) { sub[lane * 8 + q] = run; run += c[q]; }
-        }
-        __syncwarp();
-        // Each sub-bucket's keys listed together; afterwards sub[s] is the end
-        // of sub-bucket s (the start of s + 1).
-        for (uint32_t j = lane; j < cnt; j += 32)
-            ord[atomicAdd(&sub[(uint32_t)(key[j] >> sub_shift) & 255u], 1u)] = (uint16_t)j;
-        __syncwarp();
-        for (uint32_t j = lane; j < cnt; j += 32) {
-            // Slot, representative and payload loads are in flight while the
-            // rank is counted.
-            const uint32_t s = a.bucket_slot[src + j];
-            const uint32_t rep = a.bucket_rep[src + j];
-            uint8_t m = 0;
-            uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
-            if (a.out_masks) {
-                m = a.masks[rep];
-                const uint4* s4 = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
-                c0 = s4[0];
-                c1 = s4[1];
-            }
-            const uint64_t k = key[j];
-            const uint32_t sb = (uint32_t)(k >> sub_shift) & 255u;
-            const uint32_t end = sub[sb], begin = sb ? sub[sb - 1] : 0u;
-            uint32_t r = begin;
-            for (uint32_t q = begin; q < end; ++q) r += key[ord[q]] < k;
-            const uint64_t uid = start + r;
-            if (uid < a.out_capacity && s < a.table_cap) {
-                a.out_keys[uid] = k;
-                aux[2 * (uint64_t)s + 1] = (uint32_t)uid;
-                a.table_key[s] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
-                if (a.out_masks) {
-                    a.out_masks[uid] = m;
-                    uint4* d4 = reinterpret_cast<uint4*>(a.out_children + uid * 8);
-                    d4[0] = c0;
-                    d4[1] = c1;
-                }
-            } else {
-                atomicOr(a.err, kErrCapacity);
-            }
-        }
-        __syncwarp();  // the bucket's shared arrays are reused by the next one
-    }
-}
-
 __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
     pdl_prologue();
     // The bucket counters, read by dedup_sort, start the next level at zero.
@@ -574,7 +431,6 @@ void dedup_configure(int sms) {
     cudaFuncSetAttribute(dedup_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kDedupMaxSampledBuckets * 8));
     cudaFuncSetAttribute(dedup_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupSampledCapMax * 8));
-    cudaFuncSetAttribute(dedup_sort_topbit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TopBitSmem));
     g_sms = sms > 0 ? sms : 152;
 }
 
@@ -593,15 +449,8 @@ int launch_dedup(const DedupArgs& a, cudaStream_t s) {
         ++launches;
     }
     const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
-    if (a.sampled) {
-        const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
-        launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), kDedupSampledCapMax * 8, s, a);
-    } else {
-        // A few buckets per warp: the bucket count is at most the bound's.
-        const uint64_t want = (nbmax + kTopWarps - 1) / kTopWarps;
-        const int gs = (int)(want < (uint64_t)(12 * g_sms) ? (want > 0 ? want : 1) : 12 * g_sms);
-        launch_pdl(dedup_sort_topbit, dim3(gs), dim3(kTopThreads), sizeof(TopBitSmem), s, a);
-    }
+    const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
+    launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s, a);
     launch_pdl(dedup_map, dim3(gi), dim3(256), 0, s, a);
     return launches + 2;
 }

@@ -212,6 +212,12 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * every workload here (config 3: 7.1 ms against 8.3 ms). Results are
  * identical. */
 #define DAGC_OPT_PDL 7
+/* Batched calls (dagc_create_batched): 1 (default) every chunk's leaves in
+ * one persistent launch that takes per-chunk work items from a device queue
+ * (bins of each chunk's bricks counted, scattered and turned into leaves in
+ * shared memory); 0 the composite-key path (chunk rank above the local code,
+ * one sort or grouping over all chunks). Results are identical. */
+#define DAGC_OPT_BATCH_PATH 12
 /* Failure-path test hooks (off by default; no counterpart in the reference).
  * TEST_SPIN_LIMIT: polls before a bounded device wait of the sorts gives up
  * (0: the production limit, about a second). TEST_STALL_LOOKBACK: 1 makes the
@@ -244,7 +250,8 @@ int dagc_dedup_fallbacks(dagc_context ctx, uint64_t* count);
 #define DAGC_STAGE_GROUP_SKETCH 9      /* its probe (a sampled sketch of the distinct bricks) and the path choice */
 #define DAGC_STAGE_GROUP_AGGREGATE 10  /* its per-partition tables (one read of the partitioned fragments) */
 #define DAGC_STAGE_GROUP_SCATTER 11    /* its partitioning (one read and one write of the fragments) */
-#define DAGC_NUM_STAGES 12
+#define DAGC_STAGE_CHUNK_LEAVES 12     /* batched form: the persistent per-chunk leaf build, scan and pack */
+#define DAGC_NUM_STAGES 13
 int dagc_profile_enable(dagc_context ctx, int enable);
 int dagc_profile_reset(dagc_context ctx);
 int dagc_profile_read(dagc_context ctx, int stage, double* device_ms, uint64_t* launches,

@@ -36,16 +36,64 @@ def make_chunks(chunk_depth, top_levels, k, seed):
     return chunks, morton
 
 
-@pytest.mark.parametrize("chunk_depth,top_levels,k,seed", [(5, 2, 20, 1), (6, 1, 8, 2), (4, 3, 100, 3), (7, 1, 1, 4)])
-def test_batched_equals_per_chunk_merge_and_whole_volume(ctx, chunk_depth, top_levels, k, seed):
+@pytest.mark.parametrize("chunk_depth,top_levels,k,seed", [(5, 2, 20, 1), (6, 1, 8, 2), (4, 3, 100, 3), (7, 1, 1, 4),
+                                                          (8, 1, 6, 5)])
+@pytest.mark.parametrize("path", [1, 0])
+def test_batched_equals_per_chunk_merge_and_whole_volume(chunk_depth, top_levels, k, seed, path):
+    """Both batched paths (1: persistent per-chunk leaves, 0: composite keys)
+    equal the per-chunk CreateDAG + MergeDAGs and the oracle's whole volume."""
     chunks, morton = make_chunks(chunk_depth, top_levels, k, seed)
     counts = np.array([c.size for c in chunks], np.uint64)
     frag = np.concatenate(chunks) if counts.sum() else np.zeros(0, np.uint64)
-    batched = ctx.create_dag_batched(frag, counts, morton, chunk_depth, top_levels).to_host()
-    merged = per_chunk_merge(ctx, chunks, morton, chunk_depth, top_levels).to_host()
     whole = O.create_dag(global_codes(chunks, morton, chunk_depth), chunk_depth + top_levels)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_BATCH_PATH, path)
+        batched = c.create_dag_batched(frag, counts, morton, chunk_depth, top_levels).to_host()
+        merged = per_chunk_merge(c, chunks, morton, chunk_depth, top_levels).to_host()
     assert_dag_equal(batched, whole)
     assert_dag_equal(merged, whole)
+
+
+@pytest.mark.parametrize("path", [1, 0])
+def test_batched_large_uneven_chunks_depth_10(path):
+    """Chunks of 1024^3 (the batched workload's chunk size) with uneven counts,
+    several of them over many 8192-fragment tiles and 2048 bins, some empty:
+    bit-exact against the oracle, called three times (graph replay)."""
+    rng = np.random.default_rng(12)
+    k, cd, top = 9, 10, 1
+    morton = np.arange(8, dtype=np.uint64)[:k] if k <= 8 else None
+    k = 8
+    sizes = [0, 3, 9000, 250_000, 70_000, 0, 600_000, 17]
+    chunks = [random_codes(cd, n, 100 + i, cluster=bool(i % 2)) for i, n in enumerate(sizes)]
+    counts = np.array([c.size for c in chunks], np.uint64)
+    frag = np.concatenate(chunks)
+    whole = O.create_dag(global_codes(chunks, morton, cd), cd + top, threads=8)
+    with D.Context(0) as c:
+        c.set_option(D.OPT_BATCH_PATH, path)
+        for _ in range(3):
+            assert_dag_equal(c.create_dag_batched(frag, counts, morton, cd, top).to_host(), whole)
+
+
+def test_batched_chunk_path_other_sizes_same_shape():
+    """Same buffer, fragment count, chunk count and depths, but other chunk
+    sizes: the recorded call sequence must follow the new sizes."""
+    import torch
+    cd, top = 10, 1
+    rng = np.random.default_rng(13)
+    total = 200_000
+    frag = rng.integers(0, 1 << (3 * cd), total, dtype=np.uint64)
+    d_frag = torch.from_numpy(frag.view(np.int64)).cuda()
+    morton = np.arange(8, dtype=np.uint64)
+    splits = [np.array([0, 10, 20, 30, 40, 50, 60, total - 210], np.uint64),
+              np.array([total - 7 * 9000, 9000, 9000, 9000, 9000, 9000, 9000, 9000], np.uint64)]
+    expect = []
+    for counts in splits:
+        parts = np.split(frag, np.cumsum(counts)[:-1].astype(np.int64))
+        expect.append(O.create_dag(global_codes(parts, morton, cd), cd + top, threads=8))
+    with D.Context(0) as c:
+        for _ in range(3):
+            for counts, ref in zip(splits, expect):
+                assert_dag_equal(c.create_dag_batched(d_frag, counts, morton, cd, top).to_host(), ref)
 
 
 @pytest.mark.parametrize("mode", [0, 2])
@@ -71,11 +119,15 @@ def test_batched_generator_terrain_chunks(ctx):
     assert np.array_equal(words, O.final_dag(whole))
 
 
-def test_batched_rejects_out_of_range_local_code(ctx):
-    chunks = [np.array([1, 2, 3], np.uint64), np.array([1 << 15], np.uint64)]  # 2^15 >= 8^5
-    with pytest.raises(D.DagcError) as e:
-        ctx.create_dag_batched(np.concatenate(chunks), [3, 1], [0, 5], 5, 1)
-    assert e.value.status == D.ERR_BAD_INPUT
+@pytest.mark.parametrize("path", [1, 0])
+@pytest.mark.parametrize("cd", [5, 9])
+def test_batched_rejects_out_of_range_local_code(path, cd):
+    chunks = [np.array([1, 2, 3], np.uint64), np.array([1 << (3 * cd)], np.uint64)]  # = 8^cd
+    with D.Context(0) as c:
+        c.set_option(D.OPT_BATCH_PATH, path)
+        with pytest.raises(D.DagcError) as e:
+            c.create_dag_batched(np.concatenate(chunks), [3, 1], [0, 5], cd, 1)
+        assert e.value.status == D.ERR_BAD_INPUT
 
 
 def test_batched_rejects_unordered_chunks(ctx):
