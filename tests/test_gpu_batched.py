@@ -59,10 +59,8 @@ def test_batched_large_uneven_chunks_depth_10(path):
     """Chunks of 1024^3 (the batched workload's chunk size) with uneven counts,
     several of them over many 8192-fragment tiles and 2048 bins, some empty:
     bit-exact against the oracle, called three times (graph replay)."""
-    rng = np.random.default_rng(12)
-    k, cd, top = 9, 10, 1
-    morton = np.arange(8, dtype=np.uint64)[:k] if k <= 8 else None
-    k = 8
+    cd, top = 10, 1
+    morton = np.arange(8, dtype=np.uint64)
     sizes = [0, 3, 9000, 250_000, 70_000, 0, 600_000, 17]
     chunks = [random_codes(cd, n, 100 + i, cluster=bool(i % 2)) for i, n in enumerate(sizes)]
     counts = np.array([c.size for c in chunks], np.uint64)
