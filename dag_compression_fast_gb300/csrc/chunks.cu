@@ -6,8 +6,9 @@
 //
 // Every chunk's local brick space (bricks = local code >> 6, 3*chunk_depth - 6
 // bits) is cut into 2^bin_bits bins of 2^D bricks each, D <= 13, so that one
-// bin's leaf masks fit a direct-mapped array in shared memory: the bricks of a
-// bin come out in ascending order by scanning that array, with no sort. One
+// bin's leaf masks fit a direct-mapped array in shared memory, with a bitmap
+// of the bricks present: the bricks of a bin come out in ascending order by
+// walking the bitmap, with no sort. One
 // persistent grid takes work items from a device counter, in this order:
 //   COUNT(c, t)   tile t of chunk c: the chunk's bin histogram;
 //   SCATTER(c, t) tile t of chunk c, after all of c's COUNT tiles: fragments
@@ -35,14 +36,20 @@ constexpr int kDirect = 1 << kChunkDirectBits;
 constexpr int kPerThread = kChunkTile / kT;
 static_assert(kChunkTile % kT == 0 && kDirect % kT == 0 && kMaxBins % kT == 0, "chunk shapes");
 
+constexpr int kBitmapWords = kDirect / 32;
+static_assert(kBitmapWords <= kT, "one bitmap word per thread");
+
 struct ChunkSmem {
-    union {
-        struct {
-            uint32_t tcnt[kMaxBins];   // this tile's fragments per bin (then its reservation base)
-            uint32_t start[kMaxBins];  // the chunk's bin starts (exclusive scan of its histogram)
-        } bins;
-        uint64_t masks[kDirect];       // one bin's leaf masks, by brick
-    } u;
+    struct {
+        uint32_t tcnt[kMaxBins];   // this tile's fragments per bin (then its reservation base)
+        uint32_t start[kMaxBins];  // the chunk's bin starts (exclusive scan of its histogram)
+    } bins;
+    // One bin's leaf masks, by brick, as two 32-bit halves (native shared
+    // atomics); zero between bins (the emission clears what it reads), and a
+    // bitmap of the bricks present.
+    uint32_t masks[2 * kDirect];
+    uint32_t present[kBitmapWords];
+    uint32_t bin_cnt[kChunkGroupBins];  // fragments of the LEAVES item's bins
     uint32_t scan[34];
     uint32_t item;
     uint64_t running;
@@ -91,6 +98,7 @@ __global__ void __launch_bounds__(kT) chunk_leaves(ChunkArgs a) {
     const uint32_t tiles = __ldg(a.tile_off + a.k);
     const uint32_t total = 2 * tiles + a.k * a.groups_per_chunk;
     bool bad = false;
+    for (uint32_t x = tid; x < 2u * kDirect; x += kT) S.masks[x] = 0;
     while (true) {
         if (tid == 0) S.item = atomicAdd(a.work, 1u);
         __syncthreads();
@@ -121,11 +129,11 @@ __global__ void __launch_bounds__(kT) chunk_leaves(ChunkArgs a) {
                 uint32_t run = block_exclusive_sum<uint32_t>(sum, S.scan, &tot);
 #pragma unroll
                 for (int q = 0; q < kPer; ++q) {
-                    S.u.bins.start[tid * kPer + q] = run;
+                    S.bins.start[tid * kPer + q] = run;
                     run += h[q];
                 }
             }
-            for (uint32_t b = tid; b < nb; b += kT) S.u.bins.tcnt[b] = 0;
+            for (uint32_t b = tid; b < nb; b += kT) S.bins.tcnt[b] = 0;
             __syncthreads();
             uint32_t br[kPerThread];  // bin << 16 | rank of the fragment among the tile's of its bin
 #pragma unroll
@@ -137,14 +145,14 @@ __global__ void __launch_bounds__(kT) chunk_leaves(ChunkArgs a) {
                     if (code >= code_limit) bad = true;
                     uint32_t bin = (uint32_t)((code >> 6) >> dbits);
                     bin = bin < nb ? bin : nb - 1;
-                    const uint32_t r = atomicAdd(&S.u.bins.tcnt[bin], 1u);
+                    const uint32_t r = atomicAdd(&S.bins.tcnt[bin], 1u);
                     br[q] = bin << 16 | r;
                 }
             }
             __syncthreads();
             if (!scatter) {
                 for (uint32_t b = tid; b < nb; b += kT) {
-                    const uint32_t x = S.u.bins.tcnt[b];
+                    const uint32_t x = S.bins.tcnt[b];
                     if (x) atomicAdd(hist + b, x);
                 }
                 __threadfence();  // every thread's counts land before the tile is marked done
@@ -157,15 +165,15 @@ __global__ void __launch_bounds__(kT) chunk_leaves(ChunkArgs a) {
             }
             // One reservation per bin and tile.
             for (uint32_t b = tid; b < nb; b += kT) {
-                const uint32_t x = S.u.bins.tcnt[b];
-                if (x) S.u.bins.tcnt[b] = atomicAdd(a.cursor + (uint64_t)c * nb + b, x);
+                const uint32_t x = S.bins.tcnt[b];
+                if (x) S.bins.tcnt[b] = atomicAdd(a.cursor + (uint64_t)c * nb + b, x);
             }
             __syncthreads();
 #pragma unroll
             for (int q = 0; q < kPerThread; ++q) {
                 if (br[q] == 0xFFFFFFFFu) continue;
                 const uint32_t i = q * kT + tid, bin = br[q] >> 16;
-                const uint64_t dst = c0 + S.u.bins.start[bin] + S.u.bins.tcnt[bin] + (br[q] & 0xFFFFu);
+                const uint64_t dst = c0 + S.bins.start[bin] + S.bins.tcnt[bin] + (br[q] & 0xFFFFu);
                 if (dst < c1) a.scratch[dst] = __ldg(a.frags + f0 + i);
                 else bad = true;  // only after a timed-out wait
             }
@@ -196,34 +204,50 @@ __global__ void __launch_bounds__(kT) chunk_leaves(ChunkArgs a) {
             gstart += tot;
         }
         if (tid == 0) S.running = 0;
+        if (nb > 1 && tid < b1 - b0) S.bin_cnt[tid] = hist[b0 + tid];
+        __syncthreads();
         uint64_t fstart = gstart;
         for (uint32_t b = b0; b < b1; ++b) {
-            const uint64_t cnt = nb > 1 ? hist[b] : c1 - c0;
+            const uint64_t cnt = nb > 1 ? S.bin_cnt[b - b0] : c1 - c0;
             if (cnt == 0) continue;
-            for (uint32_t x = tid; x < dsize; x += kT) S.u.masks[x] = 0;
+            if (tid < (uint32_t)kBitmapWords) S.present[tid] = 0;
             __syncthreads();
-            for (uint64_t i = tid; i < cnt; i += kT) {
-                const uint64_t code = src[fstart + i];
-                if (nb == 1 && code >= code_limit) bad = true;
-                atomicOr((unsigned long long*)&S.u.masks[(code >> 6) & (dsize - 1)], 1ull << (code & 63));
+            // Four fragments per thread in flight, then their updates: the
+            // voxel bit goes to its brick's low or high half; the first bit
+            // of a half marks the brick present.
+            for (uint64_t i0 = tid; i0 < cnt; i0 += 4 * kT) {
+                uint64_t code[4];
+                bool in[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint64_t i = i0 + (uint64_t)u * kT;
+                    in[u] = i < cnt;
+                    code[u] = in[u] ? src[fstart + i] : 0ull;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (!in[u]) continue;
+                    if (nb == 1 && code[u] >= code_limit) bad = true;
+                    const uint32_t e = (uint32_t)(code[u] >> 6) & (dsize - 1);
+                    const uint32_t v = (uint32_t)code[u] & 63u;
+                    const uint32_t old = atomicOr(&S.masks[2 * e + (v >> 5)], 1u << (v & 31));
+                    if (old == 0) atomicOr(&S.present[e >> 5], 1u << (e & 31));
+                }
             }
             fstart += cnt;
             __syncthreads();
-            // The bin's non-empty bricks, in order: kPer consecutive entries
-            // per thread, a block scan for their output positions.
-            const uint32_t per = dsize >= (uint32_t)kT ? dsize / kT : 1u;
-            const uint32_t e0 = tid * per;
-            uint32_t nz = 0;
-            for (uint32_t q = 0; q < per; ++q)
-                if (e0 + q < dsize && S.u.masks[e0 + q]) ++nz;
+            // The bin's bricks in order: thread t owns bitmap word t (bricks
+            // 32t .. 32t + 31); a block scan of the words' counts gives the
+            // output positions. Every mask read is cleared for the next bin.
+            const uint32_t word = tid < (uint32_t)kBitmapWords ? S.present[tid] : 0u;
             uint32_t tot;
-            uint32_t pos = block_exclusive_sum<uint32_t>(nz, S.scan, &tot);
+            uint32_t pos = block_exclusive_sum<uint32_t>((uint32_t)__popc(word), S.scan, &tot);
             const uint64_t out0 = gstart + S.running;
-            for (uint32_t q = 0; q < per; ++q) {
-                const uint32_t e = e0 + q;
-                if (e >= dsize) break;
-                const uint64_t m = S.u.masks[e];
-                if (!m) continue;
+            for (uint32_t w = word; w; w &= w - 1) {
+                const uint32_t e = tid * 32 + (__ffs(w) - 1);
+                const uint64_t m = (uint64_t)S.masks[2 * e] | (uint64_t)S.masks[2 * e + 1] << 32;
+                S.masks[2 * e] = 0;
+                S.masks[2 * e + 1] = 0;
                 const uint64_t o = out0 + pos++;
                 if (o < c1) {
                     a.stage_parent[o] = pbase | ((uint64_t)b << dbits) | e;
@@ -266,20 +290,28 @@ __global__ void __launch_bounds__(1024) chunk_scan(ChunkArgs a) {
     }
 }
 
-// Packs each item's bricks (a warp per item) into the ascending list.
+// Packs the items' bricks into the ascending list: every thread moves a run
+// of consecutive output bricks (balanced whatever the items' sizes), finding
+// the item of its first brick by binary search over the items' output
+// starts and walking forward from there.
+constexpr int kCopyPer = 8;
 __global__ void __launch_bounds__(256) chunk_copy(ChunkArgs a) {
     pdl_prologue();
     const uint32_t g = a.k * a.groups_per_chunk;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x / 32);
-    for (uint32_t w = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); w < g; w += warps) {
-        const uint32_t cnt = a.group_bricks[w];
-        const uint64_t src = a.group_src[w], dst = a.group_dst[w];
-        for (uint32_t i = lane; i < cnt; i += 32) {
-            if (dst + i < a.out_capacity) {
-                a.parents[dst + i] = a.stage_parent[src + i];
-                a.leaves[dst + i] = a.stage_mask[src + i];
-            }
+    const uint64_t total = *a.d_out_n;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kCopyPer;
+    for (uint64_t j0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kCopyPer; j0 < total; j0 += stride) {
+        uint32_t lo = 0, hi = g;  // group_dst[lo] <= j0 < group_dst[hi] (ascending)
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (a.group_dst[mid] <= j0) lo = mid; else hi = mid;
+        }
+        uint32_t w = lo;
+        for (uint64_t j = j0; j < j0 + kCopyPer && j < total; ++j) {
+            while (w + 1 < g && a.group_dst[w + 1] <= j) ++w;
+            const uint64_t src = a.group_src[w] + (j - a.group_dst[w]);
+            a.parents[j] = a.stage_parent[src];
+            a.leaves[j] = a.stage_mask[src];
         }
     }
 }
@@ -305,9 +337,10 @@ void launch_chunk_leaves(const ChunkArgs& a, cudaStream_t s) {
     const int grid = (int)(items < (uint64_t)g_chunk_ctas ? (items ? items : 1) : g_chunk_ctas);
     launch_pdl(chunk_leaves, dim3(grid), dim3(kT), sizeof(ChunkSmem), s, a);
     launch_pdl(chunk_scan, dim3(1), dim3(1024), 0, s, a);
-    const uint64_t g = (uint64_t)a.k * a.groups_per_chunk;
-    const uint64_t blocks = (g + 7) / 8;
-    launch_pdl(chunk_copy, dim3((unsigned)(blocks < 4096 ? (blocks ? blocks : 1) : 4096)), dim3(256), 0, s, a);
+    // The brick total is on the device: the grid covers the bound and extra
+    // threads leave at once.
+    const uint64_t blocks = (a.out_capacity + 256ull * kCopyPer - 1) / (256ull * kCopyPer);
+    launch_pdl(chunk_copy, dim3((unsigned)(blocks < 8192 ? (blocks ? blocks : 1) : 8192)), dim3(256), 0, s, a);
 }
 
 }  // namespace dagc
