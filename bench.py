@@ -373,17 +373,25 @@ def main():
                 "mode": "dagc_compress_host, one call per step, each waiting for the previous"}
 
     # ---- end to end through the serving API: the same steps as jobs of a
-    # two-slot server (dagc_server_submit / dagc_server_wait). Every step still
-    # copies its pinned host fragments in and its words out inside the timed
-    # region; a step's host->device copy overlaps the previous step's kernels. ----
+    # two-slot server (dagc_server_submit_into / dagc_server_wait), at most
+    # three in flight. Every step still copies its pinned host fragments in
+    # and its words out (into pinned host buffers) inside the timed region; a
+    # step's copies overlap another step's kernels. ----
     sv = D.Server(local, slots=2, hbm_budget_bytes=256 << 30)
-    for _ in range(max(args.warmup, 2)):
-        sv.wait(sv.submit(h_view, depth))
+    window = 3
+    outs = [torch.empty(n_words, dtype=torch.int32).pin_memory().numpy().view(np.uint32) for _ in range(window)]
+    for i in range(max(args.warmup, 2)):
+        sv.wait(sv.submit_into(h_view, depth, outs[i % window]))
     barrier()
     t0 = time.perf_counter()
-    tickets = [sv.submit(h_view, depth) for _ in range(args.steps)]
+    pending = []
     pipe_words = 0
-    for tk in tickets:
+    for i in range(args.steps):
+        if len(pending) == window:
+            w_out, _ = sv.wait(pending.pop(0))
+            pipe_words = len(w_out)
+        pending.append(sv.submit_into(h_view, depth, outs[i % window]))
+    for tk in pending:
         w_out, _ = sv.wait(tk)
         pipe_words = len(w_out)
     pipe_s = max_over_ranks(time.perf_counter() - t0)
@@ -391,10 +399,12 @@ def main():
     del h_codes, h_view, h_words
     if pipe_words != int(nw.value):
         raise RuntimeError("serving path returned a different word count")
-    e2e = {"value": n * args.steps * world / pipe_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
-           "d2h_bytes_per_step": 4 * pipe_words,
-           "mode": "serving API, 2 slots: per step pinned host fragments -> device -> host words, "
-                   "steps overlapped (wall clock over K steps)"}
+    e2e_serving = {"value": n * args.steps * world / pipe_s, "unit": UNIT, "h2d_bytes_per_step": 8 * n,
+                   "d2h_bytes_per_step": 4 * pipe_words,
+                   "mode": "serving API, 2 slots, 3 jobs in flight: per step pinned host fragments -> device -> "
+                           "pinned host words, steps overlapped (wall clock over K steps)"}
+    # The headline e2e is the faster of the two ways through the public API.
+    e2e = dict(e2e_serving if e2e_serving["value"] >= e2e_sync["value"] else e2e_sync)
 
     # ---- roofline of the dominant kernel of the path the device chose ----
     # Fragments with few per brick are radix-sorted (the digit pass
@@ -417,6 +427,7 @@ def main():
                    "nodes_per_level": counts[3:]},
         "e2e": e2e,
         "e2e_sync": e2e_sync,
+        "e2e_serving": e2e_serving,
         "roofline": roofline,
         "gpu_launches": int(launches),
         "stages": stage_table(prof, args.steps),

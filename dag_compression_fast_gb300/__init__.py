@@ -68,7 +68,7 @@ DAGC_SYMBOLS = [
     "dagc_last_counts", "dagc_set_option", "dagc_dedup_fallbacks", "dagc_trace", "dagc_trace_camera", "dagc_voxelize", "dagc_profile_enable", "dagc_profile_reset",
     "dagc_profile_read", "dagc_kernel_launches", "dagc_sort_keys", "dagc_sort_pairs",
     "dagc_tune_sort", "dagc_tune_save", "dagc_tune_load", "dagc_tune_clear", "dagc_sort_plan",
-    "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_wait",
+    "dagc_sort_keys_noalloc", "dagc_server_create", "dagc_server_submit", "dagc_server_submit_into", "dagc_server_wait",
     "dagc_server_stats", "dagc_server_shared_dag", "dagc_server_folds", "dagc_server_timeline", "dagc_server_set_option",
     "dagc_server_destroy", "dagc_union", "dagc_dag_lift",
 ]
@@ -130,6 +130,7 @@ def lib() -> ctypes.CDLL:
         L.dagc_create_footprint.restype = u64
         L.dagc_server_create.argtypes = [i32, i32, u64, pvp]
         L.dagc_server_submit.argtypes = [vp, vp, u64, i32, ctypes.c_int64, pu64]
+        L.dagc_server_submit_into.argtypes = [vp, vp, u64, i32, ctypes.c_int64, vp, u64, pu64]
         L.dagc_server_wait.argtypes = [vp, u64, vp, u64, pu64, ctypes.POINTER(ctypes.c_double)]
         L.dagc_server_stats.argtypes = [vp, pu64, pu64, pu64, pu64]
         L.dagc_server_shared_dag.argtypes = [vp, i32, pvp, pvp]
@@ -681,6 +682,7 @@ class Server:
         self.handle = h.value
         self.device = device
         self._inputs = {}
+        self._outputs = {}
         self._shared = []  # DAGs on the server's merge context: freed before it
 
     def submit(self, fragments: np.ndarray, depth: int, chunk_morton: int = -1) -> int:
@@ -692,6 +694,21 @@ class Server:
         self._inputs[t.value] = a  # keep alive until the job is collected
         return t.value
 
+    def submit_into(self, fragments: np.ndarray, depth: int, out: np.ndarray, chunk_morton: int = -1) -> int:
+        """submit() with the words written straight into `out` (uint32, ideally
+        page-locked memory); wait() then returns a view of it."""
+        a = np.ascontiguousarray(fragments, dtype=np.uint64)
+        if out.dtype != np.uint32 or not out.flags.c_contiguous:
+            raise DagcError(ERR_INVALID_ARGUMENT, "out must be a contiguous uint32 array")
+        t = ctypes.c_uint64(0)
+        st = lib().dagc_server_submit_into(self.handle, _np_ptr(a), a.size, depth, chunk_morton, _np_ptr(out),
+                                           out.size, ctypes.byref(t))
+        if st:
+            raise DagcError(st, "dagc_server_submit_into failed")
+        self._inputs[t.value] = a
+        self._outputs[t.value] = out
+        return t.value
+
     def wait(self, ticket: int):
         """(words, latency_ms) of a finished job."""
         n = ctypes.c_uint64(0)
@@ -699,7 +716,12 @@ class Server:
         st = lib().dagc_server_wait(self.handle, ticket, None, 0, ctypes.byref(n), ctypes.byref(lat))
         if st:
             self._inputs.pop(ticket, None)
+            self._outputs.pop(ticket, None)
             raise DagcError(st, "job failed")
+        out = self._outputs.pop(ticket, None)
+        if out is not None and n.value <= out.size:
+            self._inputs.pop(ticket, None)
+            return out[: n.value], lat.value
         out = np.zeros(n.value, np.uint32)
         st = lib().dagc_server_wait(self.handle, ticket, _np_ptr(out), out.size, ctypes.byref(n), ctypes.byref(lat))
         self._inputs.pop(ticket, None)

@@ -334,11 +334,34 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     uint64_t start = 0;
     for (int w = 0; w < kBucketThreads / 32; ++w) start += red[w];
     uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
+    // Top-bit form: a bucket's keys share their top lg bits (nb = 2^lg) and
+    // the next 8 bits spread them evenly over 256 sub-buckets; a key is
+    // ranked among the few keys of its own sub-bucket. (The sampled form's
+    // keys are not uniform: they are ranked against the whole bucket.)
+    __shared__ uint32_t sstart[kBucketThreads], scur[kBucketThreads], sscan[34];
+    __shared__ uint16_t ord[kDedupTopBitCap];
+    static_assert(kBucketThreads == 256, "one sub-bucket per thread");
+    const bool subs = !a.sampled;
+    const int sub_shift = subs ? 64 - (31 - __clz(nb)) - 8 : 0;
     for (uint32_t b = b0; b < b1; ++b) {
         const uint32_t cnt = min(a.bucket_count[b], cap);
         const uint64_t src = (uint64_t)b * cap;
         __syncthreads();  // the previous bucket's keys are no longer read
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) key[j] = a.bucket_key[src + j];
+        if (subs) {
+            scur[tid] = 0;
+            __syncthreads();
+            for (uint32_t j = tid; j < cnt; j += kBucketThreads)
+                atomicAdd(&scur[(uint32_t)(key[j] >> sub_shift) & 255u], 1u);
+            __syncthreads();
+            uint32_t tot;
+            const uint32_t ex = block_exclusive_sum<uint32_t>(scur[tid], sscan, &tot);
+            sstart[tid] = ex;
+            scur[tid] = ex;
+            __syncthreads();
+            for (uint32_t j = tid; j < cnt; j += kBucketThreads)
+                ord[atomicAdd(&scur[(uint32_t)(key[j] >> sub_shift) & 255u], 1u)] = (uint16_t)j;
+        }
         __syncthreads();
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
             // Slot and representative come with the key; their loads (and the
@@ -355,8 +378,15 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
             }
             const uint64_t k = key[j];
             uint32_t r = 0;
+            if (subs) {
+                const uint32_t sb = (uint32_t)(k >> sub_shift) & 255u;
+                const uint32_t end = sb < 255u ? sstart[sb + 1] : cnt;
+                r = sstart[sb];
+                for (uint32_t q = sstart[sb]; q < end; ++q) r += key[ord[q]] < k;
+            } else {
 #pragma unroll 8
-            for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
+                for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
+            }
             const uint64_t uid = start + r;
             if (uid < a.out_capacity && s < a.table_cap) {
                 a.out_keys[uid] = k;

@@ -48,6 +48,10 @@ struct Request {
     int status = DAGC_OK;
     std::string error;
     std::vector<uint32_t> words;
+    uint32_t* h_out = nullptr;  // caller's word buffer (dagc_server_submit_into), or null
+    uint64_t out_cap = 0;
+    uint64_t n_out = 0;          // words written to h_out
+    bool into = false;           // the words went to h_out
     bool done = false;
     double gpu_start_ms = -1, gpu_end_ms = -1;  // device interval of its work (see dagc_server_timeline)
 };
@@ -151,7 +155,17 @@ void worker_loop(dagc_server_t* sv, int slot) {
             if (!st) st = dagc_final(ctx, dag, stream, &d_words, &nw);
             else if (dag) dagc_dag_free(dag);
             if (!st && ev1) cudaEventRecord(ev1, stream);
-            if (!st) {
+            if (!st && r->h_out && nw <= r->out_cap) {
+                // Straight into the caller's buffer (pinned memory makes this
+                // a DMA at link speed).
+                cudaError_t e = nw ? cudaMemcpyAsync(r->h_out, d_words, nw * 4, cudaMemcpyDeviceToHost, stream)
+                                   : cudaSuccess;
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) { cudaGetLastError(); st = DAGC_ERR_CUDA; }
+                dagc_free_words(ctx, d_words, stream);
+                r->n_out = nw;
+                r->into = true;
+            } else if (!st) {
                 words.resize(nw);
                 st = dagc_words_download(ctx, d_words, nw, words.data());
                 dagc_free_words(ctx, d_words, stream);
@@ -293,8 +307,15 @@ int dagc_server_create(int device, int slots, uint64_t hbm_budget_bytes, dagc_se
 
 int dagc_server_submit(dagc_server sv, const uint64_t* h_fragments, uint64_t n, int depth, int64_t chunk_morton,
                        uint64_t* ticket) {
+    return dagc_server_submit_into(sv, h_fragments, n, depth, chunk_morton, nullptr, 0, ticket);
+}
+
+int dagc_server_submit_into(dagc_server sv, const uint64_t* h_fragments, uint64_t n, int depth, int64_t chunk_morton,
+                            uint32_t* h_words, uint64_t capacity, uint64_t* ticket) {
     if (!sv || !ticket || (n && !h_fragments) || depth < 2 || depth > 21) return DAGC_ERR_INVALID_ARGUMENT;
     auto r = std::make_shared<Request>();
+    r->h_out = h_words;
+    r->out_cap = h_words ? capacity : 0;
     r->h_fragments = h_fragments;
     r->n = n;
     r->depth = depth;
@@ -329,10 +350,15 @@ int dagc_server_wait(dagc_server sv, uint64_t ticket, uint32_t* h_words, uint64_
         r = it->second;
         sv->cv_done.wait(lock, [&] { return r->done; });
     }
-    *n_words = r->words.size();
+    *n_words = r->into ? r->n_out : r->words.size();
     if (latency_ms)
         *latency_ms = std::chrono::duration<double, std::milli>(r->finished - r->submitted).count();
     if (r->status) return r->status;
+    if (r->into) {  // already in the caller's buffer: collected
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->requests.erase(ticket);
+        return DAGC_OK;
+    }
     if (h_words) {
         if (capacity < r->words.size()) return DAGC_ERR_INVALID_ARGUMENT;
         if (!r->words.empty()) std::memcpy(h_words, r->words.data(), r->words.size() * 4);

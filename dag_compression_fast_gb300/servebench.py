@@ -65,7 +65,29 @@ def run_rate(srv, jobs, rate: float, seed: int):
     wall = time.perf_counter() - start
     frags = sum(int(c.size) for c, _, _ in jobs)
     return {"rate_per_s": rate, "jobs": len(jobs), "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "voxels_per_s": frags / wall, "wall_s": wall}
+            "p99_ms": float(np.percentile(lat, 99)), "voxels_per_s": frags / wall, "wall_s": wall,
+            "device_overlap": device_overlap([srv.timeline(t) for t in tickets])}
+
+
+def device_overlap(intervals):
+    """From the jobs' device intervals (CUDA events on each slot's stream):
+    pairs of jobs whose work was on the GPU at the same time, and the sum of
+    the intervals over their union (1.0: never more than one job at a time)."""
+    iv = sorted((a, b) for a, b in intervals if b > a >= 0)
+    pairs = sum(1 for i in range(len(iv)) for j in range(i + 1, len(iv)) if iv[j][0] < iv[i][1])
+    union, cur_a, cur_b = 0.0, None, None
+    for a, b in iv:
+        if cur_b is None or a > cur_b:
+            if cur_b is not None:
+                union += cur_b - cur_a
+            cur_a, cur_b = a, b
+        else:
+            cur_b = max(cur_b, b)
+    if cur_b is not None:
+        union += cur_b - cur_a
+    total = sum(b - a for a, b in iv)
+    return {"overlapping_pairs": pairs, "busy_ms": round(union, 3),
+            "concurrency": round(total / union, 3) if union > 0 else None}
 
 
 def main(argv=None) -> int:

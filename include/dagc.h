@@ -384,6 +384,12 @@ int dagc_server_create(int device, int slots, uint64_t hbm_budget_bytes, dagc_se
  * dagc_server_shared_dag. */
 int dagc_server_submit(dagc_server server, const uint64_t* h_fragments, uint64_t n, int depth,
                        int64_t chunk_morton, uint64_t* ticket);
+/* The same, with the job's words copied straight into h_words (capacity
+ * words; page-locked memory makes the copy a DMA) when they fit: the job is
+ * then collected by its first dagc_server_wait, which only reports *n_words.
+ * Words that do not fit are kept as for dagc_server_submit. */
+int dagc_server_submit_into(dagc_server server, const uint64_t* h_fragments, uint64_t n, int depth,
+                            int64_t chunk_morton, uint32_t* h_words, uint64_t capacity, uint64_t* ticket);
 /* Blocks until the job is done. With h_words == NULL only *n_words (and the
  * latency from submission to completion) is returned; otherwise the words are
  * copied out (capacity >= *n_words) and the job is forgotten. */

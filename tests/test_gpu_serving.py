@@ -125,3 +125,20 @@ def test_jobs_overlap_on_the_device(ctx):
         assert overlaps >= 1
     finally:
         srv.close()
+
+
+def test_submit_into_caller_buffers(ctx):
+    """Words written straight into the caller's buffers equal the plain
+    submit's; a buffer too small keeps the words inside the server."""
+    jobs = job_mix(17)[:6]
+    alone = [ctx.compress_host(codes, depth) for codes, depth in jobs]
+    srv = D.Server(0, slots=3, hbm_budget_bytes=32 << 30)
+    try:
+        outs = [np.zeros(w.size + 7, np.uint32) for w in alone]
+        outs[2] = np.zeros(max(alone[2].size - 1, 1), np.uint32)  # too small
+        tickets = [srv.submit_into(codes, depth, out) for (codes, depth), out in zip(jobs, outs)]
+        for t, ref in zip(tickets, alone):
+            words, _ = srv.wait(t)
+            assert np.array_equal(words, ref)
+    finally:
+        srv.close()
