@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
         }
     }
     const bool read_first = n > kDedupClaimFirstMax;
-    uint32_t* aux = reinterpret_cast<uint32_t*>(dd.table_aux);  // [2s] representative, [2s+1] unique id
+    uint32_t* aux = reinterpret_cast<uint32_t*>(dd.table_aux);  // slot s: [4s] representative, [4s+1] unique id
     bool bad = false, full = false, overflow = false;
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
     while (true) {
@@ -341,9 +341,9 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
                     bad = true;  // 0 marks an empty slot
                 } else {
                     for (uint64_t probe = 0; probe < tslots; ++probe) {
-                        uint64_t cur = read_first ? ld_relaxed(dd.table_key + sl) : 0ull;
+                        uint64_t cur = read_first ? ld_relaxed(dd.table_key + 2 * sl) : 0ull;
                         if (cur == 0)
-                            cur = atomicCAS((unsigned long long*)(dd.table_key + sl), 0ull, (unsigned long long)hv);
+                            cur = atomicCAS((unsigned long long*)(dd.table_key + 2 * sl), 0ull, (unsigned long long)hv);
                         if (cur == 0 || cur == hv) { won = cur == 0; placed = true; break; }
                         sl = (sl + 1) & (tslots - 1);
                     }
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
                 if (!placed && hv != 0) full = true;
                 dd.item_slot[p] = placed ? (uint32_t)sl : 0xFFFFFFFFu;
                 if (won) {
-                    aux[2 * sl] = (uint32_t)p;
+                    aux[4 * sl] = (uint32_t)p;
                     const uint32_t b = shift >= 64 ? 0u : (uint32_t)(hv >> shift);
                     const uint32_t bs = atomicAdd(dd.bucket_count + b, 1u);
                     if (bs < kDedupTopBitCap) {

@@ -896,12 +896,12 @@ int reserve_table(dagc_context ctx, uint64_t slots, cudaStream_t s) {
         if (ctx->table) cudaFree(ctx->table);
         ctx->table = nullptr;
         ctx->table_cap = 0;
-        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 16));  // keys u64 | aux u64
+        DAGC_CUDA(ctx, cudaMalloc(&ctx->table, slots * 16));  // per slot: key u64, aux u64
         ctx->table_cap = slots;
         ctx->table_dirty = true;
     }
     if (ctx->table_dirty) {
-        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 8, s));
+        DAGC_CUDA(ctx, cudaMemsetAsync(ctx->table, 0, ctx->table_cap * 16, s));
         ctx->table_dirty = false;
     }
     if (!ctx->gtable && ctx->group_mode != 0) DAGC_CUDA(ctx, cudaMalloc(&ctx->gtable, kGroupScratchBytes));
@@ -1126,7 +1126,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.sampled = masks == nullptr;  // leaf masks are not uniformly distributed; node hashes are
             d.item_cap = Lo.item_cap;
             d.table_key = static_cast<uint64_t*>(ctx->table);
-            d.table_aux = static_cast<uint64_t*>(ctx->table) + ctx->table_cap;
+            d.table_aux = static_cast<uint64_t*>(ctx->table) + 1;
             d.table_cap = ctx->table_cap;
             d.item_slot = P32(Lo.o_islot);
             d.uniq_key = P64(Lo.o_ukey);

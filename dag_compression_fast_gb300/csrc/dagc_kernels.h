@@ -270,8 +270,10 @@ struct DedupArgs {
     const uint8_t* masks; const uint32_t* children;  // item payloads (null for leaves)
     bool sampled;                                    // leaf masks: splitters from a sample; else top bits
     uint64_t item_cap;
-    // Table of table_cap slots (a power of two): keys, 0 = empty (all 0 on
-    // entry and exit); aux = representative item | unique id << 32.
+    // Table of table_cap slots (a power of two), 16 bytes each so that a
+    // slot's key and aux share a sector: table_key[2s] = key, 0 = empty (all
+    // 0 on entry and exit); table_aux[2s] = representative item | unique id
+    // << 32 (table_aux = table_key + 1).
     uint64_t* table_key; uint64_t* table_aux; uint64_t table_cap;
     uint32_t* item_slot;
     uint64_t* uniq_key; uint32_t* uniq_slot; uint32_t* uniq_item; uint64_t uniq_cap;

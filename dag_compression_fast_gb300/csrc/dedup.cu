@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         }
         if (gtid == 0) a.state->nbuckets = nb;
     }
-    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);  // [2s] representative, [2s+1] unique id
+    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);  // slot s: [4s] representative, [4s+1] unique id
     const uint64_t warps = gsize / 32;
     const uint64_t warp = gtid / 32;
     bool bad = false, full = false;
@@ -118,13 +118,13 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
             if (read_first) {
 #pragma unroll
                 for (int k = 0; k < kIlp; ++k)
-                    if (pend[k]) cur[k] = ld_relaxed(a.table_key + s[k]);
+                    if (pend[k]) cur[k] = ld_relaxed(a.table_key + 2 * s[k]);
             }
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) claim[k] = pend[k] && cur[k] == 0;
 #pragma unroll
             for (int k = 0; k < kIlp; ++k)
-                if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + s[k]), 0ull, (unsigned long long)h[k]);
+                if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + 2 * s[k]), 0ull, (unsigned long long)h[k]);
             bool any = false;
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                 if (won[k]) {
                     const uint64_t i = base + k * 32 + lane;
                     const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
-                    aux[2 * s[k]] = (uint32_t)i;
+                    aux[4 * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap) {
                         a.uniq_key[pos] = h[k];
                         a.uniq_slot[pos] = (uint32_t)s[k];
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     const uint64_t i = base + k * 32 + lane;
                     const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
                     const uint32_t b = shift >= 64 ? 0u : (uint32_t)(h[k] >> shift);
-                    aux[2 * s[k]] = (uint32_t)i;
+                    aux[4 * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap && bslot[k] < kDedupTopBitCap) {
                         const uint64_t e = (uint64_t)b * kDedupTopBitCap + bslot[k];
                         a.bucket_key[e] = h[k];
@@ -334,34 +334,11 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     uint64_t start = 0;
     for (int w = 0; w < kBucketThreads / 32; ++w) start += red[w];
     uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
-    // Top-bit form: a bucket's keys share their top lg bits (nb = 2^lg) and
-    // the next 8 bits spread them evenly over 256 sub-buckets; a key is
-    // ranked among the few keys of its own sub-bucket. (The sampled form's
-    // keys are not uniform: they are ranked against the whole bucket.)
-    __shared__ uint32_t sstart[kBucketThreads], scur[kBucketThreads], sscan[34];
-    __shared__ uint16_t ord[kDedupTopBitCap];
-    static_assert(kBucketThreads == 256, "one sub-bucket per thread");
-    const bool subs = !a.sampled;
-    const int sub_shift = subs ? 64 - (31 - __clz(nb)) - 8 : 0;
     for (uint32_t b = b0; b < b1; ++b) {
         const uint32_t cnt = min(a.bucket_count[b], cap);
         const uint64_t src = (uint64_t)b * cap;
         __syncthreads();  // the previous bucket's keys are no longer read
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) key[j] = a.bucket_key[src + j];
-        if (subs) {
-            scur[tid] = 0;
-            __syncthreads();
-            for (uint32_t j = tid; j < cnt; j += kBucketThreads)
-                atomicAdd(&scur[(uint32_t)(key[j] >> sub_shift) & 255u], 1u);
-            __syncthreads();
-            uint32_t tot;
-            const uint32_t ex = block_exclusive_sum<uint32_t>(scur[tid], sscan, &tot);
-            sstart[tid] = ex;
-            scur[tid] = ex;
-            __syncthreads();
-            for (uint32_t j = tid; j < cnt; j += kBucketThreads)
-                ord[atomicAdd(&scur[(uint32_t)(key[j] >> sub_shift) & 255u], 1u)] = (uint16_t)j;
-        }
         __syncthreads();
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
             // Slot and representative come with the key; their loads (and the
@@ -378,20 +355,13 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
             }
             const uint64_t k = key[j];
             uint32_t r = 0;
-            if (subs) {
-                const uint32_t sb = (uint32_t)(k >> sub_shift) & 255u;
-                const uint32_t end = sb < 255u ? sstart[sb + 1] : cnt;
-                r = sstart[sb];
-                for (uint32_t q = sstart[sb]; q < end; ++q) r += key[ord[q]] < k;
-            } else {
 #pragma unroll 8
-                for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
-            }
+            for (uint32_t x = 0; x < cnt; ++x) r += key[x] < k;
             const uint64_t uid = start + r;
             if (uid < a.out_capacity && s < a.table_cap) {
                 a.out_keys[uid] = k;
-                aux[2 * (uint64_t)s + 1] = (uint32_t)uid;
-                a.table_key[s] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
+                aux[4 * (uint64_t)s + 1] = (uint32_t)uid;
+                a.table_key[2 * (uint64_t)s] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
                 if (a.out_masks) {
                     a.out_masks[uid] = m;
                     uint4* d4 = reinterpret_cast<uint4*>(a.out_children + uid * 8);
@@ -427,7 +397,7 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
             s[k] = i < n ? a.item_slot[i] : 0xFFFFFFFFu;
         }
 #pragma unroll
-        for (int k = 0; k < kIlp; ++k) aux[k] = s[k] < a.table_cap ? a.table_aux[s[k]] : 0;
+        for (int k = 0; k < kIlp; ++k) aux[k] = s[k] < a.table_cap ? a.table_aux[2 * (uint64_t)s[k]] : 0;
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
             const uint64_t i = i0 + k * stride;
