@@ -356,9 +356,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
                     const uint32_t bs = atomicAdd(dd.bucket_count + b, 1u);
                     if (bs < kDedupTopBitCap) {
                         const uint64_t be = (uint64_t)b * kDedupTopBitCap + bs;
-                        dd.bucket_key[be] = hv;
-                        dd.bucket_slot[be] = (uint32_t)sl;
-                        dd.bucket_rep[be] = (uint32_t)p;
+                        dd.bucket[be] = make_uint4((uint32_t)hv, (uint32_t)(hv >> 32), (uint32_t)sl, (uint32_t)p);
                     } else {
                         full = true;
                     }

@@ -799,7 +799,7 @@ struct CreateLayout {
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
-    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bkey = 0, o_bslot = 0, o_brep = 0;
+    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bent = 0;
     // Persistent per-chunk leaves (batched form): zeroed chunk state
     // (histograms, cursors, done counters, item counter), tile offsets, the
     // mask stage and per-item brick counts / offsets.
@@ -848,9 +848,7 @@ struct CreateLayout {
             o_uitem = L.take<uint32_t>(uniq_cap);
             o_spl = L.take<uint64_t>(kDedupMaxSampledBuckets);
             o_bcnt = L.take<uint32_t>(kDedupMaxBuckets);
-            o_bkey = L.take<uint64_t>(bucket_area);
-            o_bslot = L.take<uint32_t>(bucket_area);
-            o_brep = L.take<uint32_t>(bucket_area);
+            o_bent = L.take<uint4>(bucket_area);
         }
         o_M0 = L.take<uint32_t>(p0cap);
         o_M1 = L.take<uint32_t>(p0cap);
@@ -1135,9 +1133,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.uniq_cap = Lo.uniq_cap;
             d.splitters = P64(Lo.o_spl);
             d.bucket_count = P32(Lo.o_bcnt);
-            d.bucket_key = P64(Lo.o_bkey);
-            d.bucket_slot = P32(Lo.o_bslot);
-            d.bucket_rep = P32(Lo.o_brep);
+            d.bucket = reinterpret_cast<uint4*>(b + Lo.o_bent);
             d.bucket_area = Lo.bucket_area;
             d.state = cs.dedup();
             d.out_keys = out_keys;

@@ -278,7 +278,8 @@ struct DedupArgs {
     uint32_t* item_slot;
     uint64_t* uniq_key; uint32_t* uniq_slot; uint32_t* uniq_item; uint64_t uniq_cap;
     uint64_t* splitters; uint32_t* bucket_count;     // kDedupMaxSampledBuckets, kDedupMaxBuckets
-    uint64_t* bucket_key; uint32_t* bucket_slot; uint32_t* bucket_rep; uint64_t bucket_area;
+    // Bucket entries, one 16-byte store each: key (two words), slot, representative.
+    uint4* bucket; uint64_t bucket_area;
     DedupState* state;
     uint64_t* out_keys; uint8_t* out_masks; uint32_t* out_children; uint64_t out_capacity;
     uint64_t* d_out_n;

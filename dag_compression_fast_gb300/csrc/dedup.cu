@@ -191,9 +191,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     aux[4 * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap && bslot[k] < kDedupTopBitCap) {
                         const uint64_t e = (uint64_t)b * kDedupTopBitCap + bslot[k];
-                        a.bucket_key[e] = h[k];
-                        a.bucket_slot[e] = (uint32_t)s[k];
-                        a.bucket_rep[e] = (uint32_t)i;
+                        a.bucket[e] = make_uint4((uint32_t)h[k], (uint32_t)(h[k] >> 32), (uint32_t)s[k], (uint32_t)i);
                     } else {
                         full = true;
                     }
@@ -271,9 +269,7 @@ __global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
         const uint32_t slot = atomicAdd(a.bucket_count + lo, 1u);
         if (slot < cap) {
             const uint64_t e = (uint64_t)lo * cap + slot;
-            a.bucket_key[e] = key;
-            a.bucket_slot[e] = a.uniq_slot[pos];
-            a.bucket_rep[e] = a.uniq_item[pos];
+            a.bucket[e] = make_uint4((uint32_t)key, (uint32_t)(key >> 32), a.uniq_slot[pos], a.uniq_item[pos]);
         } else {
             over = true;
         }
@@ -338,13 +334,17 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
         const uint32_t cnt = min(a.bucket_count[b], cap);
         const uint64_t src = (uint64_t)b * cap;
         __syncthreads();  // the previous bucket's keys are no longer read
-        for (uint32_t j = tid; j < cnt; j += kBucketThreads) key[j] = a.bucket_key[src + j];
+        for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
+            const uint4 e = a.bucket[src + j];
+            key[j] = (uint64_t)e.x | (uint64_t)e.y << 32;
+        }
         __syncthreads();
         for (uint32_t j = tid; j < cnt; j += kBucketThreads) {
             // Slot and representative come with the key; their loads (and the
             // payload's) are in flight while the rank is counted.
-            const uint32_t s = a.bucket_slot[src + j];
-            const uint32_t rep = a.bucket_rep[src + j];
+            const uint4 ent = a.bucket[src + j];
+            const uint32_t s = ent.z;
+            const uint32_t rep = ent.w;
             uint8_t m = 0;
             uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
             if (a.out_masks) {
