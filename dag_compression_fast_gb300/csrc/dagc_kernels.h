@@ -100,11 +100,12 @@ struct SortArgs {
 };
 
 // Digit-pass kernel shapes. Keys-only sorts: (items per thread, minimum
-// resident CTAs per SM, which caps registers, equal-digit matching); each is
+// resident CTAs per SM, which caps registers, equal-digit matching: ballots,
+// match.any, alternating, shared-memory atomicOr); each is
 // built for every digit width 8..kMaxRadixBits. Key/value sorts: 8-bit
 // digits. The autotuner and dagc options pick a shape and a width per sort.
-constexpr int kNumKeyShapes = 6;
-constexpr int kNumPairShapes = 8;
+constexpr int kNumKeyShapes = 8;
+constexpr int kNumPairShapes = 10;
 constexpr int kNumSortShapes = kNumPairShapes;
 int sort_shape_items(int shape, bool with_values);
 // Resident CTAs per SM of a shape at a digit width (occupancy query) for grid sizing.

@@ -25,6 +25,7 @@
 #include "dagc_launch.h"
 
 #include <algorithm>
+#include <cstddef>
 
 namespace dagc {
 namespace {
@@ -300,11 +301,12 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
 
 // Shared memory of one onesweep CTA: the staging tile, per-warp digit
 // counters (turned into per-warp output offsets) and per-digit offsets.
-template <int kBits, int kItems, bool kValues>
+template <int kBits, int kItems, bool kValues, int kMatch = 0>
 struct PassSmem {
     static constexpr int kRadix = 1 << kBits;
     static constexpr int kTile = kPassThreads * kItems;
     static constexpr int kWarpsPerCta = kPassThreads / 32;
+    static constexpr bool kOrMatch = kMatch == 3;
     uint64_t keys[kTile];
     uint32_t vals[kValues ? kTile : 4];
     uint32_t whist[kWarpsPerCta][kRadix];
@@ -312,17 +314,32 @@ struct PassSmem {
     uint32_t adj[kRadix];
     uint32_t scan[34];
     uint32_t tile_id;
+    // Matching by shared-memory atomicOr (kMatch 3): per warp, two sets of
+    // per-digit lane masks used by alternate rows (zero between uses). Last,
+    // so that the arrays above keep their 16-byte alignment (they are read
+    // and written as vectors).
+    uint32_t peer[kOrMatch ? kWarpsPerCta : 1][kOrMatch ? 2 : 1][kOrMatch ? kRadix : 1];
 };
 
+// The vector accesses of whist, gbase and adj need 16-byte alignment.
+template <int kBits, int kItems, bool kValues, int kMatch>
+constexpr bool pass_smem_aligned() {
+    using S = PassSmem<kBits, kItems, kValues, kMatch>;
+    return offsetof(S, whist) % 16 == 0 && offsetof(S, gbase) % 16 == 0 && offsetof(S, adj) % 16 == 0;
+}
+
 // Ranks one warp's kItems rows of 32 keys stably: per row, the lanes holding
-// the same digit are found (match.any on the ADU pipe, or one ballot per
-// digit bit on the ALU pipe, or both alternating), the highest of them adds
-// the group's size to the warp's counter for that digit and the count before
-// it is broadcast. dr[j] holds the digit in its high half and receives the
-// rank (< 2^16) in its low half. kFull: every lane of every row is valid.
+// the same digit are found (match.any on the ADU pipe, one ballot per digit
+// bit on the ALU pipe, both alternating, or each lane ORing its bit into its
+// digit's word in shared memory and reading the word back), the highest of
+// them adds the group's size to the warp's counter for that digit and the
+// count before it is broadcast. dr[j] holds the digit in its high half and
+// receives the rank (< 2^16) in its low half. kFull: every lane of every row
+// is valid. `peer` (kMatch 3): the warp's two sets of kRadix zero words.
 template <int kBits, int kItems, int kMatch, bool kFull>
 __device__ __forceinline__ void rank_warp(uint32_t (&dr)[kItems], uint32_t* wh, uint32_t wofs, uint32_t tile_n,
-                                          uint32_t lane) {
+                                          uint32_t lane, uint32_t* peer) {
+    constexpr uint32_t kRadixW = 1u << kBits;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
         const bool valid = kFull || wofs + j * 32 + lane < tile_n;
@@ -330,7 +347,18 @@ __device__ __forceinline__ void rank_warp(uint32_t (&dr)[kItems], uint32_t* wh, 
         // Every warp collective below is executed by all 32 lanes (valid or
         // not); only the results are masked, never the calls.
         uint32_t peers;
-        if (kMatch == 1 || (kMatch == 2 && (j & 1))) {
+        if (kMatch == 3) {
+            // Row j uses word set j & 1; the row before cleared it (its
+            // leaders, after the row's second __syncwarp), and the
+            // __syncwarp calls of row j - 1 order that clear before this OR.
+            uint32_t* pw = peer + (j & 1) * kRadixW;
+            const uint32_t vmask = kFull ? 0xFFFFFFFFu : __ballot_sync(0xFFFFFFFFu, valid);
+            if (valid) atomicOr(&pw[d], 1u << lane);
+            __syncwarp();
+            peers = valid ? pw[d] : ~vmask;  // invalid lanes: a group of their own, unused
+            __syncwarp();
+            if (valid && lane == 31 - __clz(peers)) pw[d] = 0;
+        } else if (kMatch == 1 || (kMatch == 2 && (j & 1))) {
             peers = __match_any_sync(0xFFFFFFFFu, valid ? d : 0xFFFFFFFFu);
         } else {
             // Bits above the pass's width are zero in every lane's digit, so
@@ -374,7 +402,8 @@ __device__ __forceinline__ void rank_warp(uint32_t (&dr)[kItems], uint32_t* wh, 
 template <int kBits, int kItems, bool kValues, int kMinCtas, int kMatch>
 __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassParams p) {
     pdl_prologue();
-    using Smem = PassSmem<kBits, kItems, kValues>;
+    using Smem = PassSmem<kBits, kItems, kValues, kMatch>;
+    static_assert(pass_smem_aligned<kBits, kItems, kValues, kMatch>(), "vector-accessed arrays misaligned");
     constexpr int kTile = Smem::kTile;
     constexpr int kW = Smem::kWarpsPerCta;
     constexpr int kRadix = Smem::kRadix;
@@ -416,6 +445,8 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
         }
     }
     uint32_t* wh = S.whist[warp];
+    if constexpr (Smem::kOrMatch)
+        for (int i = tid; i < kW * 2 * kRadix; i += kPassThreads) (&S.peer[0][0][0])[i] = 0;
     while (true) {
         if (tid == 0) S.tile_id = atomicAdd(p.tile_counter, 1u);
         for (int i = tid; i < kW * kRadix; i += kPassThreads) (&S.whist[0][0])[i] = 0;
@@ -451,8 +482,9 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
             for (int j = 0; j < kItems; ++j) dr[j] = ((uint32_t)(k[j] >> p.shift) & dmask) << 16;
         }
         // 2. Ranks within the warp.
-        if (tile_n == (uint32_t)kTile) rank_warp<kBits, kItems, kMatch, true>(dr, wh, wofs, tile_n, lane);
-        else rank_warp<kBits, kItems, kMatch, false>(dr, wh, wofs, tile_n, lane);
+        uint32_t* peer = Smem::kOrMatch ? &S.peer[Smem::kOrMatch ? warp : 0][0][0] : nullptr;
+        if (tile_n == (uint32_t)kTile) rank_warp<kBits, kItems, kMatch, true>(dr, wh, wofs, tile_n, lane, peer);
+        else rank_warp<kBits, kItems, kMatch, false>(dr, wh, wofs, tile_n, lane, peer);
         __syncthreads();
 
         // 3. This thread's digits: count over the warps, publish the tile
@@ -589,10 +621,12 @@ void launch_fill_tune_keys(uint64_t* out, uint64_t n, int lo_bit, int hi_bit, ui
 
 // Keys-only shapes: (items per thread, minimum CTAs per SM, match mode); each
 // is built for digits of 8, 9, 10 and 11 bits.
-#define DAGC_KEY_SHAPES(X) X(0, 16, 3, 2) X(1, 16, 2, 2) X(2, 16, 4, 2) X(3, 12, 4, 2) X(4, 16, 3, 0) X(5, 16, 3, 1)
+#define DAGC_KEY_SHAPES(X) \
+    X(0, 16, 3, 2) X(1, 16, 2, 2) X(2, 16, 4, 2) X(3, 12, 4, 2) X(4, 16, 3, 0) X(5, 16, 3, 1) X(6, 16, 4, 3) X(7, 12, 4, 3)
 // Key/value shapes (8-bit digits).
 #define DAGC_PAIR_SHAPES(X) \
-    X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2)
+    X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2) \
+    X(8, 8, 4, 3) X(9, 16, 3, 3)
 
 namespace {
 struct PassKernel {
@@ -608,12 +642,12 @@ struct PairShape {
     PassKernel kernel;
 };
 #define DAGC_KEY_KERNEL(items, ctas, match, bits) \
-    {onesweep_pass<bits, items, false, ctas, match>, sizeof(PassSmem<bits, items, false>)}
+    {onesweep_pass<bits, items, false, ctas, match>, sizeof(PassSmem<bits, items, false, match>)}
 #define DAGC_KEY_SHAPE_ENTRY(id, items, ctas, match)                                                      \
     {items, ctas, {DAGC_KEY_KERNEL(items, ctas, match, 8), DAGC_KEY_KERNEL(items, ctas, match, 9),      \
                    DAGC_KEY_KERNEL(items, ctas, match, 10), DAGC_KEY_KERNEL(items, ctas, match, 11)}},
 #define DAGC_PAIR_SHAPE_ENTRY(id, items, ctas, match) \
-    {items, ctas, {onesweep_pass<8, items, true, ctas, match>, sizeof(PassSmem<8, items, true>)}},
+    {items, ctas, {onesweep_pass<8, items, true, ctas, match>, sizeof(PassSmem<8, items, true, match>)}},
 const KeyShape kKeyShapes[kNumKeyShapes] = {DAGC_KEY_SHAPES(DAGC_KEY_SHAPE_ENTRY)};
 const PairShape kPairShapes[kNumPairShapes] = {DAGC_PAIR_SHAPES(DAGC_PAIR_SHAPE_ENTRY)};
 #undef DAGC_KEY_KERNEL
@@ -641,18 +675,28 @@ int sort_shape_items(int shape, bool with_values) {
     return with_values ? kPairShapes[clamp_shape(shape, true)].items : kKeyShapes[clamp_shape(shape, false)].items;
 }
 
+// Shared memory a CTA may opt in to on sm_103a; kernels needing more (wide
+// digits with per-warp match words) are never planned.
+constexpr size_t kMaxPassSmem = 227 * 1024;
+
 void sort_configure() {
     for (const KeyShape& e : kKeyShapes)
         for (const PassKernel& k : e.by_bits)
-            cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+            if (k.smem <= kMaxPassSmem) cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
     for (const PairShape& e : kPairShapes)
-        cudaFuncSetAttribute(e.kernel.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.kernel.smem);
+        if (e.kernel.smem <= kMaxPassSmem)
+            cudaFuncSetAttribute(e.kernel.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.kernel.smem);
+    cudaGetLastError();  // an attribute the device refuses leaves no error behind for later checks
 }
 
 int occupancy_sort_shape(int shape, bool with_values, int radix_bits) {
     const PassKernel& k = pass_kernel(shape, with_values, with_values ? kRadixBits : radix_bits);
+    if (k.smem > kMaxPassSmem) return 0;
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, kPassThreads, k.smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, kPassThreads, k.smem) != cudaSuccess) {
+        cudaGetLastError();
+        occ = 0;
+    }
     return occ;
 }
 
@@ -661,6 +705,7 @@ bool sort_plan_valid(int shape, bool with_values, int radix_bits, int lo_bit, in
     if (radix_bits < kRadixBits || radix_bits > kMaxRadixBits) return false;
     const int passes = sort_passes_r(lo_bit, hi_bit, radix_bits);
     if (passes > kMaxPasses) return false;
+    if (pass_kernel(shape, with_values, radix_bits).smem > kMaxPassSmem) return false;
     if (passes && passes * pass_hist_stride(lo_bit, hi_bit, passes) > kSortHistWords) return false;
     // Look-back status room (sort_status_words): at most one digit word per
     // two keys of a tile.
