@@ -55,7 +55,7 @@ TERRAIN = {"name": "terrain_fbm_2048^3_depth11", "depth": 11, "seed": 0xDA6C0DE 
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="dagc", choices=["dagc", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")

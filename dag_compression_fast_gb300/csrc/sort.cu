@@ -301,24 +301,33 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
 
 // Shared memory of one onesweep CTA: the staging tile, per-warp digit
 // counters (turned into per-warp output offsets) and per-digit offsets.
+// Matching by shared-memory atomicOr (kMatch 3) adds, per warp, two sets of
+// per-digit lane masks used by alternate rows (zero between uses). They are
+// live only while the tile is ranked and the staging tile only after that,
+// so the masks share the staging tile's bytes where they fit (cleared at the
+// start of every tile) and follow the other arrays otherwise (cleared once).
 template <int kBits, int kItems, bool kValues, int kMatch = 0>
 struct PassSmem {
     static constexpr int kRadix = 1 << kBits;
     static constexpr int kTile = kPassThreads * kItems;
     static constexpr int kWarpsPerCta = kPassThreads / 32;
     static constexpr bool kOrMatch = kMatch == 3;
-    uint64_t keys[kTile];
+    static constexpr int kPeerWords = kWarpsPerCta * 2 * kRadix;
+    static constexpr bool kPeerInTile = kOrMatch && kPeerWords * 4 <= kTile * 8;
+    union {
+        uint64_t keys[kTile];
+        uint32_t peer_tile[kPeerInTile ? kPeerWords : 4];
+    };
     uint32_t vals[kValues ? kTile : 4];
     uint32_t whist[kWarpsPerCta][kRadix];
     uint32_t gbase[kRadix];
     uint32_t adj[kRadix];
     uint32_t scan[34];
     uint32_t tile_id;
-    // Matching by shared-memory atomicOr (kMatch 3): per warp, two sets of
-    // per-digit lane masks used by alternate rows (zero between uses). Last,
-    // so that the arrays above keep their 16-byte alignment (they are read
-    // and written as vectors).
-    uint32_t peer[kOrMatch ? kWarpsPerCta : 1][kOrMatch ? 2 : 1][kOrMatch ? kRadix : 1];
+    // Last, so that the arrays above keep their 16-byte alignment (they are
+    // read and written as vectors).
+    uint32_t peer_own[kOrMatch && !kPeerInTile ? kPeerWords : 1];
+    __device__ uint32_t* peer() { return kPeerInTile ? peer_tile : peer_own; }
 };
 
 // The vector accesses of whist, gbase and adj need 16-byte alignment.
@@ -396,7 +405,9 @@ __device__ __forceinline__ void rank_warp(uint32_t (&dr)[kItems], uint32_t* wh, 
 //   4. keys are fetched again (the tile was just read: cache hits) and staged
 //      in digit order in shared memory; values, if any, are fetched here;
 //   5. each thread looks back over earlier tiles for its digits' global
-//      offsets and publishes the inclusive prefixes;
+//      offsets and publishes the inclusive prefixes (after the staging: the
+//      earlier tiles have published their counts by then, so the walk
+//      rarely waits);
 //   6. the staged tile is written out so that equal digits form contiguous
 //      runs.
 template <int kBits, int kItems, bool kValues, int kMinCtas, int kMatch>
@@ -445,11 +456,16 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
         }
     }
     uint32_t* wh = S.whist[warp];
-    if constexpr (Smem::kOrMatch)
-        for (int i = tid; i < kW * 2 * kRadix; i += kPassThreads) (&S.peer[0][0][0])[i] = 0;
+    if constexpr (Smem::kOrMatch && !Smem::kPeerInTile)
+        for (int i = tid; i < Smem::kPeerWords; i += kPassThreads) S.peer_own[i] = 0;
     while (true) {
         if (tid == 0) S.tile_id = atomicAdd(p.tile_counter, 1u);
-        for (int i = tid; i < kW * kRadix; i += kPassThreads) (&S.whist[0][0])[i] = 0;
+        {
+            const uint4 z = make_uint4(0, 0, 0, 0);
+            for (int i = tid; i < kW * kRadix / 4; i += kPassThreads) reinterpret_cast<uint4*>(&S.whist[0][0])[i] = z;
+            if constexpr (Smem::kPeerInTile)
+                for (int i = tid; i < Smem::kPeerWords / 4; i += kPassThreads) reinterpret_cast<uint4*>(S.peer_tile)[i] = z;
+        }
         __syncthreads();
         const uint32_t tile = S.tile_id;
         if (tile >= ntiles) break;
@@ -482,7 +498,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
             for (int j = 0; j < kItems; ++j) dr[j] = ((uint32_t)(k[j] >> p.shift) & dmask) << 16;
         }
         // 2. Ranks within the warp.
-        uint32_t* peer = Smem::kOrMatch ? &S.peer[Smem::kOrMatch ? warp : 0][0][0] : nullptr;
+        uint32_t* peer = Smem::kOrMatch ? S.peer() + warp * 2 * kRadix : nullptr;
         if (tile_n == (uint32_t)kTile) rank_warp<kBits, kItems, kMatch, true>(dr, wh, wofs, tile_n, lane, peer);
         else rank_warp<kBits, kItems, kMatch, false>(dr, wh, wofs, tile_n, lane, peer);
         __syncthreads();
