@@ -799,7 +799,8 @@ struct CreateLayout {
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
-    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_uitem = 0, o_spl = 0, o_bcnt = 0, o_bent = 0;
+    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_ukey_alt = 0, o_uslot_sorted = 0, o_uslot_alt = 0;
+    size_t o_bcnt = 0, o_bent = 0;
     // Persistent per-chunk leaves (batched form): zeroed chunk state
     // (histograms, cursors, done counters, item counter), tile offsets, the
     // mask stage and per-item brick counts / offsets.
@@ -845,8 +846,12 @@ struct CreateLayout {
             o_islot = L.take<uint32_t>(item_cap);
             o_ukey = L.take<uint64_t>(uniq_cap);
             o_uslot = L.take<uint32_t>(uniq_cap);
-            o_uitem = L.take<uint32_t>(uniq_cap);
-            o_spl = L.take<uint64_t>(kDedupMaxSampledBuckets);
+            // The (key, slot) sort of the unique leaf masks: its other key
+            // buffer, its slots out and their other buffer (the keys go out
+            // to the leaf array).
+            o_ukey_alt = L.take<uint64_t>(uniq_cap);
+            o_uslot_sorted = L.take<uint32_t>(uniq_cap);
+            o_uslot_alt = L.take<uint32_t>(uniq_cap);
             o_bcnt = L.take<uint32_t>(kDedupMaxBuckets);
             o_bent = L.take<uint4>(bucket_area);
         }
@@ -1121,7 +1126,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.d_n = d_n;
             d.masks = masks;
             d.children = children;
-            d.sampled = masks == nullptr;  // leaf masks are not uniformly distributed; node hashes are
+            d.to_list = masks == nullptr;  // leaf masks are not uniformly distributed; node hashes are
             d.item_cap = Lo.item_cap;
             d.table_key = static_cast<uint64_t*>(ctx->table);
             d.table_aux = static_cast<uint64_t*>(ctx->table) + 1;
@@ -1129,9 +1134,7 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.item_slot = P32(Lo.o_islot);
             d.uniq_key = P64(Lo.o_ukey);
             d.uniq_slot = P32(Lo.o_uslot);
-            d.uniq_item = P32(Lo.o_uitem);
             d.uniq_cap = Lo.uniq_cap;
-            d.splitters = P64(Lo.o_spl);
             d.bucket_count = P32(Lo.o_bcnt);
             d.bucket = reinterpret_cast<uint4*>(b + Lo.o_bent);
             d.bucket_area = Lo.bucket_area;
@@ -1146,9 +1149,21 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             return d;
         };
         if (use_dedup) {
-            ctx->launches += launch_dedup(dedup_args(P64(Lo.o_LM), cs.count(kCntBricks), nullptr, nullptr, P64(Lo.o_PL),
-                                                     nullptr, nullptr, p0cap, cs.count(kCntLeaves), P32(Lo.o_M0)),
-                                          s);
+            // Distinct masks into the table and the unique list; the list
+            // sorted as (mask, slot) pairs straight into the leaf array; each
+            // slot gets its mask's rank as unique id; every brick its id.
+            const DedupArgs d = dedup_args(P64(Lo.o_LM), cs.count(kCntBricks), nullptr, nullptr, P64(Lo.o_PL), nullptr,
+                                           nullptr, p0cap, cs.count(kCntLeaves), P32(Lo.o_M0));
+            launch_dedup_insert(d, s);
+            ++ctx->launches;
+            DAGC_LAUNCHED(ctx);
+            st = run_sort(ctx, cs, sb, P64(Lo.o_ukey), P64(Lo.o_PL), P64(Lo.o_ukey_alt), P32(Lo.o_uslot),
+                          P32(Lo.o_uslot_sorted), P32(Lo.o_uslot_alt), true, Lo.uniq_cap,
+                          reinterpret_cast<const uint64_t*>(&d.state->u), 0, 64, 0, s);
+            if (st) return st;
+            launch_dedup_assign(d, P32(Lo.o_uslot_sorted), s);
+            launch_dedup_map(d, s);
+            ctx->launches += 2;
             DAGC_LAUNCHED(ctx);
         } else {
         st = run_sort(ctx, cs, sb, P64(Lo.o_LM), P64(Lo.o_SK), P64(Lo.o_SKa), nullptr, P32(Lo.o_V), P32(Lo.o_Va), true, p0cap,

@@ -248,28 +248,31 @@ void launch_unique(const UniqueArgs& a, cudaStream_t s);
 // ExtractLevel + ComputeHashes: from the sorted unique codes of the child
 // level and their child ids, build one parent node per distinct code >> 3.
 
-// Level dedup by hash set + bucket sort (dedup.cu): same outputs as sort
-// pairs + unique_runs on (key, item) for one level.
-constexpr uint32_t kDedupPerBucket = 256;            // expected distinct keys per bucket
-constexpr uint32_t kDedupTopBitCap = 1024;           // bucket room, top-bit form (128-256 expected)
-constexpr uint32_t kDedupSampledCap = 2048;          // least bucket room, sampled form (8x expected)
-constexpr uint32_t kDedupSampledCapMax = 8192;       // most (4M distinct keys over 4096 buckets)
-constexpr uint32_t kDedupMaxBuckets = 16384;         // top-bit form
-constexpr uint32_t kDedupMaxSampledBuckets = 4096;   // sampled form
-constexpr uint32_t kDedupSamplesPerBucket = 4;
-constexpr uint32_t kDedupMaxSample = kDedupSamplesPerBucket * kDedupMaxSampledBuckets;
+// Level dedup by hash set + ordering of the distinct keys (dedup.cu): same
+// outputs as sort pairs + unique_runs on (key, item) for one level.
+constexpr uint32_t kDedupPerBucket = 256;            // expected distinct keys per bucket (node hashes)
+constexpr uint32_t kDedupTopBitCap = 1024;           // bucket room (128-256 expected)
+constexpr uint32_t kDedupMaxBuckets = 16384;
 constexpr uint64_t kDedupMaxItems = 1ull << 24;
 constexpr uint64_t kDedupMaxUnique = (uint64_t)kDedupMaxBuckets * kDedupPerBucket;
-DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) { return 8 * uniq_cap + 8 * kDedupSampledCapMax; }
+// Bucket entries for up to uniq_cap distinct keys: the buckets for n items
+// (a power of two, n / 256 <= buckets < 2n / 256) hold fewer than 8n entries.
+DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) {
+    const uint64_t a = 8 * uniq_cap > kDedupTopBitCap ? 8 * uniq_cap : kDedupTopBitCap;
+    const uint64_t most = (uint64_t)kDedupMaxBuckets * kDedupTopBitCap;
+    return a < most ? a : most;
+}
 struct DedupState {
     unsigned long long u;  // distinct keys found (zero before the level)
-    uint32_t nbuckets, bucket_cap;
+    uint32_t nbuckets, pad0;
     uint32_t inserted, pad;  // 1: extract_level already inserted the level's hashes
 };
 struct DedupArgs {
     const uint64_t* keys; const uint64_t* d_n;       // items: key per item
     const uint8_t* masks; const uint32_t* children;  // item payloads (null for leaves)
-    bool sampled;                                    // leaf masks: splitters from a sample; else top bits
+    // Leaf masks (far from uniform): winners go to the unique list, which the
+    // caller sorts. Node hashes: winners go to the bucket of their top bits.
+    bool to_list;
     uint64_t item_cap;
     // Table of table_cap slots (a power of two), 16 bytes each so that a
     // slot's key and aux share a sector: table_key[2s] = key, 0 = empty (all
@@ -277,8 +280,8 @@ struct DedupArgs {
     // << 32 (table_aux = table_key + 1).
     uint64_t* table_key; uint64_t* table_aux; uint64_t table_cap;
     uint32_t* item_slot;
-    uint64_t* uniq_key; uint32_t* uniq_slot; uint32_t* uniq_item; uint64_t uniq_cap;
-    uint64_t* splitters; uint32_t* bucket_count;     // kDedupMaxSampledBuckets, kDedupMaxBuckets
+    uint64_t* uniq_key; uint32_t* uniq_slot; uint64_t uniq_cap;  // the unique list (leaf masks)
+    uint32_t* bucket_count;                                       // kDedupMaxBuckets
     // Bucket entries, one 16-byte store each: key (two words), slot, representative.
     uint4* bucket; uint64_t bucket_area;
     DedupState* state;
@@ -288,7 +291,14 @@ struct DedupArgs {
     uint32_t* err;
 };
 void dedup_configure(int sms);
-int launch_dedup(const DedupArgs& a, cudaStream_t s);  // returns the number of launches (3 or 5)
+// Node levels: insert (unless extract_level did), bucket sort, map; returns
+// the number of launches.
+int launch_dedup(const DedupArgs& a, cudaStream_t s);
+// Leaf masks: insert into the table and the unique list; after the caller's
+// (key, slot) sort of the list, assign the unique ids; then map.
+void launch_dedup_insert(const DedupArgs& a, cudaStream_t s);
+void launch_dedup_assign(const DedupArgs& a, const uint32_t* sorted_slot, cudaStream_t s);
+void launch_dedup_map(const DedupArgs& a, cudaStream_t s);
 
 constexpr uint64_t kFuseInsertMax = 1ull << 20;
 struct ExtractArgs {

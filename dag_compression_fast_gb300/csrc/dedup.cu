@@ -1,36 +1,32 @@
-// Level deduplication by hash set + bucket sort, for sm_103a. Replaces, for
-// one level (or the leaves), the reference's SortLevel
+// Level deduplication by hash set + ordering of the distinct keys, for
+// sm_103a. Replaces, for one level (or the leaves), the reference's SortLevel
 // (src/DAGCompression.cu:864-914): sort (hash, index) pairs, flag runs, scan,
 // scatter to unique ids. Same result: the distinct keys in ascending order,
 // their payloads, and a map item -> unique id. Instead of eight 8-bit radix
 // passes over every item, the distinct keys are found first and only those
-// are sorted:
+// are ordered:
 //
 //   dedup_insert   every item inserts its key into an open-addressing table
 //                  (linear probing, atomicCAS on the key); the first inserter
 //                  of a key records itself as the slot's representative and
-//                  appends (key, slot, itself) to the unique list (leaf
-//                  masks) or straight to its bucket (node hashes: the bucket
-//                  count follows from the item count, so no other pass is
-//                  needed; dedup_map of the previous level zeroed the bucket
-//                  counters);
-//   dedup_split    (leaf masks only) one CTA sorts a strided sample of 4 keys
-//                  per bucket and picks the bucket splitters: the keys are
-//                  distinct, so bucket sizes depend only on ranks, whatever
-//                  the key distribution. Node hashes are MurmurHash outputs:
-//                  their top bits are the bucket, no sample needed;
-//   dedup_scatter  (leaf masks only) unique keys, with their slot and
-//                  representative, go to fixed-capacity buckets (4x to 8x the
-//                  expected keys; sampled buckets grow past 256 expected keys
-//                  once there are 4096 of them);
-//   dedup_sort     each bucket is ranked in shared memory (rank = number of
-//                  smaller keys) and written at its global ranks, with the
-//                  representative's payload; the unique id goes to the slot;
+//                  appends (key, slot) to the unique list (leaf masks) or
+//                  (key, slot, itself) straight to its bucket (node hashes:
+//                  MurmurHash outputs, so their top bits are the bucket and
+//                  the bucket count follows from the item count; dedup_map of
+//                  the previous level zeroed the bucket counters);
+//   leaf masks     (far from uniform) the unique list is ordered by a 64-bit
+//                  radix sort of (key, slot) pairs (the caller's sort), then
+//   dedup_assign   gives each sorted key's slot its unique id (its rank) and
+//                  clears the slot's key;
+//   dedup_sort     (node hashes) each bucket is ranked in shared memory (rank
+//                  = number of smaller keys) and written at its global ranks,
+//                  with the representative's payload; the unique id goes to
+//                  the slot and the slot's key is cleared;
 //   dedup_map      every item reads its unique id and representative through
 //                  its slot, duplicates are compared in full with their
-//                  representative (collision check). dedup_sort cleared the
-//                  slots' keys, once per distinct key (items sharing a slot
-//                  only read its aux word).
+//                  representative (collision check). The slots' keys were
+//                  cleared once per distinct key (items sharing a slot only
+//                  read its aux word).
 //
 // What the fixed sizes cannot hold (table, unique list, a bucket) sets
 // kErrFallback, and the caller reruns the call with the radix-sort form.
@@ -52,25 +48,22 @@ constexpr int kIlp = 4;
 
 __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     pdl_prologue();
-    if (!a.sampled && a.state->inserted) return;  // extract_level inserted this level's hashes
+    if (!a.to_list && a.state->inserted) return;  // extract_level inserted this level's hashes
     const uint64_t n = *a.d_n;
     const uint64_t S = table_size_for(n);
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
-    // Leaf masks: the bucket counters are zeroed here (dedup_scatter fills
-    // them after this kernel). Node hashes are uniform, so their top bits
-    // give the bucket at once: winners append straight to their bucket, and
-    // the previous level's dedup_map left the counters zero.
-    if (a.sampled)
-        for (uint64_t b = gtid; b < kDedupMaxBuckets; b += gsize) a.bucket_count[b] = 0;
+    // Node hashes are uniform, so their top bits give the bucket at once:
+    // winners append straight to their bucket (the previous level's
+    // dedup_map left the counters zero). Leaf masks go to the unique list.
     if (S > a.table_cap || n > a.item_cap) {
         if (gtid == 0) atomicOr(a.err, kErrFallback);
         return;
     }
     int shift = 64;
-    const uint32_t nb = a.sampled ? 0u : topbit_buckets(n, &shift);
-    if (!a.sampled) {
+    const uint32_t nb = a.to_list ? 0u : topbit_buckets(n, &shift);
+    if (!a.to_list) {
         if ((uint64_t)nb * kDedupTopBitCap > a.bucket_area) {
             if (gtid == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
             return;
@@ -106,7 +99,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         // trip instead of two). Each round issues every pending item's read,
         // then every claim, back to back (no result is used before the last
         // one is issued).
-        const bool read_first = a.sampled || n > kDedupClaimFirstMax;
+        const bool read_first = a.to_list || n > kDedupClaimFirstMax;
         for (uint64_t probe = 0; probe < S; ++probe) {
             bool pend[kIlp], claim[kIlp];
             uint64_t cur[kIlp];
@@ -157,7 +150,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
         if (lane == 0 && wtotal)
             pos0 = atomicAdd((unsigned long long*)&a.state->u, (unsigned long long)wtotal);
         pos0 = __shfl_sync(0xFFFFFFFFu, pos0, 0);
-        if (a.sampled) {
+        if (a.to_list) {
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
                 if (won[k]) {
@@ -167,7 +160,6 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     if (pos < a.uniq_cap) {
                         a.uniq_key[pos] = h[k];
                         a.uniq_slot[pos] = (uint32_t)s[k];
-                        a.uniq_item[pos] = (uint32_t)i;
                     } else {
                         full = true;
                     }
@@ -204,77 +196,24 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     if (full) atomicOr(a.err, kErrFallback);
 }
 
-// Leaf masks: bucket count and splitters from a sorted sample (one CTA).
-constexpr int kSplitThreads = 1024;
-
-__global__ void __launch_bounds__(kSplitThreads) dedup_split(DedupArgs a) {
+// Leaf masks, after the (key, slot) sort of the unique list: the key of rank
+// r is the r-th distinct key; its slot gets unique id r and an empty key.
+__global__ void __launch_bounds__(256) dedup_assign(DedupArgs a, const uint32_t* sorted_slot) {
     pdl_prologue();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* sample = reinterpret_cast<uint64_t*>(smem_raw);  // kDedupMaxSample
-    const uint32_t tid = threadIdx.x;
     const uint64_t u = unique_count(a);
-    const uint64_t nb64 = (u + kDedupPerBucket - 1) / kDedupPerBucket;
-    const uint32_t nb = nb64 < 1 ? 1u : (uint32_t)(nb64 < kDedupMaxSampledBuckets ? nb64 : kDedupMaxSampledBuckets);
-    const uint64_t per = (u + nb - 1) / nb;  // expected keys per bucket
-    const uint64_t cap = per * 8 > kDedupSampledCap ? per * 8 : kDedupSampledCap;
-    if (cap > kDedupSampledCapMax || (uint64_t)nb * cap > a.bucket_area) {
-        if (tid == 0) { atomicOr(a.err, kErrFallback); a.state->nbuckets = 0; }
-        return;
-    }
-    if (tid == 0) { a.state->nbuckets = nb; a.state->bucket_cap = (uint32_t)cap; }
-    if (nb == 1) return;
-    const uint32_t ns = (uint32_t)(kDedupSamplesPerBucket * nb < u ? kDedupSamplesPerBucket * nb : u);
-    uint32_t p2 = 1;
-    while (p2 < ns) p2 <<= 1;
-    for (uint32_t j = tid; j < p2; j += kSplitThreads)
-        sample[j] = j < ns ? a.uniq_key[(uint64_t)j * u / ns] : ~0ull;
-    __syncthreads();
-    for (uint32_t k = 2; k <= p2; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = tid; i < p2; i += kSplitThreads) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const uint64_t x = sample[i], y = sample[ixj];
-                    if ((x > y) == ((i & k) == 0)) { sample[i] = y; sample[ixj] = x; }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    // Bucket b holds keys in [splitter b-1, splitter b); splitter b is the
-    // sample of rank (b + 1) * ns / nb.
-    for (uint32_t b = tid; b + 1 < nb; b += kSplitThreads) a.splitters[b] = sample[(uint64_t)(b + 1) * ns / nb];
-}
-
-__global__ void __launch_bounds__(256) dedup_scatter(DedupArgs a) {
-    pdl_prologue();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* spl = reinterpret_cast<uint64_t*>(smem_raw);  // kDedupMaxSampledBuckets splitters
-    const uint64_t u = unique_count(a);
-    const uint32_t cap = a.state->bucket_cap;
-    const uint32_t nb = a.state->nbuckets;
-    if (nb == 0) return;
-    for (uint32_t b = threadIdx.x; b + 1 < nb; b += blockDim.x) spl[b] = a.splitters[b];
-    __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = u;
-    bool over = false;
-    for (uint64_t pos = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < u;
-         pos += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t key = a.uniq_key[pos];
-        uint32_t lo = 0, hi = nb - 1;  // number of splitters <= key
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (spl[mid] <= key) lo = mid + 1; else hi = mid;
-        }
-        const uint32_t slot = atomicAdd(a.bucket_count + lo, 1u);
-        if (slot < cap) {
-            const uint64_t e = (uint64_t)lo * cap + slot;
-            a.bucket[e] = make_uint4((uint32_t)key, (uint32_t)(key >> 32), a.uniq_slot[pos], a.uniq_item[pos]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = u < a.out_capacity ? u : a.out_capacity;
+    uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
+    bool bad = false;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < u; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t sl = sorted_slot[r];
+        if (sl < a.table_cap && r < a.out_capacity) {
+            aux[4 * (uint64_t)sl + 1] = (uint32_t)r;
+            a.table_key[2 * (uint64_t)sl] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
         } else {
-            over = true;
+            bad = true;
         }
     }
-    if (over) atomicOr(a.err, kErrFallback);
+    if (bad) atomicOr(a.err, kErrCapacity);
 }
 
 // Each CTA takes a contiguous range of buckets; a bucket's keys are distinct,
@@ -284,13 +223,13 @@ constexpr int kBucketThreads = 256;
 __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* key = reinterpret_cast<uint64_t*>(smem_raw);  // bucket room: kDedupSampledCapMax or kDedupTopBitCap
+    uint64_t* key = reinterpret_cast<uint64_t*>(smem_raw);  // bucket room: kDedupTopBitCap
     __shared__ uint32_t red[kBucketThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t nb = a.state->nbuckets;
-    if (!a.sampled && blockIdx.x == 0) {
-        // Top-bit form: the distinct keys are the bucket entries (the insert
-        // appended every first inserter to its bucket).
+    if (blockIdx.x == 0) {
+        // The distinct keys are the bucket entries (the insert appended every
+        // first inserter to its bucket).
         __shared__ uint32_t tot[kBucketThreads / 32];
         uint32_t part = 0;
         for (uint32_t b = tid; b < nb; b += kBucketThreads) part += min(a.bucket_count[b], kDedupTopBitCap);
@@ -306,7 +245,7 @@ __global__ void __launch_bounds__(kBucketThreads) dedup_sort(DedupArgs a) {
         }
     }
     if (nb == 0) return;
-    const uint32_t cap = a.sampled ? a.state->bucket_cap : kDedupTopBitCap;
+    constexpr uint32_t cap = kDedupTopBitCap;
     const uint32_t b0 = (uint32_t)((uint64_t)nb * blockIdx.x / gridDim.x);
     const uint32_t b1 = (uint32_t)((uint64_t)nb * (blockIdx.x + 1) / gridDim.x);
     if (b0 >= b1) return;
@@ -427,32 +366,39 @@ int g_sms = 152;
 }  // namespace
 
 void dedup_configure(int sms) {
-    cudaFuncSetAttribute(dedup_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupMaxSample * 8));
-    cudaFuncSetAttribute(dedup_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(kDedupMaxSampledBuckets * 8));
-    cudaFuncSetAttribute(dedup_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupSampledCapMax * 8));
+    cudaFuncSetAttribute(dedup_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kDedupTopBitCap * 8));
     g_sms = sms > 0 ? sms : 152;
 }
 
-int launch_dedup(const DedupArgs& a, cudaStream_t s) {
+namespace {
+int item_grid(const DedupArgs& a) {
     const uint64_t want = (a.item_cap + 255) / 256;
     const int g = 8 * g_sms;  // full occupancy: 8 CTAs of 256 threads per SM
-    const int gi = (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
-    launch_pdl(dedup_insert, dim3(gi), dim3(256), 0, s, a);  // returns at once when extract_level inserted
-    int launches = 1;
-    if (a.sampled) {
-        launch_pdl(dedup_split, dim3(1), dim3(kSplitThreads), kDedupMaxSample * 8, s, a);
-        ++launches;
-    }
-    if (a.sampled) {  // node levels appended to their buckets in dedup_insert
-        launch_pdl(dedup_scatter, dim3(gi), dim3(256), kDedupMaxSampledBuckets * 8, s, a);
-        ++launches;
-    }
+    return (int)(want < (uint64_t)g ? (want > 0 ? want : 1) : g);
+}
+}  // namespace
+
+void launch_dedup_insert(const DedupArgs& a, cudaStream_t s) {
+    launch_pdl(dedup_insert, dim3(item_grid(a)), dim3(256), 0, s, a);
+}
+
+void launch_dedup_assign(const DedupArgs& a, const uint32_t* sorted_slot, cudaStream_t s) {
+    const uint64_t want = (a.uniq_cap + 255) / 256;
+    const int g = (int)(want < (uint64_t)(8 * g_sms) ? (want > 0 ? want : 1) : 8 * g_sms);
+    launch_pdl(dedup_assign, dim3(g), dim3(256), 0, s, a, sorted_slot);
+}
+
+void launch_dedup_map(const DedupArgs& a, cudaStream_t s) {
+    launch_pdl(dedup_map, dim3(item_grid(a)), dim3(256), 0, s, a);
+}
+
+int launch_dedup(const DedupArgs& a, cudaStream_t s) {
+    launch_dedup_insert(a, s);  // returns at once when extract_level inserted
     const uint64_t nbmax = (a.uniq_cap + kDedupPerBucket - 1) / kDedupPerBucket;
     const int gs = (int)(nbmax < (uint64_t)(8 * g_sms) ? (nbmax > 0 ? nbmax : 1) : 8 * g_sms);
-    launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), (a.sampled ? kDedupSampledCapMax : kDedupTopBitCap) * 8, s, a);
-    launch_pdl(dedup_map, dim3(gi), dim3(256), 0, s, a);
-    return launches + 2;
+    launch_pdl(dedup_sort, dim3(gs), dim3(kBucketThreads), kDedupTopBitCap * 8, s, a);
+    launch_dedup_map(a, s);
+    return 3;
 }
 
 }  // namespace dagc
