@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
     int shift = 64;
     uint32_t nb = 0;
     if (fuse) {
-        tslots = table_size_for(n);
+        tslots = table_size_for(n, false);
         nb = topbit_buckets(n, &shift);
         if (tslots > dd.table_cap || n > dd.item_cap || (uint64_t)nb * kDedupTopBitCap > dd.bucket_area) {
             if (blockIdx.x == 0 && threadIdx.x == 0) { atomicOr(a.err, kErrFallback); dd.state->nbuckets = 0; }
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
             if (fuse) {
                 // The node's hash into the dedup table; the first inserter of
                 // a hash is its representative and appends it to its bucket.
-                uint64_t sl = slot_hash(hv) & (tslots - 1);
+                uint64_t sl = home_slot(hv, tslots);
                 bool won = false, placed = false;
                 if (hv == 0) {
                     bad = true;  // 0 marks an empty slot
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
                         if (cur == 0)
                             cur = atomicCAS((unsigned long long*)(dd.table_key + 2 * sl), 0ull, (unsigned long long)hv);
                         if (cur == 0 || cur == hv) { won = cur == 0; placed = true; break; }
-                        sl = (sl + 1) & (tslots - 1);
+                        sl = next_slot(sl, tslots);
                     }
                 }
                 if (!placed && hv != 0) full = true;

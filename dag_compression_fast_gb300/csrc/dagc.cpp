@@ -350,7 +350,7 @@ struct dagc_context_t {
     uint64_t dedup_unique_limit = kDedupMaxUnique;  // lowered only to exercise the rerun
     void* table = nullptr;
     void* gtable = nullptr;  // fragment grouping scratch
-    uint64_t table_cap = 0;  // slots, a power of two
+    uint64_t table_cap = 0;  // slots (table_size_for of the largest item count so far)
     bool table_dirty = true;
     uint64_t fallbacks = 0;  // calls rerun with the radix form
     uint32_t* trace_err = nullptr;  // tracer error word
@@ -841,8 +841,7 @@ struct CreateLayout {
             item_cap = std::min<uint64_t>(p0cap, kDedupMaxItems);
             uniq_cap = std::min<uint64_t>(p0cap, std::min<uint64_t>(unique_limit, kDedupMaxUnique));
             bucket_area = dedup_bucket_area(uniq_cap);
-            table_slots = 1024;
-            while (table_slots < 2 * item_cap) table_slots <<= 1;
+            table_slots = std::max(table_size_for(item_cap, true), table_size_for(item_cap, false));
             o_islot = L.take<uint32_t>(item_cap);
             o_ukey = L.take<uint64_t>(uniq_cap);
             o_uslot = L.take<uint32_t>(uniq_cap);

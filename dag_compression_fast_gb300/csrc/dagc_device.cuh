@@ -22,11 +22,6 @@ __device__ __forceinline__ void pdl_prologue() {
 }
 
 // ------------------------------------------------ hash-set dedup table ----
-// Table slots for n items: a power of two >= 2n (at least 1024).
-__device__ __forceinline__ uint64_t table_size_for(uint64_t n) {
-    const uint64_t want = n < 512 ? 1024 : 2 * n;
-    return 1ull << (64 - __clzll(want - 1));
-}
 
 __device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
     // Finaliser of MurmurHash3 (published constants): spreads leaf masks,
@@ -38,6 +33,11 @@ __device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
     k ^= k >> 33;
     return k;
 }
+
+// A key's first slot in a table of S slots (any S): the high word of
+// slot_hash(k) * S; probing goes on to the next slot, wrapping at S.
+__device__ __forceinline__ uint64_t home_slot(uint64_t k, uint64_t S) { return __umul64hi(slot_hash(k), S); }
+__device__ __forceinline__ uint64_t next_slot(uint64_t s, uint64_t S) { return s + 1 == S ? 0 : s + 1; }
 
 // Buckets of the top-bit form: a power of two with ~kDedupPerBucket keys each
 // for u keys; a key's bucket is key >> *shift.

@@ -262,6 +262,16 @@ DAGC_HD uint64_t dedup_bucket_area(uint64_t uniq_cap) {
     const uint64_t most = (uint64_t)kDedupMaxBuckets * kDedupTopBitCap;
     return a < most ? a : most;
 }
+// Table slots for n items. Leaf masks repeat (about one distinct mask per ten
+// bricks): 1.25 n slots, at most 0.8 full even when every mask is distinct,
+// small enough to stay largely in the L2. Node hashes are about half distinct
+// and each probe step is a dependent round trip: kNodeTableQuarters / 4 * n
+// slots keep the load low. At least 1024 slots, a multiple of 32.
+constexpr uint64_t kNodeTableQuarters = 8;
+DAGC_HD uint64_t table_size_for(uint64_t n, bool leaf_masks) {
+    const uint64_t want = leaf_masks ? n + (n >> 2) : n * kNodeTableQuarters / 4;
+    return want < 1024 ? 1024 : (want + 31) & ~31ull;
+}
 struct DedupState {
     unsigned long long u;  // distinct keys found (zero before the level)
     uint32_t nbuckets, pad0;
@@ -274,7 +284,7 @@ struct DedupArgs {
     // caller sorts. Node hashes: winners go to the bucket of their top bits.
     bool to_list;
     uint64_t item_cap;
-    // Table of table_cap slots (a power of two), 16 bytes each so that a
+    // Table of table_cap slots, 16 bytes each so that a
     // slot's key and aux share a sector: table_key[2s] = key, 0 = empty (all
     // 0 on entry and exit); table_aux[2s] = representative item | unique id
     // << 32 (table_aux = table_key + 1).

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     pdl_prologue();
     if (!a.to_list && a.state->inserted) return;  // extract_level inserted this level's hashes
     const uint64_t n = *a.d_n;
-    const uint64_t S = table_size_for(n);
+    const uint64_t S = table_size_for(n, a.to_list);
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
             live[k] = i < n;
             h[k] = live[k] ? a.keys[i] : 0;
             if (live[k] && h[k] == 0) { bad = true; live[k] = false; }  // 0 marks an empty slot
-            s[k] = slot_hash(h[k]) & (S - 1);
+            s[k] = home_slot(h[k], S);
         }
         bool found[kIlp];
 #pragma unroll
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                 if (!pend[k]) continue;
                 if (cur[k] == 0) won[k] = true;
                 else if (cur[k] == h[k]) found[k] = true;
-                else { s[k] = (s[k] + 1) & (S - 1); any = true; }
+                else { s[k] = next_slot(s[k], S); any = true; }
             }
             if (!any) break;
         }
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
          b += (uint64_t)gridDim.x * blockDim.x)
         a.bucket_count[b] = 0;
     const uint64_t n = *a.d_n;
-    if (table_size_for(n) > a.table_cap || n > a.item_cap) return;  // insert did nothing
+    if (table_size_for(n, a.to_list) > a.table_cap || n > a.item_cap) return;  // insert did nothing
     const uint32_t last = a.out_capacity ? (uint32_t)(a.out_capacity - 1) : 0u;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     bool collision = false;
