@@ -94,34 +94,53 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) found[k] = false;
         // Leaf masks repeat (many items per key), and large levels are bound
-        // by L2 atomic throughput: read first, claim only an empty slot.
-        // Small node levels are bound by latency: claim directly (one round
-        // trip instead of two). Each round issues every pending item's read,
-        // then every claim, back to back (no result is used before the last
-        // one is issued).
+        // by L2 atomic throughput: read first, claim only an empty slot. The
+        // read takes a slot and the one after it (two loads in flight,
+        // usually one sector), so that a key displaced by one slot, or an
+        // empty slot right after an occupied one, costs no second round
+        // trip. Small node levels are bound by latency: claim directly (one
+        // round trip instead of two). Each round issues every pending item's
+        // reads, then every claim, back to back (no result is used before
+        // the last one is issued).
         const bool read_first = a.to_list || n > kDedupClaimFirstMax;
-        for (uint64_t probe = 0; probe < S; ++probe) {
+        for (uint64_t round = 0; round < S; ++round) {
             bool pend[kIlp], claim[kIlp];
-            uint64_t cur[kIlp];
+            uint64_t cur[kIlp], nxt[kIlp];
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
                 pend[k] = live[k] && !won[k] && !found[k];
+                claim[k] = pend[k];
                 cur[k] = 0;
+                nxt[k] = 0;
             }
             if (read_first) {
 #pragma unroll
-                for (int k = 0; k < kIlp; ++k)
-                    if (pend[k]) cur[k] = ld_relaxed(a.table_key + 2 * s[k]);
-            }
+                for (int k = 0; k < kIlp; ++k) {
+                    if (pend[k]) {
+                        cur[k] = ld_relaxed(a.table_key + 2 * s[k]);
+                        nxt[k] = ld_relaxed(a.table_key + 2 * next_slot(s[k], S));
+                    }
+                }
+                // In probe order: a match ends the search; the first empty
+                // slot is claimed; two other keys move the probe on by two.
 #pragma unroll
-            for (int k = 0; k < kIlp; ++k) claim[k] = pend[k] && cur[k] == 0;
+                for (int k = 0; k < kIlp; ++k) {
+                    if (!pend[k]) continue;
+                    if (cur[k] == h[k]) { found[k] = true; claim[k] = false; continue; }
+                    if (cur[k] == 0) continue;
+                    s[k] = next_slot(s[k], S);
+                    if (nxt[k] == h[k]) { found[k] = true; claim[k] = false; continue; }
+                    if (nxt[k] != 0) { s[k] = next_slot(s[k], S); claim[k] = false; }
+                }
+            }
 #pragma unroll
             for (int k = 0; k < kIlp; ++k)
                 if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + 2 * s[k]), 0ull, (unsigned long long)h[k]);
             bool any = false;
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
-                if (!pend[k]) continue;
+                if (!pend[k] || found[k]) continue;
+                if (!claim[k]) { any = true; continue; }  // both slots held other keys
                 if (cur[k] == 0) won[k] = true;
                 else if (cur[k] == h[k]) found[k] = true;
                 else { s[k] = next_slot(s[k], S); any = true; }
