@@ -207,7 +207,9 @@ struct ExtractSmem {
     uint64_t p_base;
 };
 
-__global__ void __launch_bounds__(kT) extract_level(ExtractArgs a) {
+// Three CTAs per SM (80 registers, ~47 KB of shared memory each): one more
+// tile's round trips in flight per SM than the two that 109 registers allowed.
+__global__ void __launch_bounds__(kT, 3) extract_level(ExtractArgs a) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ExtractSmem& S = *reinterpret_cast<ExtractSmem*>(smem_raw);
@@ -872,11 +874,24 @@ __global__ void iota_offset(uint32_t* out, uint64_t n, uint32_t offset) {
 
 int g_blocks_small = 152 * 8;
 
+// Asks for a shared-memory carveout that holds `ctas` CTAs of `smem` bytes
+// (the driver's default may pick a smaller one and cap the occupancy).
+void prefer_shared(const void* fn, size_t smem, int ctas) {
+    int dev = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (per_sm <= 0) return;
+    const size_t want = (size_t)ctas * (smem + 1024);  // 1 KB reserved per CTA
+    const int pct = (int)std::min<size_t>(100, (want * 100 + per_sm - 1) / per_sm);
+    cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 }  // namespace
 
 void kernels_configure() {
     cudaFuncSetAttribute(leaf_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LeafSmem));
     cudaFuncSetAttribute(extract_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ExtractSmem));
+    prefer_shared(reinterpret_cast<const void*>(extract_level), sizeof(ExtractSmem), 3);
     cudaFuncSetAttribute(unique_runs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(UniqueSmem));
     cudaFuncSetAttribute(tail_levels, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TailSmem));
     int dev = 0, sms = 152;

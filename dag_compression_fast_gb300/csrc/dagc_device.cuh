@@ -38,6 +38,7 @@ __device__ __forceinline__ uint64_t slot_hash(uint64_t k) {
 // slot_hash(k) * S; probing goes on to the next slot, wrapping at S.
 __device__ __forceinline__ uint64_t home_slot(uint64_t k, uint64_t S) { return __umul64hi(slot_hash(k), S); }
 __device__ __forceinline__ uint64_t next_slot(uint64_t s, uint64_t S) { return s + 1 == S ? 0 : s + 1; }
+__device__ __forceinline__ uint32_t next_slot(uint32_t s, uint32_t S) { return s + 1 == S ? 0u : s + 1; }
 
 // Buckets of the top-bit form: a power of two with ~kDedupPerBucket keys each
 // for u keys; a key's bucket is key >> *shift.

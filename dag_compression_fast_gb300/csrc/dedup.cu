@@ -46,11 +46,12 @@ __device__ __forceinline__ uint64_t unique_count(const DedupArgs& a) {
 // Items per lane in flight at once (independent probe chains).
 constexpr int kIlp = 4;
 
-__global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
+__global__ void __launch_bounds__(256, 4) dedup_insert(DedupArgs a) {
     pdl_prologue();
     if (!a.to_list && a.state->inserted) return;  // extract_level inserted this level's hashes
     const uint64_t n = *a.d_n;
     const uint64_t S = table_size_for(n, a.to_list);
+    const uint32_t S32 = (uint32_t)S;
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t gsize = (uint64_t)gridDim.x * blockDim.x;
@@ -79,7 +80,8 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
     // slot takes an atomicCAS: duplicated keys (common leaf masks) would
     // otherwise serialise on their slot's atomics.
     for (uint64_t base = warp * 32 * kIlp; base < n; base += warps * 32 * kIlp) {
-        uint64_t h[kIlp], s[kIlp];
+        uint64_t h[kIlp];
+        uint32_t s[kIlp];  // slot indices (tables hold fewer than 2^32 slots)
         bool live[kIlp], won[kIlp];
 #pragma unroll
         for (int k = 0; k < kIlp; ++k) {
@@ -88,7 +90,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
             live[k] = i < n;
             h[k] = live[k] ? a.keys[i] : 0;
             if (live[k] && h[k] == 0) { bad = true; live[k] = false; }  // 0 marks an empty slot
-            s[k] = home_slot(h[k], S);
+            s[k] = (uint32_t)home_slot(h[k], S);
         }
         bool found[kIlp];
 #pragma unroll
@@ -117,8 +119,8 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
 #pragma unroll
                 for (int k = 0; k < kIlp; ++k) {
                     if (pend[k]) {
-                        cur[k] = ld_relaxed(a.table_key + 2 * s[k]);
-                        nxt[k] = ld_relaxed(a.table_key + 2 * next_slot(s[k], S));
+                        cur[k] = ld_relaxed(a.table_key + 2ull * s[k]);
+                        nxt[k] = ld_relaxed(a.table_key + 2ull * next_slot(s[k], S32));
                     }
                 }
                 // In probe order: a match ends the search; the first empty
@@ -128,14 +130,14 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     if (!pend[k]) continue;
                     if (cur[k] == h[k]) { found[k] = true; claim[k] = false; continue; }
                     if (cur[k] == 0) continue;
-                    s[k] = next_slot(s[k], S);
+                    s[k] = next_slot(s[k], S32);
                     if (nxt[k] == h[k]) { found[k] = true; claim[k] = false; continue; }
-                    if (nxt[k] != 0) { s[k] = next_slot(s[k], S); claim[k] = false; }
+                    if (nxt[k] != 0) { s[k] = next_slot(s[k], S32); claim[k] = false; }
                 }
             }
 #pragma unroll
             for (int k = 0; k < kIlp; ++k)
-                if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + 2 * s[k]), 0ull, (unsigned long long)h[k]);
+                if (claim[k]) cur[k] = atomicCAS((unsigned long long*)(a.table_key + 2ull * s[k]), 0ull, (unsigned long long)h[k]);
             bool any = false;
 #pragma unroll
             for (int k = 0; k < kIlp; ++k) {
@@ -143,7 +145,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                 if (!claim[k]) { any = true; continue; }  // both slots held other keys
                 if (cur[k] == 0) won[k] = true;
                 else if (cur[k] == h[k]) found[k] = true;
-                else { s[k] = next_slot(s[k], S); any = true; }
+                else { s[k] = next_slot(s[k], S32); any = true; }
             }
             if (!any) break;
         }
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
             if (i < n) {
                 const bool placed = live[k] && (won[k] || found[k]);
                 if (live[k] && !placed) full = true;  // cannot happen below half load; rerun rather than guess
-                a.item_slot[i] = placed ? (uint32_t)s[k] : 0xFFFFFFFFu;
+                a.item_slot[i] = placed ? s[k] : 0xFFFFFFFFu;
             }
         }
         // Winners append to the unique list: one atomic per warp for all its
@@ -175,10 +177,10 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                 if (won[k]) {
                     const uint64_t i = base + k * 32 + lane;
                     const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
-                    aux[4 * s[k]] = (uint32_t)i;
+                    aux[4ull * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap) {
                         a.uniq_key[pos] = h[k];
-                        a.uniq_slot[pos] = (uint32_t)s[k];
+                        a.uniq_slot[pos] = s[k];
                     } else {
                         full = true;
                     }
@@ -199,10 +201,10 @@ __global__ void __launch_bounds__(256) dedup_insert(DedupArgs a) {
                     const uint64_t i = base + k * 32 + lane;
                     const uint64_t pos = pos0 + __popc(wm[k] & lanemask_lt());
                     const uint32_t b = shift >= 64 ? 0u : (uint32_t)(h[k] >> shift);
-                    aux[4 * s[k]] = (uint32_t)i;
+                    aux[4ull * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap && bslot[k] < kDedupTopBitCap) {
                         const uint64_t e = (uint64_t)b * kDedupTopBitCap + bslot[k];
-                        a.bucket[e] = make_uint4((uint32_t)h[k], (uint32_t)(h[k] >> 32), (uint32_t)s[k], (uint32_t)i);
+                        a.bucket[e] = make_uint4((uint32_t)h[k], (uint32_t)(h[k] >> 32), s[k], (uint32_t)i);
                     } else {
                         full = true;
                     }
