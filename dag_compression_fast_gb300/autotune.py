@@ -6,8 +6,8 @@ module, or --out).
 A sort class is (keys-only or key/value, number of sorted bits, power of two
 of the key count). The grid covers the sorts the compression path runs: the
 fragment sort on the brick bits [6, 3*depth) for depths 7-13 and the batched
-composite keys, the brick sort of the grouping path, and the 64-bit hash
-sorts of the radix dedup form.
+composite keys, the brick sort of the grouping path, the 64-bit hash
+sorts of the radix dedup form and the sort of the distinct leaf masks.
 
   python -m dag_compression_fast_gb300.autotune [--reps 3] [--out FILE] [--quick]
 
@@ -25,7 +25,7 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_OUT = os.path.join(HERE, "sort_plans.json")
 
-KEY_BITS = [15, 18, 21, 24, 27, 30, 32, 33, 36, 39]
+KEY_BITS = [15, 18, 21, 24, 27, 30, 32, 33, 36, 39, 64]
 PAIR_BITS = [15, 21, 27, 32, 33, 64]
 
 

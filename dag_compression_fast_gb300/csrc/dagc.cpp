@@ -799,7 +799,7 @@ struct CreateLayout {
     // Hash-set dedup (when `dedup`): per-item slots, the unique list, buckets.
     bool dedup = false;
     uint64_t item_cap = 0, uniq_cap = 0, bucket_area = 0, table_slots = 0;
-    size_t o_islot = 0, o_ukey = 0, o_uslot = 0, o_ukey_alt = 0, o_uslot_sorted = 0, o_uslot_alt = 0;
+    size_t o_islot = 0, o_ukey = 0, o_ukey_alt = 0;
     size_t o_bcnt = 0, o_bent = 0;
     // Persistent per-chunk leaves (batched form): zeroed chunk state
     // (histograms, cursors, done counters, item counter), tile offsets, the
@@ -844,13 +844,9 @@ struct CreateLayout {
             table_slots = std::max(table_size_for(item_cap, true), table_size_for(item_cap, false));
             o_islot = L.take<uint32_t>(item_cap);
             o_ukey = L.take<uint64_t>(uniq_cap);
-            o_uslot = L.take<uint32_t>(uniq_cap);
-            // The (key, slot) sort of the unique leaf masks: its other key
-            // buffer, its slots out and their other buffer (the keys go out
-            // to the leaf array).
+            // The other key buffer of the unique leaf masks' sort (the sorted
+            // keys go out to the leaf array).
             o_ukey_alt = L.take<uint64_t>(uniq_cap);
-            o_uslot_sorted = L.take<uint32_t>(uniq_cap);
-            o_uslot_alt = L.take<uint32_t>(uniq_cap);
             o_bcnt = L.take<uint32_t>(kDedupMaxBuckets);
             o_bent = L.take<uint4>(bucket_area);
         }
@@ -1132,7 +1128,6 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             d.table_cap = ctx->table_cap;
             d.item_slot = P32(Lo.o_islot);
             d.uniq_key = P64(Lo.o_ukey);
-            d.uniq_slot = P32(Lo.o_uslot);
             d.uniq_cap = Lo.uniq_cap;
             d.bucket_count = P32(Lo.o_bcnt);
             d.bucket = reinterpret_cast<uint4*>(b + Lo.o_bent);
@@ -1149,18 +1144,17 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
         };
         if (use_dedup) {
             // Distinct masks into the table and the unique list; the list
-            // sorted as (mask, slot) pairs straight into the leaf array; each
-            // slot gets its mask's rank as unique id; every brick its id.
+            // sorted (keys only) straight into the leaf array; each mask's
+            // slot gets the mask's rank as unique id; every brick its id.
             const DedupArgs d = dedup_args(P64(Lo.o_LM), cs.count(kCntBricks), nullptr, nullptr, P64(Lo.o_PL), nullptr,
                                            nullptr, p0cap, cs.count(kCntLeaves), P32(Lo.o_M0));
             launch_dedup_insert(d, s);
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
-            st = run_sort(ctx, cs, sb, P64(Lo.o_ukey), P64(Lo.o_PL), P64(Lo.o_ukey_alt), P32(Lo.o_uslot),
-                          P32(Lo.o_uslot_sorted), P32(Lo.o_uslot_alt), true, Lo.uniq_cap,
-                          reinterpret_cast<const uint64_t*>(&d.state->u), 0, 64, 0, s);
+            st = run_sort(ctx, cs, sb, P64(Lo.o_ukey), P64(Lo.o_PL), P64(Lo.o_ukey_alt), nullptr, nullptr, nullptr,
+                          false, Lo.uniq_cap, reinterpret_cast<const uint64_t*>(&d.state->u), 0, 64, 0, s);
             if (st) return st;
-            launch_dedup_assign(d, P32(Lo.o_uslot_sorted), s);
+            launch_dedup_assign(d, P64(Lo.o_PL), s);
             launch_dedup_map(d, s);
             ctx->launches += 2;
             DAGC_LAUNCHED(ctx);

@@ -290,7 +290,7 @@ struct DedupArgs {
     // << 32 (table_aux = table_key + 1).
     uint64_t* table_key; uint64_t* table_aux; uint64_t table_cap;
     uint32_t* item_slot;
-    uint64_t* uniq_key; uint32_t* uniq_slot; uint64_t uniq_cap;  // the unique list (leaf masks)
+    uint64_t* uniq_key; uint64_t uniq_cap;  // the unique list (leaf masks)
     uint32_t* bucket_count;                                       // kDedupMaxBuckets
     // Bucket entries, one 16-byte store each: key (two words), slot, representative.
     uint4* bucket; uint64_t bucket_area;
@@ -305,9 +305,9 @@ void dedup_configure(int sms);
 // the number of launches.
 int launch_dedup(const DedupArgs& a, cudaStream_t s);
 // Leaf masks: insert into the table and the unique list; after the caller's
-// (key, slot) sort of the list, assign the unique ids; then map.
+// sort of the list (keys only), assign the unique ids; then map.
 void launch_dedup_insert(const DedupArgs& a, cudaStream_t s);
-void launch_dedup_assign(const DedupArgs& a, const uint32_t* sorted_slot, cudaStream_t s);
+void launch_dedup_assign(const DedupArgs& a, const uint64_t* sorted, cudaStream_t s);
 void launch_dedup_map(const DedupArgs& a, cudaStream_t s);
 
 constexpr uint64_t kFuseInsertMax = 1ull << 20;

@@ -9,24 +9,26 @@
 //   dedup_insert   every item inserts its key into an open-addressing table
 //                  (linear probing, atomicCAS on the key); the first inserter
 //                  of a key records itself as the slot's representative and
-//                  appends (key, slot) to the unique list (leaf masks) or
+//                  appends its key to the unique list (leaf masks) or
 //                  (key, slot, itself) straight to its bucket (node hashes:
 //                  MurmurHash outputs, so their top bits are the bucket and
 //                  the bucket count follows from the item count; dedup_map of
 //                  the previous level zeroed the bucket counters);
 //   leaf masks     (far from uniform) the unique list is ordered by a 64-bit
-//                  radix sort of (key, slot) pairs (the caller's sort), then
-//   dedup_assign   gives each sorted key's slot its unique id (its rank) and
-//                  clears the slot's key;
+//                  keys-only radix sort (the caller's sort), then
+//   dedup_assign   finds each sorted key's slot (probing as the insert did)
+//                  and gives it its unique id (its rank);
 //   dedup_sort     (node hashes) each bucket is ranked in shared memory (rank
 //                  = number of smaller keys) and written at its global ranks,
 //                  with the representative's payload; the unique id goes to
 //                  the slot and the slot's key is cleared;
 //   dedup_map      every item reads its unique id and representative through
 //                  its slot, duplicates are compared in full with their
-//                  representative (collision check). The slots' keys were
-//                  cleared once per distinct key (items sharing a slot only
-//                  read its aux word).
+//                  representative (collision check). Every slot's key is
+//                  cleared once per distinct key: by dedup_sort (node hashes)
+//                  or here by the key's representative (leaf masks, after
+//                  every probe of dedup_assign); items sharing a slot
+//                  otherwise only read its aux word.
 //
 // What the fixed sizes cannot hold (table, unique list, a bucket) sets
 // kErrFallback, and the caller reruns the call with the radix-sort form.
@@ -180,7 +182,6 @@ __global__ void __launch_bounds__(256, 4) dedup_insert(DedupArgs a) {
                     aux[4ull * s[k]] = (uint32_t)i;
                     if (pos < a.uniq_cap) {
                         a.uniq_key[pos] = h[k];
-                        a.uniq_slot[pos] = s[k];
                     } else {
                         full = true;
                     }
@@ -217,24 +218,34 @@ __global__ void __launch_bounds__(256, 4) dedup_insert(DedupArgs a) {
     if (full) atomicOr(a.err, kErrFallback);
 }
 
-// Leaf masks, after the (key, slot) sort of the unique list: the key of rank
-// r is the r-th distinct key; its slot gets unique id r and an empty key.
-__global__ void __launch_bounds__(256) dedup_assign(DedupArgs a, const uint32_t* sorted_slot) {
+// Leaf masks, after the sort of the unique list: the key of rank r is the
+// r-th distinct key; the slot holding it (found by the insert's probe
+// sequence, every key being in the table) gets unique id r. The keys stay
+// until dedup_map: clearing one here could cut another key's probe sequence.
+__global__ void __launch_bounds__(256) dedup_assign(DedupArgs a, const uint64_t* sorted) {
     pdl_prologue();
     const uint64_t u = unique_count(a);
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.d_out_n = u < a.out_capacity ? u : a.out_capacity;
+    const uint64_t n = *a.d_n;
+    const uint64_t S = table_size_for(n, true);
+    if (S > a.table_cap || n > a.item_cap) return;  // insert did nothing (fallback set)
+    const uint32_t S32 = (uint32_t)S;
     uint32_t* aux = reinterpret_cast<uint32_t*>(a.table_aux);
-    bool bad = false;
+    bool lost = false;
     for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < u; r += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t sl = sorted_slot[r];
-        if (sl < a.table_cap && r < a.out_capacity) {
-            aux[4 * (uint64_t)sl + 1] = (uint32_t)r;
-            a.table_key[2 * (uint64_t)sl] = 0;  // the slot is empty for the next level (dedup_map reads only aux)
-        } else {
-            bad = true;
+        const uint64_t key = sorted[r];
+        uint32_t sl = (uint32_t)home_slot(key, S);
+        bool hit = false;
+        for (uint32_t probe = 0; probe < S32; ++probe) {
+            const uint64_t cur = a.table_key[2ull * sl];
+            if (cur == key) { hit = true; break; }
+            if (cur == 0) break;
+            sl = next_slot(sl, S32);
         }
+        if (hit && r < a.out_capacity) aux[4ull * sl + 1] = (uint32_t)r;
+        else lost = true;
     }
-    if (bad) atomicOr(a.err, kErrCapacity);
+    if (lost) atomicOr(a.err, kErrCapacity);
 }
 
 // Each CTA takes a contiguous range of buckets; a bucket's keys are distinct,
@@ -366,6 +377,7 @@ __global__ void __launch_bounds__(256) dedup_map(DedupArgs a) {
             if (s[k] < a.table_cap) {
                 const uint32_t rep = (uint32_t)aux[k];
                 uid = (uint32_t)(aux[k] >> 32);
+                if (a.to_list && rep == (uint32_t)i) a.table_key[2 * (uint64_t)s[k]] = 0;  // empty for the next level
                 if (a.masks && rep != (uint32_t)i && rep < n) {
                     const uint4* x = reinterpret_cast<const uint4*>(a.children + i * 8);
                     const uint4* y = reinterpret_cast<const uint4*>(a.children + (uint64_t)rep * 8);
@@ -403,10 +415,10 @@ void launch_dedup_insert(const DedupArgs& a, cudaStream_t s) {
     launch_pdl(dedup_insert, dim3(item_grid(a)), dim3(256), 0, s, a);
 }
 
-void launch_dedup_assign(const DedupArgs& a, const uint32_t* sorted_slot, cudaStream_t s) {
+void launch_dedup_assign(const DedupArgs& a, const uint64_t* sorted, cudaStream_t s) {
     const uint64_t want = (a.uniq_cap + 255) / 256;
     const int g = (int)(want < (uint64_t)(8 * g_sms) ? (want > 0 ? want : 1) : 8 * g_sms);
-    launch_pdl(dedup_assign, dim3(g), dim3(256), 0, s, a, sorted_slot);
+    launch_pdl(dedup_assign, dim3(g), dim3(256), 0, s, a, sorted);
 }
 
 void launch_dedup_map(const DedupArgs& a, cudaStream_t s) {

@@ -31,12 +31,15 @@ def main(argv=None) -> int:
     p.add_argument("--fraction", type=float, default=1.0, help="terrain column / soup triangle fraction")
     p.add_argument("--seed", type=int, default=0xDA6C0DE + 1)
     p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--group", choices=["auto", "sort", "group"], default="auto",
+                   help="leaf path: the device's choice, always the fragment sort, always grouping (DAGC_OPT_GROUP)")
     a = p.parse_args(argv)
     import torch
 
     import dag_compression_fast_gb300 as D
     codes = make(a.workload, a.depth, a.fraction, a.seed)
     ctx = D.Context(0)
+    ctx.set_option(D.OPT_GROUP, {"auto": 1, "sort": 0, "group": 2}[a.group])
     t = torch.from_numpy(codes.view(np.int64)).cuda()
     s = torch.cuda.current_stream()
     for i in range(a.steps):
