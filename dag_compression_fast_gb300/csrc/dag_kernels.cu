@@ -42,13 +42,16 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* counter, uint32_t* s_slo
 // ---------------------------------------------------------------------------
 // Tiles of kLeafTile sorted keys; thread t holds keys [16t, 16t + 16) of the
 // tile in registers (one 128-byte line, eight 16-byte loads), so shared memory
-// carries only one word per thread.
+// carries only one word per thread. 512 threads per tile, two CTAs per SM:
+// every tile waits once for its predecessors' run counts (the look-back), so
+// larger tiles wait less per key.
 constexpr int kLeafItems = 16;
-static_assert(kLeafTile == kT * kLeafItems, "leaf tile = 256 threads x 16 keys");
+constexpr int kLeafThreads = 512;
+static_assert(kLeafTile == kLeafThreads * kLeafItems, "leaf tile = 512 threads x 16 keys");
 
 struct LeafSmem {
-    uint64_t lead[kT];   // OR of the thread's keys before its first run head (all keys if none)
-    uint8_t has_head[kT];
+    uint64_t lead[kLeafThreads];   // OR of the thread's keys before its first run head (all keys if none)
+    uint8_t has_head[kLeafThreads];
     uint32_t scan[34];
     uint32_t slot;
     uint64_t p_base;
@@ -69,7 +72,7 @@ __device__ __forceinline__ uint64_t global_code(const LeafBuildArgs& a, uint64_t
 // memory) up to the next head. Keys before the tile's first head continue a
 // run of an earlier tile: their OR goes to lead_or[tile] and leaf_fixup folds
 // it in after this kernel.
-__global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
+__global__ void __launch_bounds__(kLeafThreads, 2) leaf_build(LeafBuildArgs a) {
     pdl_prologue();
     __shared__ LeafSmem S;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
                     acc |= open ? 1ull << (k[j] & 63) : 0ull;
                 }
             }
-            for (uint32_t t = tid + 1; t < (uint32_t)kT; ++t) {
+            for (uint32_t t = tid + 1; t < (uint32_t)kLeafThreads; ++t) {
                 acc |= S.lead[t];
                 if (S.has_head[t]) break;
             }
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(kT) leaf_build(LeafBuildArgs a) {
             // Keys continuing the previous run: folded in by leaf_fixup. Tile 0
             // starts with a head, so it never has any.
             uint64_t lo = 0;
-            for (uint32_t t = 0; t < (uint32_t)kT; ++t) {
+            for (uint32_t t = 0; t < (uint32_t)kLeafThreads; ++t) {
                 lo |= S.lead[t];
                 if (S.has_head[t]) break;
             }
@@ -904,7 +907,7 @@ int occupancy_kernel(int which) {
     int occ = 0;
     switch (which) {
         case kKernelLeafBuild:
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_build, kT, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, leaf_build, kLeafThreads, 0);
             break;
         case kKernelExtract:
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, extract_level, kT, sizeof(ExtractSmem));
@@ -920,7 +923,7 @@ int occupancy_kernel(int which) {
 }
 
 void launch_leaf_build(const LeafBuildArgs& a, cudaStream_t s) {
-    launch_pdl(leaf_build, dim3(a.grid), dim3(kT), 0, s, a);
+    launch_pdl(leaf_build, dim3(a.grid), dim3(kLeafThreads), 0, s, a);
     const uint64_t tiles = leaf_tiles(a.n_bound);
     const int grid = (int)std::min<uint64_t>((tiles + 255) / 256, (uint64_t)g_blocks_small);
     launch_pdl(leaf_fixup, dim3(grid > 0 ? grid : 1), dim3(256), 0, s, a);
