@@ -915,6 +915,9 @@ int occupancy_kernel(int which) {
         case kKernelUnique:
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, unique_runs, kT, sizeof(UniqueSmem));
             break;
+        case kKernelFinalWrite:
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, final_write, kT, 0);
+            break;
         default:
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, final_positions, kT, 0);
             break;

@@ -1958,14 +1958,16 @@ int dagc_context_create(int device, dagc_context* out) {
             if (load_tune_file(c.get(), tune_path.c_str()) == DAGC_OK) c->tune_file = tune_path;
         }
     }
-    c->grid_hist = 8 * c->sms;
+    c->grid_hist = std::max(1, occupancy_sort_histogram()) * c->sms;
     c->grid_leaf = std::max(1, occupancy_kernel(0)) * c->sms;
     if (const char* e = std::getenv("DAGC_SCAN_CTAS_PER_SM"))
         c->grid_leaf = std::min(c->grid_leaf, std::max(1, std::atoi(e)) * c->sms);
     c->grid_extract = std::max(1, occupancy_kernel(1)) * c->sms;
     c->grid_unique = std::max(1, occupancy_kernel(2)) * c->sms;
     c->grid_scan = std::max(1, occupancy_kernel(3)) * c->sms;
-    c->grid_write = 8 * c->sms;
+    // Grid-stride kernels get the resident CTA count: a second, partial wave
+    // of CTAs with full shares would run at a fraction of the occupancy.
+    c->grid_write = std::max(1, occupancy_kernel(kKernelFinalWrite)) * c->sms;
     dedup_configure(c->sms);
     group_configure(c->sms);
     chunk_configure(c->sms);

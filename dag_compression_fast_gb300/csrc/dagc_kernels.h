@@ -110,6 +110,7 @@ constexpr int kNumSortShapes = kNumPairShapes;
 int sort_shape_items(int shape, bool with_values);
 // Resident CTAs per SM of a shape at a digit width (occupancy query) for grid sizing.
 int occupancy_sort_shape(int shape, bool with_values, int radix_bits = kRadixBits);
+int occupancy_sort_histogram();
 // Whether a (shape, width) plan can sort bits [lo, hi): histogram room and
 // look-back status room.
 bool sort_plan_valid(int shape, bool with_values, int radix_bits, int lo_bit, int hi_bit);
@@ -415,7 +416,7 @@ void launch_copy_segments(const CopyTable& t, cudaStream_t s);
 void kernels_configure();
 
 // Resident CTAs per SM of the persistent kernels (for grid sizing).
-enum KernelId { kKernelLeafBuild = 0, kKernelExtract = 1, kKernelUnique = 2, kKernelFinalScan = 3 };
+enum KernelId { kKernelLeafBuild = 0, kKernelExtract = 1, kKernelUnique = 2, kKernelFinalScan = 3, kKernelFinalWrite = 4 };
 int occupancy_kernel(int which);
 
 }  // namespace dagc

@@ -121,22 +121,24 @@ __global__ void __launch_bounds__(kSortThreads) radix_histogram(HistParams h) {
     if (blockIdx.x >= active) return;
     const uint64_t astride = (uint64_t)active * blockDim.x;
 
-    // Four independent loads in flight per thread (grid-stride, unrolled).
-    // A thread's positions only grow, so its segment (batched input) is found
-    // once by binary search and then followed forward.
+    // Eight independent loads in flight per thread (grid-stride, unrolled):
+    // the pass is bound by the bytes in flight. A thread's positions only
+    // grow, so its segment (batched input) is found once by binary search and
+    // then followed forward.
+    constexpr int kHistIlp = 8;
     uint64_t bad = 0;
     uint32_t sg = h.seg_offsets && gtid < n ? segment_search(h.seg_offsets, h.seg_count, gtid) : 0u;
-    for (uint64_t i0 = gtid; i0 < n; i0 += 4 * astride) {
-        uint64_t k[4];
-        bool in[4];
+    for (uint64_t i0 = gtid; i0 < n; i0 += kHistIlp * astride) {
+        uint64_t k[kHistIlp];
+        bool in[kHistIlp];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kHistIlp; ++u) {
             const uint64_t i = i0 + u * astride;
             in[u] = i < n;
             k[u] = in[u] ? __ldg(h.keys + i) : 0;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kHistIlp; ++u) {
             if (!in[u]) continue;
             if (h.validate_bits > 0 && h.validate_bits < 64) bad |= k[u] >> h.validate_bits;
             if (h.seg_offsets) {
@@ -703,6 +705,17 @@ void sort_configure() {
         if (e.kernel.smem <= kMaxPassSmem)
             cudaFuncSetAttribute(e.kernel.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.kernel.smem);
     cudaGetLastError();  // an attribute the device refuses leaves no error behind for later checks
+}
+
+// CTAs of radix_histogram resident per SM: its grid, so that no second wave
+// of CTAs with a full grid-stride share runs at a fraction of the occupancy.
+int occupancy_sort_histogram() {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, radix_histogram, kSortThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        occ = 0;
+    }
+    return occ;
 }
 
 int occupancy_sort_shape(int shape, bool with_values, int radix_bits) {

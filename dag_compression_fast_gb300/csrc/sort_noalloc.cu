@@ -58,6 +58,7 @@ struct DeviceSetup {
     void* scratch = nullptr;  // device address of g_noalloc_scratch on this device
     int sms = 0;
     int occ_pass = 0;
+    int hist_per_sm = 0;
 };
 std::mutex g_setup_mu;
 DeviceSetup g_setup[kMaxDevices];
@@ -83,6 +84,8 @@ int setup_current_device(DeviceSetup* out) {
         d.sms = sms;
         d.occ_pass = occupancy_sort_shape(kNoAllocShape, false, kRadixBits);
         if (d.occ_pass < 1) d.occ_pass = 1;
+        d.hist_per_sm = occupancy_sort_histogram();
+        if (d.hist_per_sm < 1) d.hist_per_sm = 1;
         d.scratch = p;
     }
     *out = d;
@@ -132,7 +135,7 @@ extern "C" int dagc_sort_keys_noalloc(const uint64_t* d_in, uint64_t* d_out, uin
     const uint64_t tiles = (n + tile - 1) / tile;
     const uint64_t resident = (uint64_t)dev.occ_pass * (uint64_t)dev.sms;
     a.grid_pass = (int)(tiles < resident ? tiles : resident);
-    const uint64_t hist_blocks = (n + 4095) / 4096, hist_cap = 8ull * (uint64_t)dev.sms;
+    const uint64_t hist_blocks = (n + 4095) / 4096, hist_cap = (uint64_t)dev.hist_per_sm * (uint64_t)dev.sms;
     a.grid_hist = (int)(hist_blocks < hist_cap ? hist_blocks : hist_cap);
     a.shape = kNoAllocShape;
     a.radix_bits = kRadixBits;
