@@ -14,8 +14,9 @@ Second workload, reported under "terrain_2048": the fBm terrain heightfield
 of a 2048^3 grid (depth 11), ~31.5M fragments, on which the device takes the
 fragment-grouping path.
 
-One step = DAGCompression::CreateDAG + CreateFinalDAG through the dagc C ABI,
-from device-resident fragments to the device-resident uint32 DAG.
+One step = DAGCompression::CreateDAG + CreateFinalDAG through the dagc C ABI
+(dagc_compress, both in one call), from device-resident fragments to the
+device-resident uint32 DAG.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -315,8 +316,9 @@ def main():
         return x
 
     def step_on(frags, dp):
-        dag = ctx.create_dag(frags, dp)
-        words = ctx.create_final_dag(dag)
+        # CreateDAG + CreateFinalDAG in one call (dagc_compress): the words
+        # come straight from the call's level pools, no DAG copied out.
+        words = ctx.compress(frags, dp)
         nw = words.n
         words.free()
         return nw

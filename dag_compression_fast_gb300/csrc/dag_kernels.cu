@@ -735,23 +735,48 @@ struct FinalScanSmem {
     uint64_t p_base;
 };
 
+// The level table of FinalArgs in shared memory (indexed at run time).
+struct FinalLevels {
+    const uint8_t* masks[kFinalMaxLevels];
+    const uint32_t* children[kFinalMaxLevels];
+    uint64_t off[kFinalMaxLevels + 1];
+};
+__device__ __forceinline__ void load_levels(const FinalArgs& a, FinalLevels& L) {
+    const int t = threadIdx.x;
+    if (t < a.num_levels) { L.masks[t] = a.lv_masks[t]; L.children[t] = a.lv_children[t]; }
+    if (t <= a.num_levels) L.off[t] = a.lv_off[t];
+    __syncthreads();
+}
+// Level of node i, searching up from level l (nodes are visited in order).
+__device__ __forceinline__ int level_of(const FinalLevels& L, int num_levels, uint64_t i, int l) {
+    while (l + 1 < num_levels && i >= L.off[l + 1]) ++l;
+    return l;
+}
+
 // word_pos[i] = sum over nodes j < i of (popc(mask_j) + 1); word_pos[n] = total.
 __global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
     pdl_prologue();
     __shared__ FinalScanSmem S;
+    __shared__ FinalLevels LV;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t n = a.num_nodes;
     const uint32_t ntiles = scan_tiles(n);
     if (blockIdx.x >= ntiles) return;  // grids are sized by an upper bound on n
+    load_levels(a, LV);
     while (true) {
         const uint32_t tile = next_tile(a.tile_counter, &S.slot);
         if (tile >= ntiles) break;
         const uint64_t i0 = (uint64_t)tile * kTile + (uint64_t)tid * kI;
         uint32_t w[kI];
         uint32_t sum = 0;
+        int l = level_of(LV, a.num_levels, i0, 0);
 #pragma unroll
         for (int j = 0; j < kI; ++j) {
-            w[j] = i0 + j < n ? (uint32_t)__popc(a.masks[i0 + j]) + 1u : 0u;
+            w[j] = 0;
+            if (i0 + j < n) {
+                l = level_of(LV, a.num_levels, i0 + j, l);
+                w[j] = (uint32_t)__popc(LV.masks[l][i0 + j - LV.off[l]]) + 1u;
+            }
             sum += w[j];
         }
         uint32_t total;
@@ -777,9 +802,9 @@ __global__ void __launch_bounds__(kT) final_positions(FinalArgs a) {
 
 __global__ void __launch_bounds__(kT) final_write(FinalArgs a) {
     pdl_prologue();
-    __shared__ uint64_t s_off[24];
-    if (threadIdx.x <= (unsigned)a.num_levels) s_off[threadIdx.x] = a.level_offsets[threadIdx.x];
-    __syncthreads();
+    __shared__ FinalLevels LV;
+    load_levels(a, LV);
+    const uint64_t* s_off = LV.off;
     const uint64_t n = a.num_nodes;
     const uint64_t leaf_start = a.word_pos[n];
     const uint64_t gstride = (uint64_t)gridDim.x * blockDim.x;
@@ -792,13 +817,13 @@ __global__ void __launch_bounds__(kT) final_write(FinalArgs a) {
             a.words[leaf_start + 2 * j + 1] = (uint32_t)(leaf >> 32);
             continue;
         }
-        int l = 0;
-        while (l + 1 < a.num_levels && i >= s_off[l + 1]) ++l;
+        const int l = level_of(LV, a.num_levels, i, 0);
         const bool last = l + 1 == a.num_levels;
-        const uint32_t mask = a.masks[i];
+        const uint64_t li = i - s_off[l];
+        const uint32_t mask = LV.masks[l][li];
         const uint64_t pos = a.word_pos[i];
         a.words[pos] = mask;
-        const uint4* src = reinterpret_cast<const uint4*>(a.children + i * 8);
+        const uint4* src = reinterpret_cast<const uint4*>(LV.children[l] + li * 8);
         const uint4 c0 = src[0], c1 = src[1];
         const uint32_t ch[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
         uint32_t k = 1;

@@ -1430,44 +1430,64 @@ int empty_dag(dagc_context ctx, int nl, dagc_dag* out) {
 }
 
 // --------------------------------------------------------- CreateFinalDAG --
-int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, uint64_t* n_words) {
+// The node levels (root first) and leaves that CreateFinalDAG lays out.
+struct FinalSource {
+    std::vector<const uint8_t*> masks;     // per level
+    std::vector<const uint32_t*> children;  // per level, 8 per node
+    std::vector<uint64_t> off;              // num_levels + 1 node offsets
+    const uint64_t* leaves = nullptr;
+    uint64_t num_leaves = 0;
+};
+
+// Bytes of arena scratch the final layout of nn nodes takes (from offset 0).
+size_t final_scratch_bytes(uint64_t nn) {
+    Layout L;
+    L.take<CallHeader>(1);
+    L.take<uint64_t>(scan_tiles(nn) + 1);
+    L.take<uint32_t>(nn + 1);
+    return L.off;
+}
+
+// Positions and words of `src`, their scratch at the start of the arena,
+// which the caller has reserved and made safe to write.
+int final_words(dagc_context ctx, const FinalSource& src, cudaStream_t s, uint32_t** d_words, uint64_t* n_words) {
     t_pdl = ctx->pdl;
     *d_words = nullptr;
     *n_words = 0;
-    if (d->num_leaves == 0) return DAGC_OK;
-    const uint64_t nn = d->num_nodes();
+    const int nlv = (int)src.masks.size();
+    if (nlv > kFinalMaxLevels) return set_error(ctx, DAGC_ERR_TOO_LARGE, "too many levels");
+    const uint64_t nn = src.off[nlv];
     Layout L;
     const size_t o_hdr = L.take<CallHeader>(1);
     const uint64_t svt = scan_tiles(nn) + 1;
     const size_t o_sv = L.take<uint64_t>(svt);
     const size_t zero_bytes = L.off;
     const size_t o_pos = L.take<uint32_t>(nn + 1);
-    DAGC_CUDA(ctx, ctx->arena.reserve(L.off));
-    arena_wait(ctx, s);
-    dag_ready_wait(d, s);
     char* b = static_cast<char*>(ctx->arena.base);
     CallHeader* h = reinterpret_cast<CallHeader*>(b + o_hdr);
     uint32_t* pos = reinterpret_cast<uint32_t*>(b + o_pos);
     DAGC_CUDA(ctx, cudaMemsetAsync(b, 0, zero_bytes, s));
     FinalArgs a{};
-    a.masks = d->masks;
-    a.children = d->children;
+    for (int l = 0; l < nlv; ++l) {
+        a.lv_masks[l] = src.masks[l];
+        a.lv_children[l] = src.children[l];
+    }
+    for (int l = 0; l <= nlv; ++l) a.lv_off[l] = src.off[l];
+    a.num_levels = nlv;
     a.num_nodes = nn;
-    a.leaves = d->leaves;
-    a.num_leaves = d->num_leaves;
-    a.level_offsets = d->d_level_offset;
-    a.num_levels = d->num_levels;
+    a.leaves = src.leaves;
+    a.num_leaves = src.num_leaves;
     a.word_pos = pos;
     a.d_total = &h->counts[0];
     a.status = reinterpret_cast<uint64_t*>(b + o_sv);
     a.tile_counter = &h->tile_counters[0];
     a.err = &h->err;
     a.grid_scan = grid_for(ctx->grid_scan / ctx->sms, ctx->sms, scan_tiles(nn));
-    a.grid_write = grid_for(8, ctx->sms, (nn + d->num_leaves + 255) / 256);
+    a.grid_write = grid_for(ctx->grid_write / ctx->sms, ctx->sms, (nn + src.num_leaves + 255) / 256);
     // Words: at most 1 + 8 per node and 2 per leaf. Allocating that bound
     // lets the positions and the write run back to back; the exact count
     // comes back with the error word in the call's one read-back.
-    const uint64_t bound = 9 * nn + 2 * d->num_leaves;
+    const uint64_t bound = 9 * nn + 2 * src.num_leaves;
     const bool by_bound = bound < (1ull << 32);
     uint64_t node_words = 0;
     void* w = nullptr;
@@ -1480,13 +1500,13 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
             DAGC_CUDA(ctx, cudaMemcpyAsync(ctx->h_stage, &h->counts[0], 8, cudaMemcpyDeviceToHost, s));
             DAGC_CUDA(ctx, cudaStreamSynchronize(s));
             node_words = ctx->h_stage[0];
-            if (node_words + 2 * d->num_leaves >= (1ull << 32))
+            if (node_words + 2 * src.num_leaves >= (1ull << 32))
                 return set_error(ctx, DAGC_ERR_TOO_LARGE, "final DAG exceeds 2^32 words");
         }
     } else {
         DAGC_CUDA(ctx, cudaMemsetAsync(pos, 0, 4, s));
     }
-    DAGC_CUDA(ctx, ctx->pool.alloc(&w, (by_bound ? bound : node_words + 2 * d->num_leaves) * 4, "final DAG words"));
+    DAGC_CUDA(ctx, ctx->pool.alloc(&w, (by_bound ? bound : node_words + 2 * src.num_leaves) * 4, "final DAG words"));
     a.words = static_cast<uint32_t*>(w);
     launch_final_write(a, s);
     ++ctx->launches;
@@ -1499,8 +1519,8 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
         return set_error(ctx, cuda_status(le), std::string("final: ") + cudaGetErrorString(le));
     }
     if (nn) node_words = ctx->h_stage[1];
-    const uint64_t total = node_words + 2 * d->num_leaves;
-    set_pending_bytes(ctx, DAGC_STAGE_FINAL, nn * 2 + (41 * nn + 8 * d->num_leaves) + 4 * total);
+    const uint64_t total = node_words + 2 * src.num_leaves;
+    set_pending_bytes(ctx, DAGC_STAGE_FINAL, nn * 2 + (41 * nn + 8 * src.num_leaves) + 4 * total);
     settle_profile(ctx);
     std::string msg;
     const int st = device_error_status((uint32_t)ctx->h_stage[0], msg);
@@ -1508,6 +1528,50 @@ int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, 
     *d_words = a.words;
     *n_words = total;
     return DAGC_OK;
+}
+
+int final_dag(dagc_context ctx, dagc_dag d, cudaStream_t s, uint32_t** d_words, uint64_t* n_words) {
+    *d_words = nullptr;
+    *n_words = 0;
+    if (d->num_leaves == 0) return DAGC_OK;
+    FinalSource src;
+    for (int l = 0; l < d->num_levels; ++l) {
+        src.masks.push_back(d->masks + d->level_offset[l]);
+        src.children.push_back(d->children + 8 * d->level_offset[l]);
+    }
+    src.off.assign(d->level_offset.begin(), d->level_offset.begin() + d->num_levels + 1);
+    src.leaves = d->leaves;
+    src.num_leaves = d->num_leaves;
+    DAGC_CUDA(ctx, ctx->arena.reserve(final_scratch_bytes(d->num_nodes())));
+    arena_wait(ctx, s);
+    dag_ready_wait(d, s);
+    return final_words(ctx, src, s, d_words, n_words);
+}
+
+// CreateDAG + CreateFinalDAG in one call: the words straight from the call's
+// per-level pools, with no copy of the DAG out of the arena, when the final
+// layout's scratch lies below every pool in the arena.
+int compress_from_pools(dagc_context ctx, const CreatePools& p, int nl, cudaStream_t s, uint32_t** d_words,
+                        uint64_t* n_words, bool* done) {
+    *done = false;
+    if (p.num_leaves == 0) { *done = true; *d_words = nullptr; *n_words = 0; return DAGC_OK; }
+    FinalSource src;
+    src.off.push_back(0);
+    const char* base = static_cast<const char*>(ctx->arena.base);
+    size_t lowest = reinterpret_cast<const char*>(p.leaves) - base;
+    for (int l = 0; l < nl; ++l) {
+        src.masks.push_back(p.masks[l]);
+        src.children.push_back(p.children[l]);
+        src.off.push_back(src.off.back() + p.unique[l]);
+        lowest = std::min<size_t>(lowest, reinterpret_cast<const char*>(p.masks[l]) - base);
+        lowest = std::min<size_t>(lowest, reinterpret_cast<const char*>(p.children[l]) - base);
+        lowest = std::min<size_t>(lowest, reinterpret_cast<const char*>(p.hashes[l]) - base);
+    }
+    src.leaves = p.leaves;
+    src.num_leaves = p.num_leaves;
+    if (final_scratch_bytes(src.off[nl]) > lowest) return DAGC_OK;  // would overlap a pool
+    *done = true;
+    return final_words(ctx, src, s, d_words, n_words);
 }
 
 // -------------------------------------------------------------- MergeDAGs --
@@ -2308,7 +2372,37 @@ int dagc_free_all(dagc_context ctx) {
 
 int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth, void* stream,
                   uint32_t** d_words, uint64_t* n_words) {
-    if (!d_words || !n_words) return DAGC_ERR_INVALID_ARGUMENT;
+    if (!valid_ctx(ctx) || !d_words || !n_words) return DAGC_ERR_INVALID_ARGUMENT;
+    *d_words = nullptr;
+    *n_words = 0;
+    {
+        // The pipeline, then the words from its pools (no DAG in between).
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        if (depth < 2 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [2, 21]");
+        if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+        if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
+        if (n) {
+            DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
+            cudaStream_t s = static_cast<cudaStream_t>(stream);
+            CreatePools p;
+            int st = create_pipeline(ctx, d_fragments, n, depth, s, p, nullptr, ctx->use_dedup);
+            if (st == kStatusFallback) {
+                ++ctx->fallbacks;
+                st = create_pipeline(ctx, d_fragments, n, depth, s, p, nullptr, false);
+            }
+            if (st) return st;
+            bool done = false;
+            st = compress_from_pools(ctx, p, depth - 2, s, d_words, n_words, &done);
+            if (st || done) return st;
+            // The layout's scratch would overlap the pools: copy the DAG out.
+            dagc_dag d = nullptr;
+            st = materialise(ctx, p, depth - 2, s, &d);
+            if (st) return st;
+            st = final_dag(ctx, d, s, d_words, n_words);
+            free_dag(d);
+            return st;
+        }
+    }
     dagc_dag d = nullptr;
     int st = dagc_create(ctx, d_fragments, n, depth, stream, &d);
     if (st) return st;

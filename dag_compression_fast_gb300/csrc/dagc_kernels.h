@@ -376,10 +376,18 @@ void launch_tail(const TailArgs& a, cudaStream_t s);
 
 // Final layout: word position of every node (exclusive scan of popc+1 over all
 // levels concatenated), then headers, child pointers and leaves.
+// Node levels root first: level l holds nodes [lv_off[l], lv_off[l + 1]) of
+// the concatenated numbering, their masks at lv_masks[l] and children (8 per
+// node, ids in level l + 1 or leaf ids) at lv_children[l]: slices of one
+// DAG's arrays, or a call's separate per-level pools.
+constexpr int kFinalMaxLevels = 24;
 struct FinalArgs {
-    const uint8_t* masks; const uint32_t* children; uint64_t num_nodes;
+    const uint8_t* lv_masks[kFinalMaxLevels];
+    const uint32_t* lv_children[kFinalMaxLevels];
+    uint64_t lv_off[kFinalMaxLevels + 1];
+    int num_levels;
+    uint64_t num_nodes;  // lv_off[num_levels]
     const uint64_t* leaves; uint64_t num_leaves;
-    const uint64_t* level_offsets; int num_levels;  // device, num_levels + 1 entries
     uint32_t* word_pos;  // num_nodes + 1
     uint64_t* d_total;   // exact 64-bit sum of node words
     uint32_t* words;

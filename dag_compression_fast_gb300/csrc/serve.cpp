@@ -142,18 +142,21 @@ void worker_loop(dagc_server_t* sv, int slot) {
                 cudaGetLastError();
                 st = DAGC_ERR_CUDA;
             }
-            dagc_dag dag = nullptr;
             if (!st && ev0) cudaEventRecord(ev0, stream);
-            if (!st) st = dagc_create(ctx, static_cast<const uint64_t*>(stage), r->n, r->depth, stream, &dag);
-            if (!st && r->chunk >= 0) {
-                // Keep a device copy of the chunk's DAG for the shared DAG
-                // (the merge context serialises its own calls).
-                st = dagc_dag_copy(sv->merge_ctx, dag, stream, &keep);
-            }
             uint32_t* d_words = nullptr;
             uint64_t nw = 0;
-            if (!st) st = dagc_final(ctx, dag, stream, &d_words, &nw);
-            else if (dag) dagc_dag_free(dag);
+            if (!st && r->chunk < 0) {
+                // No DAG to keep: CreateDAG + CreateFinalDAG in one call.
+                st = dagc_compress(ctx, static_cast<const uint64_t*>(stage), r->n, r->depth, stream, &d_words, &nw);
+            } else if (!st) {
+                dagc_dag dag = nullptr;
+                st = dagc_create(ctx, static_cast<const uint64_t*>(stage), r->n, r->depth, stream, &dag);
+                // Keep a device copy of the chunk's DAG for the shared DAG
+                // (the merge context serialises its own calls).
+                if (!st) st = dagc_dag_copy(sv->merge_ctx, dag, stream, &keep);
+                if (!st) st = dagc_final(ctx, dag, stream, &d_words, &nw);
+                else if (dag) dagc_dag_free(dag);
+            }
             if (!st && ev1) cudaEventRecord(ev1, stream);
             if (!st && r->h_out && nw <= r->out_cap) {
                 // Straight into the caller's buffer (pinned memory makes this

@@ -251,6 +251,22 @@ def test_compress_host_and_fused(ctx):
     assert np.array_equal(ctx.compress(codes, depth).to_numpy(), ref_words)
 
 
+@pytest.mark.parametrize("dedup", [1, 0])
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_compress_from_call_pools_bit_exact(case, dedup):
+    """dagc_compress lays the words out straight from the call's level pools
+    (no DAG copied out of the call's scratch): every input case, both dedup
+    forms, direct launches and the recorded graph, equal the oracle's words
+    and CreateDAG + CreateFinalDAG."""
+    codes, depth = CASES[case]()
+    ref = O.final_dag(O.create_dag(codes, depth, threads=8))
+    with D.Context(0) as c:
+        c.set_option(D.OPT_DEDUP, dedup)
+        for _ in range(3):  # first call, recording call, replay
+            assert np.array_equal(c.compress(codes, depth).to_numpy(), ref)
+        assert np.array_equal(c.create_final_dag(c.create_dag(codes, depth)).to_numpy(), ref)
+
+
 def test_graph_replay_matches_direct_launches(ctx):
     """Repeated calls on one device buffer replay a recorded CUDA graph; the
     result must equal the directly launched pipeline and the oracle."""
@@ -364,6 +380,9 @@ def test_soup_8192_full_size_bit_exact(soup_8192, group):
         dag = c.create_dag(codes, 13)
         assert_dag_equal(dag.to_host(), ref)
         w = c.create_final_dag(dag).to_numpy()
+        # The one-call form (words straight from the call's level pools).
+        wc = c.compress(codes, 13).to_numpy()
     assert np.array_equal(w, ref_words)
+    assert np.array_equal(wc, ref_words)
     if group == 1:
         assert np.array_equal(decode_final(w, 13), np.unique(codes))
