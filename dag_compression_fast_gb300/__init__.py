@@ -41,7 +41,7 @@ OPT_TEST_FAIL_ALLOCS = 11
 OPT_BATCH_PATH = 12
 VOXELIZE_GL = 0
 VOXELIZE_SAT = 1
-NUM_KEY_SHAPES = 8
+NUM_KEY_SHAPES = 9
 NUM_PAIR_SHAPES = 10
 NUM_SORT_SHAPES = NUM_PAIR_SHAPES
 RADIX_BITS = (8, 9, 10, 11)

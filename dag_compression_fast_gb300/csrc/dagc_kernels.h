@@ -104,7 +104,7 @@ struct SortArgs {
 // match.any, alternating, shared-memory atomicOr); each is
 // built for every digit width 8..kMaxRadixBits. Key/value sorts: 8-bit
 // digits. The autotuner and dagc options pick a shape and a width per sort.
-constexpr int kNumKeyShapes = 8;
+constexpr int kNumKeyShapes = 9;
 constexpr int kNumPairShapes = 10;
 constexpr int kNumSortShapes = kNumPairShapes;
 int sort_shape_items(int shape, bool with_values);

@@ -640,7 +640,7 @@ void launch_fill_tune_keys(uint64_t* out, uint64_t n, int lo_bit, int hi_bit, ui
 // Keys-only shapes: (items per thread, minimum CTAs per SM, match mode); each
 // is built for digits of 8, 9, 10 and 11 bits.
 #define DAGC_KEY_SHAPES(X) \
-    X(0, 16, 3, 2) X(1, 16, 2, 2) X(2, 16, 4, 2) X(3, 12, 4, 2) X(4, 16, 3, 0) X(5, 16, 3, 1) X(6, 16, 4, 3) X(7, 12, 4, 3)
+    X(0, 16, 3, 2) X(1, 16, 2, 2) X(2, 16, 4, 2) X(3, 12, 4, 2) X(4, 16, 3, 0) X(5, 16, 3, 1) X(6, 16, 4, 3) X(7, 12, 4, 3) X(8, 24, 3, 3)
 // Key/value shapes (8-bit digits).
 #define DAGC_PAIR_SHAPES(X) \
     X(0, 16, 2, 0) X(1, 16, 3, 0) X(2, 12, 3, 0) X(3, 8, 4, 0) X(4, 16, 3, 1) X(5, 16, 3, 2) X(6, 16, 2, 2) X(7, 12, 3, 2) \

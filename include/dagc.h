@@ -175,8 +175,9 @@ int dagc_last_counts(dagc_context ctx, uint64_t* out, int cap);
  * Keys-only shapes (each built for 8- to 11-bit digits): 0 = (16, 3,
  * alternate), 1 = (16, 2, alternate), 2 = (16, 4, alternate), 3 = (12, 4,
  * alternate), 4 = (16, 3, ballot), 5 = (16, 3, match), 6 = (16, 4, or),
- * 7 = (12, 4, or), where "or" finds equal digits by each lane ORing its bit
- * into its digit's word in shared memory. Key/value shapes (8-bit digits):
+ * 7 = (12, 4, or), 8 = (24, 3, or), where "or" finds equal digits by each
+ * lane ORing its bit into its digit's word in shared memory. Key/value
+ * shapes (8-bit digits):
  * 0 = (16, 2, ballot), 1 = (16, 3, ballot), 2 = (12, 3, ballot), 3 = (8, 4,
  * ballot), 4 = (16, 3, match), 5 = (16, 3, alternate), 6 = (16, 2,
  * alternate), 7 = (12, 3, alternate), 8 = (8, 4, or), 9 = (16, 3, or).
