@@ -58,6 +58,8 @@ struct CallHeader {
     uint32_t gover[kGroupMaxParts];     // its partitions that spilled past their slabs
     uint64_t gcursor[kGroupMaxParts];   // its partition starts, then ends
     uint32_t path[4];                   // [0] 1: fragments grouped by hash, 0: sorted; [1], [2] its shape
+    uint32_t leaf_sorted;               // 1: the distinct leaf masks were sorted by one CTA in shared memory
+    uint32_t pad1;
 };
 static_assert(kCntSlots <= kCntOverflow, "count slots");
 
@@ -1151,8 +1153,13 @@ int create_pipeline(dagc_context ctx, const uint64_t* d_frag, uint64_t n, int de
             launch_dedup_insert(d, s);
             ++ctx->launches;
             DAGC_LAUNCHED(ctx);
+            // Up to kSmallSortMax distinct masks: one CTA sorts them in shared
+            // memory and the grid-wide sort's kernels return at once.
+            const uint64_t* d_u = reinterpret_cast<const uint64_t*>(&d.state->u);
+            launch_small_sort(P64(Lo.o_ukey), P64(Lo.o_PL), d_u, Lo.uniq_cap, &cs.h->leaf_sorted, s);
+            ++ctx->launches;
             st = run_sort(ctx, cs, sb, P64(Lo.o_ukey), P64(Lo.o_PL), P64(Lo.o_ukey_alt), nullptr, nullptr, nullptr,
-                          false, Lo.uniq_cap, reinterpret_cast<const uint64_t*>(&d.state->u), 0, 64, 0, s);
+                          false, Lo.uniq_cap, d_u, 0, 64, 0, s, -1, -1, nullptr, &cs.h->leaf_sorted, 0u);
             if (st) return st;
             launch_dedup_assign(d, P64(Lo.o_PL), s);
             launch_dedup_map(d, s);

@@ -111,6 +111,12 @@ int sort_shape_items(int shape, bool with_values);
 // Resident CTAs per SM of a shape at a digit width (occupancy query) for grid sizing.
 int occupancy_sort_shape(int shape, bool with_values, int radix_bits = kRadixBits);
 int occupancy_sort_histogram();
+// One-CTA sort of up to kSmallSortMax 64-bit keys (all 64 bits) held in
+// shared memory, keys_in -> keys_out, when the device count *d_n fits; sets
+// *done to 1 then (a grid-wide sort gated on *done == 0 then does nothing).
+constexpr uint32_t kSmallSortMax = 12288;
+void launch_small_sort(const uint64_t* keys_in, uint64_t* keys_out, const uint64_t* d_n, uint64_t n_bound,
+                       uint32_t* done, cudaStream_t s);
 // Whether a (shape, width) plan can sort bits [lo, hi): histogram room and
 // look-back status room.
 bool sort_plan_valid(int shape, bool with_values, int radix_bits, int lo_bit, int hi_bit);

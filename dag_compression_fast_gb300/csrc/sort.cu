@@ -619,6 +619,83 @@ __global__ void copy_keys(const uint64_t* in, uint64_t* out, const uint32_t* vin
 
 // Synthetic keys for the autotuner: a SplitMix64 sequence (Steele, Lea and
 // Flood, 2014) of the index, placed in bits [lo, hi).
+// One-CTA LSD sort of at most kSmallSortMax 64-bit keys on bits [0, 64)
+// (eight 8-bit digits), the keys held in shared memory from the first load
+// to the last store: for small unique lists, where the grid-wide passes are
+// all launch and look-back latency. Each warp owns a contiguous segment of
+// the keys; per pass the warps count their segment's digits, the counts
+// become per-warp output offsets (digit start over all warps, then the
+// earlier warps' counts), and each warp places its segment row by row with
+// the digit pass's stable in-warp ranking. Runs when the device count fits,
+// and then sets *done, on which the grid-wide sort's kernels return at once.
+constexpr int kSmallSortThreads = 1024;
+constexpr int kSmallSortWarps = kSmallSortThreads / 32;
+constexpr int kSmallSortRows = 4;  // rows of 32 keys per warp and step
+struct SmallSortSmem {
+    uint64_t keys[2][kSmallSortMax];
+    uint32_t whist[kSmallSortWarps][256];
+    uint32_t scan[34];
+};
+
+__global__ void __launch_bounds__(kSmallSortThreads) small_sort(const uint64_t* in, uint64_t* out, const uint64_t* d_n,
+                                                                 uint64_t n_bound, uint32_t* done) {
+    pdl_prologue();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SmallSortSmem& S = *reinterpret_cast<SmallSortSmem*>(smem_raw);
+    const uint64_t n64 = load_n(d_n, n_bound);
+    if (n64 > kSmallSortMax) return;  // the grid-wide sort takes it
+    const uint32_t n = (uint32_t)n64;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) *done = 1u;
+    for (uint32_t i = tid; i < n; i += kSmallSortThreads) S.keys[0][i] = in[i];
+    const uint32_t seg = (n + kSmallSortWarps - 1) / kSmallSortWarps;
+    const uint32_t s0 = min(n, warp * seg), len = min(n, s0 + seg) - s0;
+    uint32_t* wh = S.whist[warp];
+    __syncthreads();
+#pragma unroll 1
+    for (int p = 0; p < 8; ++p) {
+        const uint64_t* src = S.keys[p & 1];
+        uint64_t* dst = S.keys[(p & 1) ^ 1];
+        const int shift = 8 * p;
+        for (int d = lane; d < 256; d += 32) wh[d] = 0;
+        __syncwarp();
+        for (uint32_t i = lane; i < len; i += 32) atomicAdd(&wh[(uint32_t)(src[s0 + i] >> shift) & 255u], 1u);
+        __syncthreads();
+        uint32_t tot = 0;
+        if (tid < 256)
+            for (int w = 0; w < kSmallSortWarps; ++w) tot += S.whist[w][tid];
+        uint32_t total;
+        const uint32_t start = block_exclusive_sum<uint32_t>(tid < 256 ? tot : 0u, S.scan, &total);
+        if (tid < 256) {
+            uint32_t run = start;
+            for (int w = 0; w < kSmallSortWarps; ++w) {
+                const uint32_t c = S.whist[w][tid];
+                S.whist[w][tid] = run;
+                run += c;
+            }
+        }
+        __syncthreads();
+        for (uint32_t b = 0; b < len; b += kSmallSortRows * 32) {
+            uint64_t k[kSmallSortRows];
+            uint32_t dr[kSmallSortRows];
+#pragma unroll
+            for (int j = 0; j < kSmallSortRows; ++j) {
+                const uint32_t i = b + j * 32 + lane;
+                k[j] = i < len ? src[s0 + i] : 0ull;
+                dr[j] = ((uint32_t)(k[j] >> shift) & 255u) << 16;
+            }
+            // Ranks are absolute positions (the counters start at the
+            // warp's offsets): below n <= 2^16, as the low half holds them.
+            rank_warp<8, kSmallSortRows, 2, false>(dr, wh, b, len, lane, nullptr);
+#pragma unroll
+            for (int j = 0; j < kSmallSortRows; ++j)
+                if (b + j * 32 + lane < len) dst[dr[j] & 0xFFFFu] = k[j];
+        }
+        __syncthreads();
+    }
+    for (uint32_t i = tid; i < n; i += kSmallSortThreads) out[i] = S.keys[0][i];
+}
+
 __global__ void fill_tune_keys(uint64_t* out, uint64_t n, int lo, int hi, uint64_t seed) {
     const uint64_t mask = hi - lo >= 64 ? ~0ull : ((1ull << (hi - lo)) - 1ull) << lo;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -698,6 +775,7 @@ int sort_shape_items(int shape, bool with_values) {
 constexpr size_t kMaxPassSmem = 227 * 1024;
 
 void sort_configure() {
+    cudaFuncSetAttribute(small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmallSortSmem));
     for (const KeyShape& e : kKeyShapes)
         for (const PassKernel& k : e.by_bits)
             if (k.smem <= kMaxPassSmem) cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
@@ -817,6 +895,12 @@ void launch_sort_pass(const SortArgs& a, int i, cudaStream_t s) {
     const PassKernel& k = pass_kernel(a.shape, a.with_values, p.bits);
     void* args[] = {const_cast<PassParams*>(&p)};
     launch_pdl_c((const void*)k.fn, dim3(a.grid_pass), dim3(kPassThreads), args, k.smem, s);
+}
+
+void launch_small_sort(const uint64_t* keys_in, uint64_t* keys_out, const uint64_t* d_n, uint64_t n_bound,
+                       uint32_t* done, cudaStream_t s) {
+    launch_pdl(small_sort, dim3(1), dim3(kSmallSortThreads), sizeof(SmallSortSmem), s, keys_in, keys_out, d_n, n_bound,
+               done);
 }
 
 void launch_sort(const SortArgs& a, cudaStream_t s) {
