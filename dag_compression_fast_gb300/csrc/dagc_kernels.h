@@ -137,7 +137,7 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 DAGC_HD uint32_t scan_tiles(uint64_t n) { return (uint32_t)((n + kScanTile - 1) / kScanTile); }
-// leaf_build takes 4096 sorted keys per tile (its per-tile arrays, sized by
+// leaf_build takes 8192 sorted keys per tile (its per-tile arrays, sized by
 // scan_tiles, are large enough).
 constexpr int kLeafTile = 8192;
 DAGC_HD uint32_t leaf_tiles(uint64_t n) { return (uint32_t)((n + kLeafTile - 1) / kLeafTile); }
