@@ -28,7 +28,7 @@ def test_hash_matches_reference_known_answers():
         assert O.hash_children(h) == int(kat["node_hash"], 16)
 
 
-def test_hash_published_survey_values():
+def test_hash_known_answers_of_reference_utils():
     # Values computed from the reference's src/Utils.h (MurmurHash128xN, Size 4).
     assert O.hash_children([0] * 8) == 0x8B0AE71F762F012B
     assert O.hash_children([1, 0, 0, 0, 0, 0, 0, 0]) == 0xB9F19737C11352F1
