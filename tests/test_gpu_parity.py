@@ -161,9 +161,8 @@ def test_dedup_rerun_when_unique_list_is_full():
 
 
 def test_dedup_form_is_the_one_that_runs():
-    """Three (node levels) or five (leaves) launches per deduplicated level
-    instead of a radix sort's ten or more: the launch counter tells the two
-    forms apart."""
+    """Three launches per deduplicated node level instead of a radix sort's
+    ten or more: the launch counter tells the two forms apart."""
     codes, depth = CASES["clustered_d10"]()
     launches = {}
     for form in (0, 1):
@@ -177,8 +176,8 @@ def test_dedup_form_is_the_one_that_runs():
 
 
 def test_dedup_over_a_million_distinct_leaves():
-    """More distinct leaf masks than 4096 sampled buckets of 256: the buckets
-    grow instead of the call being rerun."""
+    """Over a million distinct leaf masks: the grid-wide sort of the unique
+    list orders them without a rerun in the radix form."""
     rng = np.random.default_rng(12)
     depth = 11
     bricks = rng.choice(8 ** (depth - 2), size=1_500_000, replace=False).astype(np.uint64)
@@ -202,6 +201,30 @@ def test_dedup_many_buckets_and_skewed_leaves():
     ref = O.create_dag(codes, depth)
     with D.Context(0) as c:
         assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert c.dedup_fallbacks() == 0
+
+
+@pytest.mark.parametrize("distinct", [1, 12_287, 12_288, 12_289, 40_000])
+def test_distinct_leaf_masks_around_the_one_cta_sort(distinct):
+    """Exactly `distinct` distinct leaf masks (each brick's mask a different
+    value, some bricks sharing one): up to 12,288 of them are sorted by one
+    CTA in shared memory, more by the grid-wide sort; both equal the oracle."""
+    rng = np.random.default_rng(distinct)
+    depth = 9
+    bricks = rng.choice(8 ** (depth - 2), size=distinct + 3000, replace=False).astype(np.uint64)
+    masks = rng.choice(2**40, size=distinct, replace=False).astype(np.uint64) + np.uint64(1)
+    brick_mask = np.concatenate([masks, masks[rng.integers(0, distinct, size=3000)]])
+    codes = []
+    for k in range(40):
+        sel = (brick_mask >> np.uint64(k)) & np.uint64(1) == 1
+        codes.append((bricks[sel] << np.uint64(6)) | np.uint64(k))
+    codes = np.concatenate(codes)
+    rng.shuffle(codes)
+    ref = O.create_dag(codes, depth, threads=8)
+    assert ref.leaves.size == distinct
+    with D.Context(0) as c:
+        assert_dag_equal(c.create_dag(codes, depth).to_host(), ref)
+        assert np.array_equal(c.compress(codes, depth).to_numpy(), O.final_dag(ref))
         assert c.dedup_fallbacks() == 0
 
 
