@@ -32,7 +32,7 @@ namespace dagc {
 namespace {
 
 constexpr int kMaxDepth = 21;
-constexpr uint64_t kMaxFragments = (1ull << 30) - 1;
+constexpr uint64_t kMaxFragments = (1ull << 31) - 2;  // digit counts + 1 in the sort's 31-bit status
 constexpr int kMaxSorts = 48;
 constexpr int kMaxTileCounters = 1024;
 
@@ -2074,7 +2074,7 @@ int dagc_create(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int d
     std::lock_guard<std::mutex> lock(ctx->mu);
     *out = nullptr;
     if (depth < 2 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [2, 21]");
-    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^31 - 2 fragments");
     if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
     DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
     const int nl = depth - 2;
@@ -2112,7 +2112,7 @@ int dagc_create_batched(dagc_context ctx, const uint64_t* d_fragments, const uin
             return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "chunk Morton indices must ascend inside the grid");
     }
     const uint64_t n = h_chunk_offsets[k];
-    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^31 - 2 fragments");
     if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
     if (3 * chunk_depth + bits_for(k) > 64) return set_error(ctx, DAGC_ERR_TOO_LARGE, "composite key exceeds 64 bits");
     DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -2386,7 +2386,7 @@ int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int
         // The pipeline, then the words from its pools (no DAG in between).
         std::lock_guard<std::mutex> lock(ctx->mu);
         if (depth < 2 || depth > kMaxDepth) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "depth must be in [2, 21]");
-        if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 fragments");
+        if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^31 - 2 fragments");
         if (n && !d_fragments) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "null fragments");
         if (n) {
             DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -2855,7 +2855,7 @@ int dagc_sort_keys(dagc_context ctx, const uint64_t* d_in, uint64_t* d_out, uint
 int dagc_sort_pairs(dagc_context ctx, const uint64_t* d_keys_in, uint64_t* d_keys_out, const uint32_t* d_vals_in,
                     uint32_t* d_vals_out, uint64_t n, int lo, int hi, void* stream) {
     if (!valid_ctx(ctx) || lo < 0 || hi > 64 || lo > hi) return DAGC_ERR_INVALID_ARGUMENT;
-    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 keys");
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^31 - 2 keys");
     if (n == 0) return DAGC_OK;
     if (!d_keys_in || !d_keys_out || d_keys_in == d_keys_out) return set_error(ctx, DAGC_ERR_INVALID_ARGUMENT, "bad key buffers");
     std::lock_guard<std::mutex> lock(ctx->mu);
@@ -2881,7 +2881,7 @@ int dagc_tune_sort(dagc_context ctx, uint64_t n, int lo_bit, int hi_bit, int wit
                    int* best_radix_bits, double* best_ms, double* default_ms) {
     if (!valid_ctx(ctx) || lo_bit < 0 || hi_bit > 64 || lo_bit >= hi_bit || n == 0 || reps < 1)
         return DAGC_ERR_INVALID_ARGUMENT;
-    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^30 - 1 keys");
+    if (n > kMaxFragments) return set_error(ctx, DAGC_ERR_TOO_LARGE, "more than 2^31 - 2 keys");
     std::lock_guard<std::mutex> lock(ctx->mu);
     DAGC_CUDA(ctx, cudaSetDevice(ctx->device));
     const bool values = with_values != 0;

@@ -30,9 +30,12 @@
 namespace dagc {
 namespace {
 
-constexpr uint32_t kSAgg = 1u << 30;
-constexpr uint32_t kSInc = 2u << 30;
-constexpr uint32_t kSVal = (1u << 30) - 1;
+// Look-back status word of one digit of one tile: 0 until the tile publishes;
+// then the count + 1 in bits 0-30 (counts up to 2^31 - 2) and bit 31 set once
+// the count is the inclusive prefix over all tiles up to this one (clear: the
+// tile's own count).
+constexpr uint32_t kSInc = 1u << 31;
+constexpr uint32_t kSVal = (1u << 31) - 1;
 
 constexpr int kPassThreads = 256;
 
@@ -267,7 +270,7 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
                 ld_status<kDPT>(status + (uint64_t)(t - k) * radix + d0, st[k]);
             } else {
 #pragma unroll
-                for (int q = 0; q < kDPT; ++q) st[k][q] = kSInc;
+                for (int q = 0; q < kDPT; ++q) st[k][q] = kSInc | 1u;  // before the first tile: 0
             }
         }
         // Tiles every unfinished digit can take: up to the first unpublished
@@ -278,9 +281,9 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
             if (done >> q & 1u) continue;
 #pragma unroll
             for (int k = 0; k < kLB; ++k) {
-                const uint32_t f = st[k][q] >> 30;
-                if (f == 2) break;
-                if (f == 0) { consumed = min(consumed, k); break; }
+                const uint32_t w = st[k][q];
+                if (w >> 31) break;
+                if (w == 0) { consumed = min(consumed, k); break; }
             }
         }
 #pragma unroll
@@ -289,8 +292,8 @@ __device__ __forceinline__ void lookback_digits(const uint32_t* status, uint32_t
 #pragma unroll
             for (int k = 0; k < kLB; ++k) {
                 if (k >= consumed) break;
-                excl[q] += st[k][q] & kSVal;
-                if ((st[k][q] >> 30) == 2) { done |= 1u << q; break; }
+                excl[q] += (st[k][q] & kSVal) - 1u;
+                if (st[k][q] >> 31) { done |= 1u << q; break; }
             }
         }
         t -= consumed;
@@ -525,7 +528,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
 #pragma unroll
             for (int q = 0; q < kDPT; ++q) {
                 cnt[q] = acc[q];
-                pub[q] = (tile == 0 ? kSInc : kSAgg) | cnt[q];
+                pub[q] = (tile == 0 ? kSInc : 0u) | (cnt[q] + 1u);
                 sum += cnt[q];
             }
             if (!(p.stall_first_tile && tile == 0)) st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
@@ -574,7 +577,7 @@ __global__ void __launch_bounds__(kPassThreads, kMinCtas) onesweep_pass(PassPara
                 lookback_digits<kDPT>(p.status, kRadix, tile, d0, excl, p.err, p.spin_limit);
                 uint32_t pub[kDPT];
 #pragma unroll
-                for (int q = 0; q < kDPT; ++q) pub[q] = kSInc | (excl[q] + cnt[q]);
+                for (int q = 0; q < kDPT; ++q) pub[q] = kSInc | (excl[q] + cnt[q] + 1u);
                 st_status<kDPT>(p.status + (uint64_t)tile * kRadix + d0, pub);
             } else {
 #pragma unroll

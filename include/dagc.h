@@ -11,8 +11,9 @@
  * code; dagc_last_error() gives the message of the last failure on a context.
  * The library never aborts or traps.
  *
- * Limits: depth in [2, 21] (3 * depth <= 64 code bits), fewer than 2^30
- * fragments per call, fewer than 2^32 words in a final DAG.
+ * Limits: depth in [2, 21] (3 * depth <= 64 code bits), at most 2^31 - 2
+ * fragments per call (the reference's int32 counts allow 2^31 - 1), fewer
+ * than 2^32 words in a final DAG.
  */
 #ifndef DAGC_H
 #define DAGC_H

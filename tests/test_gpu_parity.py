@@ -39,6 +39,28 @@ def test_sort_keys_matches_stable_numpy(ctx, n, lo, hi):
     assert np.array_equal(out, expect)
 
 
+def test_sort_keys_past_2_30_keys(ctx):
+    """1.2e9 keys, more than 2^30: the digit passes' look-back prefixes pass
+    2^30 (a count + 1 in 31 bits); the result equals torch's stable sort on
+    the same bits."""
+    import torch
+    n = 1_200_000_000
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    k = torch.randint(0, 2**62, (n,), dtype=torch.int64, device="cuda", generator=g)
+    out = ctx.sort_keys(k, 0, 32)
+    order = torch.sort(k & 0xFFFFFFFF, stable=True).indices
+    assert torch.equal(out, k[order])
+
+
+def test_key_count_limit(ctx):
+    """At most 2^31 - 2 keys (fragments) per call, checked before any
+    pointer: one more is TOO_LARGE, the limit itself passes the size check."""
+    L = D.lib()
+    assert L.dagc_sort_keys(ctx.handle, None, None, 2**31 - 1, 0, 64, None) == D.ERR_TOO_LARGE
+    assert L.dagc_sort_keys(ctx.handle, None, None, 2**31 - 2, 0, 64, None) == D.ERR_INVALID_ARGUMENT
+
+
 @pytest.mark.parametrize("n", [1, 5000, 300_001])
 def test_sort_pairs_iota_is_stable_permutation(ctx, n):
     rng = np.random.default_rng(n)
