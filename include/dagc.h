@@ -157,8 +157,9 @@ int dagc_free_all(dagc_context ctx);
 int dagc_compress_host(dagc_context ctx, const uint64_t* h_fragments, uint64_t n, int depth,
                        void* stream, uint32_t* h_words, uint64_t capacity, uint64_t* n_words);
 
-/* Fused device path: CreateDAG + CreateFinalDAG without materialising the
- * intermediate DAG. Same result as dagc_create followed by dagc_final. */
+/* Fused device path: CreateDAG + CreateFinalDAG in one call, the words laid
+ * out straight from the call's per-level scratch (no intermediate DAG is
+ * allocated or copied). Same result as dagc_create followed by dagc_final. */
 int dagc_compress(dagc_context ctx, const uint64_t* d_fragments, uint64_t n, int depth,
                   void* stream, uint32_t** d_words, uint64_t* n_words);
 
